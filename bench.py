@@ -1,0 +1,471 @@
+#!/usr/bin/env python
+"""Two-qubit gate + truncated-SVD updates per second at chi = 1024 on one GB300.
+
+Workload (one step = one update of one bond): theta = A.B with A, B of shape
+(1024, 2, 1024); theta's singular spectrum is 0.97^k normalised to unit norm
+(A = Q1[:, :chi] diag(s), B = Q2[:, :chi]^H with Q1, Q2 from QR of seeded
+complex Gaussian 2048 x 2048 matrices); a seeded Haar-random gate on the two
+physical legs; truncation by the tail rule at cutoff 1e-6 and chi_max = 1024.
+Storage complex64, the mixed-precision ("chosen") mode.  Beside it the plain
+FP64 GPU path and the cuSOLVER FP64 cross-check are timed on the same inputs.
+
+`value` is updates/s with the inputs resident in HBM (each step clones the
+resident input MPS on the device, flushes L2 by writing a 256 MiB buffer and
+runs the update); `e2e` is the same metric through the host-buffer API
+(pinned host arrays uploaded, updated, downloaded every step).
+
+Multi-GPU: replicas only (one independent bond stream per GPU, no collective
+on the data path); value = all ranks' updates / max-over-ranks time.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+CHI = 1024
+CUTOFF = 1e-6
+DECAY = 0.97
+PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
+# FP64 / FP32 FMA throughput of this machine's GB300, measured by the project's
+# FMA-loop probe (MEASURED_PEAKS.json has HBM and bf16 only).
+FP64_PEAK_TFLOPS = 1.199
+FP32_PEAK_TFLOPS = 70.11
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--chi", type=int, default=CHI)
+    ap.add_argument("--plain-steps", type=int, default=1)
+    ap.add_argument("--no-baselines", action="store_true", help="skip the plain FP64 / cuSOLVER / CPU legs")
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------------------
+# inputs
+# ---------------------------------------------------------------------------
+
+def decay_pair(chi: int, seed: int):
+    rng = np.random.default_rng(seed)
+    n = 2 * chi
+    g1 = (rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))) / math.sqrt(2)
+    g2 = (rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))) / math.sqrt(2)
+    q1, _ = np.linalg.qr(g1)
+    q2, _ = np.linalg.qr(g2)
+    s = DECAY ** np.arange(chi, dtype=np.float64)
+    s /= np.linalg.norm(s)
+    a = (q1[:, :chi] * s[None, :]).reshape((chi, 2, chi), order="F")
+    b = q2[:, :chi].conj().T.reshape((chi, 2, chi), order="F")
+    return a, b, s
+
+
+def haar(rng):
+    z = (rng.standard_normal((4, 4)) + 1j * rng.standard_normal((4, 4))) / math.sqrt(2)
+    q, r = np.linalg.qr(z)
+    d = np.diag(r)
+    return q * (d / np.abs(d))[None, :]
+
+
+# ---------------------------------------------------------------------------
+# clocks
+# ---------------------------------------------------------------------------
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_bench_{os.getpid()}.csv")
+
+    def start(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.fh,
+                                         stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.fh.close()
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append((float(parts[1]), float(parts[2]), parts[5:9]))
+            except ValueError:
+                continue
+        if not rows:
+            return None
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for _, _, fl in rows for i, f in enumerate(fl) if f.lower() == "active"})
+        return {"sm_mhz": statistics.median(r[0] for r in rows), "sm_max_mhz": max(r[1] for r in rows),
+                "reasons": reasons, "samples": len(rows)}
+
+
+# ---------------------------------------------------------------------------
+# distributed plumbing (replicas only)
+# ---------------------------------------------------------------------------
+
+class Dist:
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as dist
+            dist.init_process_group("gloo")
+            self.dist = dist
+
+    def barrier(self):
+        if self.world > 1:
+            self.dist.barrier()
+
+    def max(self, x: float) -> float:
+        if self.world == 1:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, x: float) -> float:
+        if self.world == 1:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.world > 1:
+            self.dist.destroy_process_group()
+
+
+# ---------------------------------------------------------------------------
+# the engine arm
+# ---------------------------------------------------------------------------
+
+def load_engine():
+    import __graft_entry__ as g
+    return g.load_package()
+
+
+def load_rank_model(eng):
+    p = os.path.join(ROOT, "qaintensor.jl_gb300", "rank_model_params.npy")
+    if os.path.exists(p):
+        eng.set_rank_params(np.load(p), enable=True)
+        return p
+    return None
+
+
+def run_updates(eng, templates, gates, steps, flush, spectra):
+    """steps updates; returns (device ms, list of stats)."""
+    stats = []
+    eng.sync()
+    eng.timer_record(0)
+    for i in range(steps):
+        flush()
+        m = templates[i % len(templates)].clone()
+        stats.append(m.apply_2q(gates[i % len(gates)], 1))
+        m.free()
+    eng.timer_record(1)
+    return eng.timer_elapsed(0, 1), stats
+
+
+def flop_model(chi, stats):
+    """Algorithmic real flops of one update (see the measurement notes):
+    contraction 8*(2chi)*chi*(2chi), gate 8*16*chi^2, and the SVD part."""
+    n = 2 * chi
+    w_c = 8.0 * n * chi * n + 128.0 * chi * chi
+    return w_c
+
+
+def bench_ours(args, dist: Dist):
+    qt = load_engine()
+    dev = dist.local
+    chi = args.chi
+    seeds = [1001 + 2 * dist.rank, 1002 + 2 * dist.rank]
+    pairs = [decay_pair(chi, s) for s in seeds]
+    rng = np.random.default_rng(77 + dist.rank)
+    gates = [haar(rng) for _ in range(max(8, args.steps + args.warmup))]
+
+    eng = qt.Engine(mode="chosen", cutoff=CUTOFF, chi_max=chi, device=dev)
+    model_path = load_rank_model(eng)
+    templates = []
+    for a, b, s in pairs:
+        t = eng.mps([a.astype(np.complex64), b.astype(np.complex64)], dtype=np.complex64)
+        t.set_bond_spectrum(1, s)
+        templates.append(t)
+    flush = eng.l2_flush
+    # warm-up
+    for i in range(args.warmup):
+        m = templates[i % 2].clone()
+        m.apply_2q(gates[i], 1)
+        m.free()
+    dist.barrier()
+    eng.sync()
+    clocks = ClockSampler(dev)
+    clocks.start()
+    l0 = eng.launches
+    ms, stats = run_updates(eng, templates, gates[args.warmup:], args.steps, flush, None)
+    launches = eng.launches - l0
+    clk = clocks.stop()
+    dist.barrier()
+    ms_max = dist.max(ms)
+    total_updates = dist.sum(args.steps)
+    value = total_updates / (ms_max / 1e3)
+
+    # per-kernel device times over the same workload (events around every launch)
+    eng.profile_enable(True)
+    run_updates(eng, templates, gates[args.warmup:], min(args.steps, 3), flush, None)
+    prof = eng.profile_collect()
+    eng.profile_enable(False)
+
+    out = {"value": value, "ms": ms_max, "stats": stats, "launches": launches, "clocks": clk, "profile": prof,
+           "model": model_path}
+
+    # end-to-end through the host-buffer API
+    a64 = [eng.pinned_empty((chi, 2, chi), np.complex64) for _ in range(2)]
+    b64 = [eng.pinned_empty((chi, 2, chi), np.complex64) for _ in range(2)]
+    for j, (a, b, _) in enumerate(pairs):
+        a64[j][...] = a
+        b64[j][...] = b
+    outA = eng.pinned_empty((chi, 2, chi), np.complex64)
+    outB = eng.pinned_empty((chi, 2, chi), np.complex64)
+    h2d = d2h = 0
+    e2e_steps = max(2, min(args.steps, 5))
+    dist.barrier()
+    t0 = time.perf_counter()
+    for i in range(e2e_steps):
+        j = i % 2
+        m = eng.mps([a64[j], b64[j]], dtype=np.complex64)
+        m.set_bond_spectrum(1, pairs[j][2])
+        st = m.apply_2q(gates[args.warmup + i], 1)
+        k = st["rank"]
+        oa = np.ndarray((chi, 2, k), dtype=np.complex64, buffer=outA, order="F")
+        ob = np.ndarray((k, 2, chi), dtype=np.complex64, buffer=outB, order="F")
+        m.download_into(1, oa)
+        m.download_into(2, ob)
+        m.free()
+        h2d += a64[j].nbytes + b64[j].nbytes
+        d2h += oa.nbytes + ob.nbytes
+    t1 = time.perf_counter()
+    e2e_s = dist.max(t1 - t0)
+    out["e2e"] = {"value": dist.sum(e2e_steps) / e2e_s, "unit": "updates/s", "h2d_bytes_per_step": h2d // e2e_steps,
+                  "d2h_bytes_per_step": d2h // e2e_steps}
+
+    # accuracy of one chosen update against the engine's exact FP64 path
+    out["accuracy"] = accuracy_check(qt, dev, pairs[0], gates[args.warmup])
+
+    # plain FP64 GPU and cuSOLVER FP64 denominators (same inputs, fewer steps)
+    if not args.no_baselines:
+        out["plain"] = time_mode(qt, dev, pairs, gates[args.warmup:], "plain", args.plain_steps)
+        out["cusolver"] = time_mode(qt, dev, pairs, gates[args.warmup:], "cusolver", args.plain_steps)
+    for t in templates:
+        t.free()
+    eng.close()
+    return out
+
+
+def time_mode(qt, dev, pairs, gates, mode, steps):
+    eng = qt.Engine(mode=mode, cutoff=CUTOFF, chi_max=CHI, device=dev)
+    tmpl = [eng.mps([a, b], dtype=np.complex128) for a, b, _ in pairs]
+    m = tmpl[0].clone()
+    m.apply_2q(gates[0], 1)  # warm-up
+    m.free()
+    ms, stats = run_updates(eng, tmpl, gates[1:], steps, lambda: None, None)
+    for t in tmpl:
+        t.free()
+    eng.close()
+    return {"updates_per_s": steps / (ms / 1e3), "ms_per_update": ms / steps, "rank": stats[0]["rank"],
+            "sweeps": stats[0]["sweeps"]}
+
+
+def accuracy_check(qt, dev, pair, gate):
+    a, b, s = pair
+    chi = a.shape[0]
+    ex = qt.Engine(mode="plain", cutoff=CUTOFF, chi_max=chi, device=dev)
+    ch = qt.Engine(mode="chosen", cutoff=CUTOFF, chi_max=chi, device=dev)
+    load_rank_model(ch)
+    m1 = ex.mps([a.astype(np.complex64).astype(np.complex128), b.astype(np.complex64).astype(np.complex128)])
+    st1 = m1.apply_2q(gate, 1)
+    m2 = ch.mps([a.astype(np.complex64), b.astype(np.complex64)], dtype=np.complex64)
+    m2.set_bond_spectrum(1, s)
+    st2 = m2.apply_2q(gate, 1)
+    A1, B1 = m1.site(1), m1.site(2)
+    A2, B2 = m2.site(1).astype(np.complex128), m2.site(2).astype(np.complex128)
+    t1 = A1.reshape((2 * chi, -1), order="F") @ B1.reshape((B1.shape[0], -1), order="F")
+    t2 = A2.reshape((2 * chi, -1), order="F") @ B2.reshape((B2.shape[0], -1), order="F")
+    # exact theta' in FP64 from the same complex64 inputs
+    a64, b64 = a.astype(np.complex64).astype(np.complex128), b.astype(np.complex64).astype(np.complex128)
+    th = a64.reshape((2 * chi, chi), order="F") @ b64.reshape((chi, 2 * chi), order="F")
+    g4 = np.asarray(gate).reshape((2, 2, 2, 2), order="F")
+    th = np.einsum("pqrs,arsb->apqb", g4, th.reshape((chi, 2, 2, chi), order="F")).reshape((2 * chi, 2 * chi), order="F")
+    err_exact = np.linalg.norm(th - t1)
+    err_chosen = np.linalg.norm(th - t2)
+    # <Z_1> and <Z_2> of the two-site state (theta'/||theta'||)
+    def zexp(t, which):
+        t4 = t.reshape((chi, 2, 2, chi), order="F")
+        w = np.sum(np.abs(t4) ** 2, axis=(0, 3))
+        z = np.array([1.0, -1.0])
+        return float((z @ w.sum(1)) / w.sum()) if which == 1 else float((w.sum(0) @ z) / w.sum())
+    dz = max(abs(zexp(t1, 1) - zexp(t2, 1)), abs(zexp(t1, 2) - zexp(t2, 2)))
+    for o in (m1, m2):
+        o.free()
+    ex.close()
+    ch.close()
+    return {"rank_exact": st1["rank"], "rank_chosen": st2["rank"], "predicted_rank": st2["predicted_rank"],
+            "sketch_size": st2["sketch_size"], "fallback": st2["fallback"],
+            "trunc_err_exact": err_exact, "trunc_err_chosen": err_chosen,
+            "trunc_err_ratio": err_chosen / err_exact if err_exact > 0 else None, "dZ_vs_exact": dz}
+
+
+def cpu_baseline(chi, pair, gate):
+    """The oracle (numpy/scipy gesdd on OpenBLAS) on one update of the same workload."""
+    import oracle
+    a, b, _ = pair
+    t0 = time.perf_counter()
+    n = 0
+    while True:
+        oracle.apply_2q([a.copy(), b.copy()], gate, 1, CUTOFF, chi)
+        n += 1
+        if time.perf_counter() - t0 > 10.0 or n >= 3:
+            break
+    dt = time.perf_counter() - t0
+    return {"value": n / dt, "unit": "updates/s", "cores": os.cpu_count(), "kind": "port",
+            "sample": f"{n} update(s) of the chi={chi} workload (numpy gesdd, OpenBLAS on all host threads)"}
+
+
+# ---------------------------------------------------------------------------
+# roofline
+# ---------------------------------------------------------------------------
+
+def roofline(prof, chi, stats, steps_profiled):
+    if not prof:
+        return None
+    name, launches, ms = prof[0]
+    kind = name
+    # algorithmic work per launch of the dominant kernel
+    if "jacobi_pair_kernel" in name:
+        # a round of the one-sided block Jacobi: every CTA forms one 16-column
+        # Gram (FP64: 8 flops per complex MAC over the rows of the matrix)
+        rows = 2 * chi
+        l = stats[0]["sketch_size"] or 2 * chi
+        pairs = max(1, (l // 8 + (l // 8) % 2) // 2)
+        work = pairs * 8.0 * rows * (16 * 17 / 2)
+        peak, unit, bound = FP64_PEAK_TFLOPS, "TFLOP/s", "fp64"
+        achieved = work / (ms / launches * 1e-3) / 1e12
+    elif "cgemm_kernel" in name or "theta_gate" in name:
+        return {"kernel": name, "note": "per-launch shapes vary; see profiles/"}
+    else:
+        return {"kernel": name}
+    return {"kernel": kind, "bound": bound, "achieved": achieved, "peak": peak, "unit": unit,
+            "frac": achieved / peak, "traffic": None, "peak_source": "project FMA-loop probe (not in MEASURED_PEAKS.json)"}
+
+
+# ---------------------------------------------------------------------------
+# the reference arm: the CPU restatement of the reference path
+# ---------------------------------------------------------------------------
+
+def bench_reference(args, dist: Dist):
+    if dist.rank != 0:
+        return None
+    import oracle
+    chi = args.chi
+    pair = decay_pair(chi, 1001)
+    rng = np.random.default_rng(77)
+    gates = [haar(rng) for _ in range(8)]
+    steps = max(1, min(args.steps, 2))
+    warm = min(args.warmup, 1)
+    for i in range(warm):
+        oracle.apply_2q([pair[0].copy(), pair[1].copy()], gates[i], 1, CUTOFF, chi)
+    t0 = time.perf_counter()
+    for i in range(steps):
+        oracle.apply_2q([pair[0].copy(), pair[1].copy()], gates[warm + i], 1, CUTOFF, chi)
+    dt = time.perf_counter() - t0
+    v = steps / dt
+    return {"metric": "2q gate+SVD updates/s at chi=1024", "value": v, "unit": "updates/s", "n_gpus": 0,
+            "steps": steps, "warmup": warm, "ms_per_step": dt / steps * 1e3, "higher_is_better": True,
+            "impl": "reference", "dtype": "c128", "data": "synthetic",
+            "config": {"workload": f"single-bond update chi={chi}, spectrum {DECAY}^k, Haar gate, cutoff {CUTOFF}"},
+            "cpu_baseline": {"value": v, "unit": "updates/s", "cores": os.cpu_count(), "kind": "port",
+                             "sample": f"{steps} timed update(s) at chi={chi} (steps capped at 2 to bound the run)"},
+            "e2e": {"value": v, "unit": "updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "vs_baseline": None}
+
+
+def main():
+    args = parse()
+    dist = Dist()
+    if args.impl == "reference":
+        line = bench_reference(args, dist)
+        if line is not None:
+            print(json.dumps(line))
+        dist.close()
+        return
+    res = bench_ours(args, dist)
+    if dist.rank == 0:
+        stats = res["stats"]
+        prof = res["profile"]
+        line = {
+            "metric": "2q gate+SVD updates/s at chi=1024 (mixed-precision + learned-rank path)",
+            "value": res["value"], "unit": "updates/s", "n_gpus": dist.world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": res["ms"] / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "c64 storage, fp32-level products, fp64 small SVD",
+            "data": "synthetic (seeded decaying-spectrum theta, Haar gates)",
+            "config": {"workload": f"single-bond 2q gate+SVD update, theta (chi,2,2,chi) chi={args.chi}, "
+                                   f"spectrum {DECAY}^k unit norm, Haar gate, cutoff {CUTOFF}, chi_max {args.chi}",
+                       "parallelism": f"replicas x{dist.world}", "l2": "256 MiB device write between steps",
+                       "rank_model": res["model"]},
+            "gpu_launches": res["launches"],
+            "clocks": res["clocks"],
+            "e2e": res["e2e"],
+            "update_stats": {k: stats[0][k] for k in ("rank", "predicted_rank", "sketch_size", "fallback", "sweeps")},
+            "accuracy": res["accuracy"],
+            "kernels": [{"name": n, "launches": c, "ms": round(t, 3)} for n, c, t in prof[:8]],
+        }
+        line["roofline"] = roofline(prof, args.chi, stats, min(args.steps, 3))
+        if "plain" in res:
+            line["plain_fp64_gpu"] = res["plain"]
+            line["cusolver_fp64_gpu"] = res["cusolver"]
+            best = max(res["plain"]["updates_per_s"], res["cusolver"]["updates_per_s"])
+            line["speedup_vs_best_plain_fp64"] = res["value"] / best
+            pair = decay_pair(args.chi, 1001)
+            rng = np.random.default_rng(77)
+            line["cpu_baseline"] = cpu_baseline(args.chi, pair, haar(rng))
+        print(json.dumps(line))
+    dist.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,204 @@
+/*
+ * qaintensor_gb300.h -- C ABI of the GB300 (sm_103a) engine for the
+ * Qaintensor.jl contraction + truncated-SVD hot path.
+ *
+ * Conventions (all entry points):
+ *   - Tensors are column-major (Julia order) with interleaved complex
+ *     elements: QT_C64 = {float re, im}, QT_C128 = {double re, im}.
+ *   - An MPS site is (chiL, 2, chiR); the first site of an open chain may have
+ *     chiL = 1 and the last chiR = 1 (the memory of the reference's 2-leg end
+ *     tensors (2, chi) / (chi, 2)).
+ *   - Site numbers at this ABI are 0-based; the Julia/Python layers add 1.
+ *   - A 4x4 gate G is complex128, column-major, interleaved; its matrix index
+ *     is b_i + 2 b_{i+1} for wires (i, i+1): wire i is the fastest bit
+ *     (src/decompose.jl:16-31, src/mpo.jl:41-57 -- the gate acts on the input legs).
+ *   - Every call returns 0 (QT_OK) or a negative qt_status; no exception
+ *     crosses the ABI.  qt_last_error() gives the message of the last failure
+ *     on that handle.  The reference's own messages are returned verbatim
+ *     where the reference has one.
+ *   - A handle owns one CUDA stream on one device and is not thread-safe;
+ *     calls are synchronous from the caller's view.
+ */
+#ifndef QAINTENSOR_GB300_H
+#define QAINTENSOR_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define QT_ABI_VERSION 1
+
+typedef enum {
+  QT_OK = 0,
+  QT_EINVAL_ERR_NEG = -1,      /* "Error must be positive"            src/svd.jl:9, src/mps.jl:192 */
+  QT_EDIM_MISMATCH = -2,       /* "Dimensions of contraction legs do not match"  src/svd.jl:16 */
+  QT_ENOMEM = -3,              /* device allocation failed */
+  QT_ECUDA = -4,               /* a CUDA runtime call failed */
+  QT_ETIMEOUT = -5,            /* a bounded device-side wait gave up */
+  QT_ENUMERIC = -6,            /* non-finite input or a factorisation broke down */
+  QT_EFALLBACK_FAILED = -7,    /* the exact fallback itself failed */
+  QT_EINVAL = -8,              /* bad argument (null pointer, bad dtype, bad mode) */
+  QT_EPERIODIC = -9,           /* "Function doesn't support periodic boundary conditions for now" src/mps.jl:195 */
+  QT_EBOUNDS = -10,            /* site index out of range (BoundsError in src/switch.jl) */
+  QT_ENOTSUP = -11             /* size or mode not supported by this build */
+} qt_status;
+
+typedef enum { QT_C64 = 0, QT_C128 = 1 } qt_dtype;
+
+typedef enum {
+  QT_MODE_PLAIN = 0,     /* FP64 everywhere: FP64 GEMM + exact FP64 one-sided Jacobi SVD */
+  QT_MODE_CHOSEN = 1,    /* FP32-level products, randomized SVD sized by the rank
+                            predictor, FP64 orthogonalisation / small SVD / tail sums;
+                            exact FP64 SVD as fallback */
+  QT_MODE_CUSOLVER = 2   /* cross-check: FP64 GEMM + cuSOLVER zgesvd (library) */
+} qt_mode;
+
+typedef struct {
+  int device;              /* CUDA device ordinal */
+  int mode;                /* qt_mode used when a call passes mode < 0 */
+  double cutoff;           /* tail-norm cutoff (src/svd.jl:29-33), used when a call passes cutoff < 0 */
+  int chi_max;             /* kept-rank cap (<= 0: none), used when a call passes chi_max < 0 */
+  int oversample;          /* randomized SVD: extra probes beyond the predicted rank */
+  int power_iters;         /* randomized SVD: subspace iterations */
+  int renormalize;         /* rescale kept values to the full spectrum's norm */
+  int use_rank_model;      /* size the sketch with the learned-rank MLP when trained */
+  int max_sweeps;          /* Jacobi sweep limit */
+  double jacobi_tol;       /* Jacobi orthogonality tolerance (relative) */
+  double noise_floor;      /* chosen mode: tail norms below noise_floor*||theta|| are
+                              below the FP32-level arithmetic and are not resolved */
+  uint64_t seed;           /* sketch RNG seed */
+  int tc_gemm;             /* chosen mode: 1 = tcgen05 split-TF32x3 products, 0 = FP32 SIMT */
+} qt_config;
+
+typedef struct {
+  int rank;                /* kept rank k */
+  int rank_cutoff;         /* rank from the tail rule before chi_max */
+  int predicted_rank;      /* learned-rank prediction (-1 when unused) */
+  int sketch_size;         /* probes used (0: exact path) */
+  int fallback;            /* 1 when the chosen mode fell back to the exact SVD */
+  int sweeps;              /* Jacobi sweeps run */
+  double discarded_weight; /* sum of discarded s_i^2 over the computed spectrum */
+  double norm2;            /* sum of s_i^2 over the computed spectrum */
+  double residual;         /* chosen mode: ||theta - Q Q^H theta||_F estimate */
+} qt_update_stats;
+
+typedef struct qt_handle qt_handle;
+typedef struct qt_mps qt_mps;
+
+/* ---- handle ------------------------------------------------------------ */
+int qt_config_default(qt_config* cfg);
+int qt_create(qt_handle** out, const qt_config* cfg);
+int qt_destroy(qt_handle* h);
+const char* qt_last_error(const qt_handle* h);
+int qt_abi_version(void);
+/* Kernel launches issued by this handle since creation (a monotone counter). */
+int64_t qt_launch_count(const qt_handle* h);
+
+/* ---- measurement helpers ------------------------------------------------ */
+/* CUDA events on the handle's stream: record into slot 0..7, elapsed a -> b. */
+int qt_timer_record(qt_handle* h, int slot);
+int qt_timer_elapsed(qt_handle* h, int slot_a, int slot_b, double* ms);
+int qt_sync(qt_handle* h);
+/* Write a 256 MiB device buffer on the handle's stream (evicts the 129 MB L2). */
+int qt_l2_flush(qt_handle* h);
+/* Per-launch device time of every kernel launch while enabled (events around
+ * each launch on the handle's stream); collect aggregates by kernel name. */
+int qt_profile_enable(qt_handle* h, int on);
+int qt_profile_collect(qt_handle* h);
+int qt_profile_get(int idx, char* name, int namelen, int64_t* launches, double* total_ms);
+/* Pinned host memory for host-buffer (end-to-end) callers. */
+void* qt_host_alloc(size_t bytes);
+int qt_host_free(void* p);
+
+/* ---- dense primitives on host buffers ----------------------------------- */
+
+/* Pairwise contraction with ncon semantics: contract legs axesA[i] of A with
+ * axesB[i] of B (0-based); the result's legs are A's free legs in order, then
+ * B's.  Replaces the TensorOperations.ncon pairwise step called at
+ * src/contract.jl:257,263 (and the products of src/svd.jl:35). */
+int qt_contract_pair(qt_handle* h, int dtype,
+                     int ndA, const int64_t* dimsA, const void* A,
+                     int ndB, const int64_t* dimsB, const void* B,
+                     int ncontract, const int* axesA, const int* axesB, void* C);
+
+/* Thin SVD of the m x n matrix M truncated by the tail rule of src/svd.jl:29-33
+ * (cutoff = er) and chi_max: U (m x k), S (k), Vh (k x n).  Outputs are sized
+ * for kcap = min(m, n) columns/rows; *k receives the kept rank.  Replaces the
+ * svd() calls at src/svd.jl:26-27, src/switch.jl (svd of the swapped pair),
+ * src/mps.jl:63,73, src/mpo.jl:53,62, src/decompose.jl:26,38. */
+int qt_truncated_svd(qt_handle* h, int dtype, int64_t m, int64_t n, const void* M,
+                     double cutoff, int chi_max, int mode,
+                     void* U, double* S, void* Vh, int* k, double* discarded);
+
+/* contract_svd(T1, T2, (i1, i2); er) of src/svd.jl:7-38 (i1, i2 are 1-based,
+ * as in Julia).  out holds the free legs of T1 then of T2, column-major. */
+int qt_contract_svd(qt_handle* h, int dtype,
+                    int nd1, const int64_t* dims1, const void* T1,
+                    int nd2, const int64_t* dims2, const void* T2,
+                    int i1, int i2, double er, void* out);
+
+/* ---- device-resident MPS ------------------------------------------------ */
+
+/* dims: 3 per site (chiL, 2, chiR).  host_sites may be NULL for |0...0>
+ * (then every dim must be (1,2,1)).  The library copies the data. */
+int qt_mps_create(qt_handle* h, int nsites, const int64_t* dims,
+                  const void* const* host_sites, int dtype, qt_mps** out);
+int qt_mps_free(qt_handle* h, qt_mps* mps);
+/* Device-to-device copy of an MPS (stream-ordered; no host round trip). */
+int qt_mps_clone(qt_handle* h, const qt_mps* src, qt_mps** out);
+int qt_mps_nsites(const qt_mps* mps);
+int qt_mps_site_dims(const qt_mps* mps, int site, int64_t* dims3);
+int qt_mps_download(qt_handle* h, const qt_mps* mps, int site, void* host);
+int qt_mps_upload_site(qt_handle* h, qt_mps* mps, int site, const int64_t* dims3, const void* host);
+
+/* The two-qubit gate + truncated-SVD update on sites (site, site+1):
+ * theta = A.B, theta' = G on the input legs, SVD, tail rule + chi_max,
+ * A' = U[:, :k], B' = diag(S_k) V'[:k, :]  (src/switch.jl split convention).
+ * cutoff < 0 / chi_max < 0 / mode < 0 take the handle's configuration. */
+int qt_apply_2q(qt_handle* h, qt_mps* mps, int site, const double* G,
+                double cutoff, int chi_max, int mode, qt_update_stats* stats);
+
+/* switch!(mps, i) of src/switch.jl (function at file lines 56-94): swap the
+ * physical legs of sites (site, site+1) with an untruncated SVD split. */
+int qt_switch(qt_handle* h, qt_mps* mps, int site);
+
+/* <psi|Z_site|psi>/<psi|psi>, <psi|Z_site Z_site+1|psi>/<psi|psi> and <psi|psi>
+ * (no reference counterpart: its observables are closure networks contracted
+ * with ncon, examples/expectation_value_optimization_example.ipynb). */
+int qt_expect_z(qt_handle* h, const qt_mps* mps, int site, double* out);
+int qt_expect_zz(qt_handle* h, const qt_mps* mps, int site, double* out);
+int qt_mps_norm2(qt_handle* h, const qt_mps* mps, double* out);
+
+/* Context for the rank model: the spectrum last kept at a bond (the engine
+ * records it after every update; callers that built the MPS elsewhere may
+ * supply it) and the circuit position (layer of depth) of the next update. */
+int qt_mps_set_bond_spectrum(qt_mps* mps, int bond, const double* s, int n);
+int qt_mps_set_circuit_position(qt_mps* mps, int layer, int depth);
+
+/* ---- learned-rank model (16-64-64-1 ReLU MLP; no reference counterpart:
+ * the reference's only rank rule is src/svd.jl:29-33) -------------------- */
+int qt_rank_model_nparams(void);
+int qt_rank_model_set_logging(qt_handle* h, int on);   /* log (features, k/k_max) of plain updates */
+int64_t qt_rank_model_log_size(const qt_handle* h);
+int qt_rank_model_get_log(const qt_handle* h, float* X /* n x 16 row-major */, float* Y /* n */);
+int qt_rank_model_clear_log(qt_handle* h);
+int qt_rank_model_set_params(qt_handle* h, const float* params, int nparams, int enable);
+int qt_rank_model_get_params(const qt_handle* h, float* params, int nparams);
+int qt_rank_model_enable(qt_handle* h, int on);
+int qt_rank_model_set_margin(qt_handle* h, double margin);
+/* Adam on minibatches with the GPU forward/backward kernels; init may be NULL. */
+int qt_rank_model_train(qt_handle* h, int64_t n, const float* X, const float* Y, const float* init, int epochs,
+                        int batch, double lr, uint64_t seed, double* final_loss);
+int qt_mlp_forward(qt_handle* h, int64_t n, const float* X, float* out);
+int qt_mlp_loss_grad(qt_handle* h, int64_t n, const float* X, const float* Y, const float* params, float* grad,
+                     double* loss);
+/* The 16 features of the update of bond (site, site+1) with gate G. */
+int qt_rank_features_of(const qt_mps* mps, int site, const double* G, double cutoff, int chi_max, float* f);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* QAINTENSOR_GB300_H */

@@ -1,0 +1,528 @@
+"""Host-side mirror of Qaintensor.jl's contraction / truncated-SVD API over the
+GB300 engine's C ABI (``libqaintensor_gb300.so``, declared in
+``include/qaintensor_gb300.h``).
+
+Names, argument meaning and error messages follow the Julia entry points:
+``contract_svd(T1, T2, (i1, i2); er)`` (src/svd.jl:7-38), ``switch!``
+(src/switch.jl), and the eager two-qubit update ``apply_2q!`` that the
+engine adds on top of ``tensor_circuit!``'s gate convention.  Wire and site
+numbers are 1-based here, as in Julia; the C ABI is 0-based.
+
+There is no CPU fallback: importing works anywhere, but creating an
+``Engine`` loads the CUDA library and raises if it is missing or no GPU is
+usable.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import List, Optional, Sequence
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libqaintensor_gb300.so")
+
+QT_OK, QT_EINVAL_ERR_NEG, QT_EDIM_MISMATCH, QT_ENOMEM, QT_ECUDA, QT_ETIMEOUT, QT_ENUMERIC, \
+    QT_EFALLBACK_FAILED, QT_EINVAL, QT_EPERIODIC, QT_EBOUNDS, QT_ENOTSUP = 0, -1, -2, -3, -4, -5, -6, -7, -8, -9, -10, -11
+QT_C64, QT_C128 = 0, 1
+MODES = {"plain": 0, "chosen": 1, "cusolver": 2}
+
+# the reference's own messages for the codes that have one
+REFERENCE_MESSAGES = {
+    QT_EINVAL_ERR_NEG: "Error must be positive",                                  # src/svd.jl:9, src/mps.jl:192
+    QT_EDIM_MISMATCH: "Dimensions of contraction legs do not match",              # src/svd.jl:16
+    QT_EPERIODIC: "Function doesn't support periodic boundary conditions for now",  # src/mps.jl:195
+}
+
+
+class QaintensorError(ValueError):
+    """An error the reference raises as ErrorException(msg); ``str(e)`` is msg."""
+
+    def __init__(self, msg: str, code: int = QT_EINVAL):
+        super().__init__(msg)
+        self.code = code
+
+
+class QaintensorBoundsError(IndexError):
+    """Out-of-range site (the reference's BoundsError)."""
+
+
+class EngineError(RuntimeError):
+    """A device-side failure (CUDA, allocation, numerics)."""
+
+    def __init__(self, msg: str, code: int):
+        super().__init__(msg)
+        self.code = code
+
+
+class QtConfig(C.Structure):
+    _fields_ = [("device", C.c_int), ("mode", C.c_int), ("cutoff", C.c_double), ("chi_max", C.c_int),
+                ("oversample", C.c_int), ("power_iters", C.c_int), ("renormalize", C.c_int),
+                ("use_rank_model", C.c_int), ("max_sweeps", C.c_int), ("jacobi_tol", C.c_double),
+                ("noise_floor", C.c_double), ("seed", C.c_uint64), ("tc_gemm", C.c_int)]
+
+
+class QtUpdateStats(C.Structure):
+    _fields_ = [("rank", C.c_int), ("rank_cutoff", C.c_int), ("predicted_rank", C.c_int), ("sketch_size", C.c_int),
+                ("fallback", C.c_int), ("sweeps", C.c_int), ("discarded_weight", C.c_double),
+                ("norm2", C.c_double), ("residual", C.c_double)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+_lib = None
+
+
+def library() -> C.CDLL:
+    """Load the engine library (once).  Raises when it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"CUDA engine not built: {LIB_PATH} is missing (run __graft_entry__.build())")
+    lib = C.CDLL(LIB_PATH)
+    P, I, D, L = C.c_void_p, C.c_int, C.c_double, C.c_int64
+    sig = {
+        "qt_config_default": (I, [C.POINTER(QtConfig)]),
+        "qt_create": (I, [C.POINTER(P), C.POINTER(QtConfig)]),
+        "qt_destroy": (I, [P]),
+        "qt_last_error": (C.c_char_p, [P]),
+        "qt_abi_version": (I, []),
+        "qt_launch_count": (L, [P]),
+        "qt_contract_pair": (I, [P, I, I, C.POINTER(L), P, I, C.POINTER(L), P, I, C.POINTER(I), C.POINTER(I), P]),
+        "qt_truncated_svd": (I, [P, I, L, L, P, D, I, I, P, C.POINTER(D), P, C.POINTER(I), C.POINTER(D)]),
+        "qt_contract_svd": (I, [P, I, I, C.POINTER(L), P, I, C.POINTER(L), P, I, I, D, P]),
+        "qt_mps_create": (I, [P, I, C.POINTER(L), C.POINTER(P), I, C.POINTER(P)]),
+        "qt_mps_free": (I, [P, P]),
+        "qt_mps_nsites": (I, [P]),
+        "qt_mps_site_dims": (I, [P, I, C.POINTER(L)]),
+        "qt_mps_download": (I, [P, P, I, P]),
+        "qt_mps_upload_site": (I, [P, P, I, C.POINTER(L), P]),
+        "qt_apply_2q": (I, [P, P, I, C.POINTER(D), D, I, I, C.POINTER(QtUpdateStats)]),
+        "qt_switch": (I, [P, P, I]),
+        "qt_expect_z": (I, [P, P, I, C.POINTER(D)]),
+        "qt_expect_zz": (I, [P, P, I, C.POINTER(D)]),
+        "qt_mps_norm2": (I, [P, P, C.POINTER(D)]),
+        "qt_rank_model_set_logging": (I, [P, I]),
+        "qt_rank_model_log_size": (L, [P]),
+        "qt_rank_model_get_log": (I, [P, P, P]),
+        "qt_rank_model_clear_log": (I, [P]),
+        "qt_rank_model_set_params": (I, [P, P, I, I]),
+        "qt_rank_model_get_params": (I, [P, P, I]),
+        "qt_rank_model_enable": (I, [P, I]),
+        "qt_rank_model_set_margin": (I, [P, D]),
+        "qt_rank_model_nparams": (I, []),
+        "qt_rank_model_train": (I, [P, L, P, P, P, I, I, D, C.c_uint64, C.POINTER(D)]),
+        "qt_mlp_forward": (I, [P, L, P, P]),
+        "qt_mlp_loss_grad": (I, [P, L, P, P, P, P, C.POINTER(D)]),
+        "qt_rank_features_of": (I, [P, I, C.POINTER(D), D, I, P]),
+        "qt_mps_set_bond_spectrum": (I, [P, I, C.POINTER(D), I]),
+        "qt_mps_set_circuit_position": (I, [P, I, I]),
+        "qt_mps_clone": (I, [P, P, C.POINTER(P)]),
+        "qt_timer_record": (I, [P, I]),
+        "qt_timer_elapsed": (I, [P, I, I, C.POINTER(D)]),
+        "qt_sync": (I, [P]),
+        "qt_l2_flush": (I, [P]),
+        "qt_profile_enable": (I, [P, I]),
+        "qt_profile_collect": (I, [P]),
+        "qt_profile_get": (I, [I, C.c_char_p, I, C.POINTER(L), C.POINTER(D)]),
+        "qt_host_alloc": (P, [C.c_size_t]),
+        "qt_host_free": (I, [P]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def _ptr(a: np.ndarray) -> C.c_void_p:
+    return C.c_void_p(a.ctypes.data)
+
+
+def _dtype_code(dt) -> int:
+    dt = np.dtype(dt)
+    if dt == np.complex64:
+        return QT_C64
+    if dt == np.complex128:
+        return QT_C128
+    raise QaintensorError(f"unsupported dtype {dt}: use complex64 or complex128")
+
+
+def _np_dtype(code: int):
+    return np.complex64 if code == QT_C64 else np.complex128
+
+
+def _gate_arg(g) -> C.Array:
+    g = np.asfortranarray(np.asarray(g, dtype=np.complex128))
+    if g.shape != (4, 4):
+        raise QaintensorError("a two-qubit gate must be a 4x4 matrix")
+    flat = np.empty(32, dtype=np.float64)
+    gf = g.reshape(-1, order="F")
+    flat[0::2], flat[1::2] = gf.real, gf.imag
+    return (C.c_double * 32)(*flat)
+
+
+class Engine:
+    """One engine handle: one CUDA stream on one device (not thread-safe)."""
+
+    def __init__(self, mode: str = "plain", cutoff: float = 0.0, chi_max: int = 0, device: int = 0, **kw):
+        lib = library()
+        cfg = QtConfig()
+        lib.qt_config_default(C.byref(cfg))
+        cfg.device, cfg.mode, cfg.cutoff, cfg.chi_max = device, MODES[mode], cutoff, chi_max
+        for k, v in kw.items():
+            if not hasattr(cfg, k):
+                raise TypeError(f"unknown engine option {k}")
+            setattr(cfg, k, v)
+        self._lib = lib
+        self._h = C.c_void_p()
+        rc = lib.qt_create(C.byref(self._h), C.byref(cfg))
+        if rc != QT_OK:
+            raise EngineError(f"qt_create failed with status {rc} (is a CUDA GPU visible?)", rc)
+        self.config = cfg
+
+    # -- plumbing -------------------------------------------------------------
+    def _check(self, rc: int):
+        if rc == QT_OK:
+            return
+        msg = self._lib.qt_last_error(self._h).decode()
+        if rc in REFERENCE_MESSAGES:
+            raise QaintensorError(REFERENCE_MESSAGES[rc], rc)
+        if rc == QT_EBOUNDS:
+            raise QaintensorBoundsError(msg)
+        if rc in (QT_EINVAL,):
+            raise QaintensorError(msg, rc)
+        raise EngineError(f"{msg} (status {rc})", rc)
+
+    def close(self):
+        if self._h:
+            self._lib.qt_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def launches(self) -> int:
+        """Kernel launches issued by this handle so far."""
+        return int(self._lib.qt_launch_count(self._h))
+
+    # -- measurement ----------------------------------------------------------
+    def timer_record(self, slot: int):
+        """Record CUDA event `slot` (0..7) on the handle's stream."""
+        self._check(self._lib.qt_timer_record(self._h, slot))
+
+    def timer_elapsed(self, a: int, b: int) -> float:
+        ms = C.c_double()
+        self._check(self._lib.qt_timer_elapsed(self._h, a, b, C.byref(ms)))
+        return ms.value
+
+    def sync(self):
+        self._check(self._lib.qt_sync(self._h))
+
+    def l2_flush(self):
+        """Write 256 MiB on the device (evicts L2) on the handle's stream."""
+        self._check(self._lib.qt_l2_flush(self._h))
+
+    def profile_enable(self, on: bool = True):
+        self._check(self._lib.qt_profile_enable(self._h, int(on)))
+
+    def profile_collect(self):
+        """[(kernel name, launches, total device ms)] of the launches recorded
+        since profile_enable(True), longest first."""
+        n = self._lib.qt_profile_collect(self._h)
+        if n < 0:
+            self._check(n)
+        out = []
+        buf = C.create_string_buffer(256)
+        for i in range(n):
+            cnt, ms = C.c_int64(), C.c_double()
+            self._lib.qt_profile_get(i, buf, 256, C.byref(cnt), C.byref(ms))
+            out.append((buf.value.decode(), cnt.value, ms.value))
+        return sorted(out, key=lambda r: -r[2])
+
+    def pinned_empty(self, shape, dtype, order="F") -> np.ndarray:
+        """A numpy array over pinned (page-locked) host memory, freed with the array."""
+        dt = np.dtype(dtype)
+        nbytes = int(np.prod(shape)) * dt.itemsize
+        p = self._lib.qt_host_alloc(nbytes)
+        if not p:
+            raise EngineError("pinned host allocation failed", QT_ENOMEM)
+        buf = (C.c_byte * nbytes).from_address(p)
+        arr = np.frombuffer(buf, dtype=dt).reshape(shape, order=order)
+        lib = self._lib
+
+        class _Owner:
+            def __del__(self_inner):
+                lib.qt_host_free(C.c_void_p(p))
+
+        arr_base = _Owner()
+        arr = arr.view(_PinnedArray)
+        arr._owner = arr_base
+        return arr
+
+    # -- MPS ------------------------------------------------------------------
+    def mps(self, sites: Sequence[np.ndarray], dtype=np.complex128) -> "DeviceMPS":
+        """Upload 3-leg sites (chiL, 2, chiR); 2-leg end tensors (2, chi) /
+        (chi, 2) of the reference's MPS are accepted and reshaped."""
+        n = len(sites)
+        arrs = []
+        for i, t in enumerate(sites):
+            t = np.asarray(t)
+            if t.ndim == 2:
+                t = t.reshape((1,) + t.shape, order="F") if i == 0 else t.reshape(t.shape + (1,), order="F")
+            arrs.append(np.asfortranarray(t.astype(dtype, copy=False)))
+        dims = (C.c_int64 * (3 * n))(*[d for t in arrs for d in t.shape])
+        ptrs = (C.c_void_p * n)(*[t.ctypes.data for t in arrs])
+        out = C.c_void_p()
+        self._check(self._lib.qt_mps_create(self._h, n, dims, ptrs, _dtype_code(dtype), C.byref(out)))
+        return DeviceMPS(self, out, _dtype_code(dtype))
+
+    def product_state(self, n: int, dtype=np.complex128) -> "DeviceMPS":
+        """|0...0> on n sites of bond dimension 1."""
+        dims = (C.c_int64 * (3 * n))(*([1, 2, 1] * n))
+        out = C.c_void_p()
+        self._check(self._lib.qt_mps_create(self._h, n, dims, None, _dtype_code(dtype), C.byref(out)))
+        return DeviceMPS(self, out, _dtype_code(dtype))
+
+    # -- dense primitives -----------------------------------------------------
+    def contract_pair(self, A: np.ndarray, B: np.ndarray, axesA: Sequence[int], axesB: Sequence[int]) -> np.ndarray:
+        """ncon pairwise step: contract axesA of A with axesB of B (0-based);
+        the result's legs are A's free legs then B's (column-major)."""
+        dt = np.result_type(A.dtype, B.dtype, np.complex64)
+        A = np.asfortranarray(A.astype(dt))
+        B = np.asfortranarray(B.astype(dt))
+        nc = len(axesA)
+        free = [A.shape[i] for i in range(A.ndim) if i not in axesA] + [B.shape[i] for i in range(B.ndim) if i not in axesB]
+        out = np.zeros(free if free else [1], dtype=dt, order="F")
+        dA = (C.c_int64 * A.ndim)(*A.shape)
+        dB = (C.c_int64 * B.ndim)(*B.shape)
+        self._check(self._lib.qt_contract_pair(self._h, _dtype_code(dt), A.ndim, dA, _ptr(A), B.ndim, dB, _ptr(B), nc,
+                                               (C.c_int * nc)(*axesA), (C.c_int * nc)(*axesB), _ptr(out)))
+        return out
+
+    def truncated_svd(self, M: np.ndarray, cutoff: float = 0.0, chi_max: int = 0, mode: str = "plain"):
+        """Exact truncated SVD (tail rule of src/svd.jl:29-33): (U, S, Vh, k, discarded)."""
+        M = np.asarray(M)
+        dt = M.dtype if M.dtype in (np.complex64, np.complex128) else np.complex128
+        M = np.asfortranarray(M.astype(dt))
+        m, n = M.shape
+        kc = min(m, n)
+        U = np.zeros((m, kc), dtype=dt, order="F")
+        Vh = np.zeros((kc, n), dtype=dt, order="F")
+        S = np.zeros(kc)
+        k = C.c_int()
+        disc = C.c_double()
+        self._check(self._lib.qt_truncated_svd(self._h, _dtype_code(dt), m, n, _ptr(M), float(cutoff), int(chi_max),
+                                               MODES[mode], _ptr(U), S.ctypes.data_as(C.POINTER(C.c_double)),
+                                               _ptr(Vh), C.byref(k), C.byref(disc)))
+        kk = k.value
+        return U[:, :kk], S[:kk], Vh[:kk, :], kk, disc.value
+
+    def contract_svd(self, T1: np.ndarray, T2: np.ndarray, indx, er: float = 0.0) -> np.ndarray:
+        """``contract_svd(T1, T2, (i1, i2); er)`` of src/svd.jl:7-38 (1-based legs)."""
+        if not er >= 0:
+            raise QaintensorError("Error must be positive", QT_EINVAL_ERR_NEG)
+        i1, i2 = indx
+        dt = np.result_type(T1.dtype, T2.dtype, np.complex64)
+        T1 = np.asfortranarray(T1.astype(dt))
+        T2 = np.asfortranarray(T2.astype(dt))
+        d1 = T1.shape[i1 - 1] if i1 <= T1.ndim else 1
+        d2 = T2.shape[i2 - 1] if i2 <= T2.ndim else 1
+        if d1 != d2:
+            raise QaintensorError("Dimensions of contraction legs do not match", QT_EDIM_MISMATCH)
+        newdim = list(T1.shape[: i1 - 1]) + list(T1.shape[i1:]) + list(T2.shape[: i2 - 1]) + list(T2.shape[i2:])
+        out = np.zeros(newdim, dtype=dt, order="F")
+        self._check(self._lib.qt_contract_svd(self._h, _dtype_code(dt), T1.ndim, (C.c_int64 * T1.ndim)(*T1.shape),
+                                              _ptr(T1), T2.ndim, (C.c_int64 * T2.ndim)(*T2.shape), _ptr(T2),
+                                              int(i1), int(i2), float(er), _ptr(out)))
+        return out
+
+    # -- learned rank ---------------------------------------------------------
+    def set_rank_logging(self, on: bool = True):
+        self._check(self._lib.qt_rank_model_set_logging(self._h, int(on)))
+
+    def rank_log(self):
+        n = int(self._lib.qt_rank_model_log_size(self._h))
+        X = np.zeros((n, 16), dtype=np.float32)
+        Y = np.zeros(n, dtype=np.float32)
+        if n:
+            self._check(self._lib.qt_rank_model_get_log(self._h, _ptr(X), _ptr(Y)))
+        return X, Y
+
+    def clear_rank_log(self):
+        self._check(self._lib.qt_rank_model_clear_log(self._h))
+
+    @property
+    def n_params(self) -> int:
+        return int(self._lib.qt_rank_model_nparams())
+
+    def set_rank_params(self, p: np.ndarray, enable: bool = True):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        self._check(self._lib.qt_rank_model_set_params(self._h, _ptr(p), p.size, int(enable)))
+
+    def rank_params(self) -> np.ndarray:
+        p = np.zeros(self.n_params, dtype=np.float32)
+        self._check(self._lib.qt_rank_model_get_params(self._h, _ptr(p), p.size))
+        return p
+
+    def enable_rank_model(self, on: bool = True):
+        self._check(self._lib.qt_rank_model_enable(self._h, int(on)))
+
+    def set_rank_margin(self, margin: float):
+        self._check(self._lib.qt_rank_model_set_margin(self._h, float(margin)))
+
+    def train_rank_model(self, X, Y, epochs=30, batch=256, lr=1e-3, seed=0, init=None) -> float:
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        Y = np.ascontiguousarray(Y, dtype=np.float32)
+        init_p = None if init is None else np.ascontiguousarray(init, dtype=np.float32)
+        loss = C.c_double()
+        self._check(self._lib.qt_rank_model_train(self._h, X.shape[0], _ptr(X), _ptr(Y),
+                                                  None if init_p is None else _ptr(init_p), int(epochs), int(batch),
+                                                  float(lr), int(seed), C.byref(loss)))
+        return loss.value
+
+    def mlp_forward(self, X) -> np.ndarray:
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        out = np.zeros(X.shape[0], dtype=np.float32)
+        self._check(self._lib.qt_mlp_forward(self._h, X.shape[0], _ptr(X), _ptr(out)))
+        return out
+
+    def mlp_loss_grad(self, X, Y, params):
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        Y = np.ascontiguousarray(Y, dtype=np.float32)
+        p = np.ascontiguousarray(params, dtype=np.float32)
+        g = np.zeros_like(p)
+        loss = C.c_double()
+        self._check(self._lib.qt_mlp_loss_grad(self._h, X.shape[0], _ptr(X), _ptr(Y), _ptr(p), _ptr(g), C.byref(loss)))
+        return loss.value, g
+
+
+class _PinnedArray(np.ndarray):
+    """ndarray view that keeps its pinned host allocation alive."""
+    pass
+
+
+class DeviceMPS:
+    """An MPS resident in device memory; sites are (chiL, 2, chiR)."""
+
+    def __init__(self, eng: Engine, ptr: C.c_void_p, dtype_code: int):
+        self.eng, self._p, self.dtype_code = eng, ptr, dtype_code
+
+    @property
+    def nsites(self) -> int:
+        return int(self.eng._lib.qt_mps_nsites(self._p))
+
+    def dims(self, i: int):
+        """Dims of site i (1-based)."""
+        d = (C.c_int64 * 3)()
+        rc = self.eng._lib.qt_mps_site_dims(self._p, i - 1, d)
+        if rc == QT_EBOUNDS:
+            raise QaintensorBoundsError(f"site {i} out of range")
+        return tuple(d)
+
+    def clone(self) -> "DeviceMPS":
+        """Device-to-device copy."""
+        out = C.c_void_p()
+        self.eng._check(self.eng._lib.qt_mps_clone(self.eng._h, self._p, C.byref(out)))
+        return DeviceMPS(self.eng, out, self.dtype_code)
+
+    def download_into(self, i: int, out: np.ndarray):
+        """Download site i (1-based) into a preallocated column-major array."""
+        self.eng._check(self.eng._lib.qt_mps_download(self.eng._h, self._p, i - 1, _ptr(out)))
+
+    def site(self, i: int) -> np.ndarray:
+        """Download site i (1-based) as a (chiL, 2, chiR) column-major array."""
+        out = np.zeros(self.dims(i), dtype=_np_dtype(self.dtype_code), order="F")
+        self.eng._check(self.eng._lib.qt_mps_download(self.eng._h, self._p, i - 1, _ptr(out)))
+        return out
+
+    def sites(self) -> List[np.ndarray]:
+        return [self.site(i) for i in range(1, self.nsites + 1)]
+
+    def upload_site(self, i: int, t: np.ndarray):
+        t = np.asfortranarray(np.asarray(t, dtype=_np_dtype(self.dtype_code)))
+        self.eng._check(self.eng._lib.qt_mps_upload_site(self.eng._h, self._p, i - 1, (C.c_int64 * 3)(*t.shape), _ptr(t)))
+
+    def apply_2q(self, gate, i: int, cutoff: Optional[float] = None, chi_max: Optional[int] = None,
+                 mode: Optional[str] = None) -> dict:
+        """``apply_2q!(mps, G, i)``: gate G on wires (i, i+1), truncated SVD split."""
+        st = QtUpdateStats()
+        rc = self.eng._lib.qt_apply_2q(self.eng._h, self._p, i - 1, _gate_arg(gate),
+                                       -1.0 if cutoff is None else float(cutoff),
+                                       -1 if chi_max is None else int(chi_max),
+                                       -1 if mode is None else MODES[mode], C.byref(st))
+        self.eng._check(rc)
+        return st.as_dict()
+
+    def switch(self, i: int):
+        """``switch!(mps, i)`` (src/switch.jl): swap the physical legs of sites i, i+1."""
+        self.eng._check(self.eng._lib.qt_switch(self.eng._h, self._p, i - 1))
+
+    def expect_z(self, i: int) -> float:
+        out = C.c_double()
+        self.eng._check(self.eng._lib.qt_expect_z(self.eng._h, self._p, i - 1, C.byref(out)))
+        return out.value
+
+    def expect_zz(self, i: int) -> float:
+        out = C.c_double()
+        self.eng._check(self.eng._lib.qt_expect_zz(self.eng._h, self._p, i - 1, C.byref(out)))
+        return out.value
+
+    def norm2(self) -> float:
+        out = C.c_double()
+        self.eng._check(self.eng._lib.qt_mps_norm2(self.eng._h, self._p, C.byref(out)))
+        return out.value
+
+    def set_bond_spectrum(self, bond: int, s):
+        s = np.ascontiguousarray(s, dtype=np.float64)
+        rc = self.eng._lib.qt_mps_set_bond_spectrum(self._p, bond - 1, s.ctypes.data_as(C.POINTER(C.c_double)), s.size)
+        self.eng._check(rc)
+
+    def set_circuit_position(self, layer: int, depth: int):
+        self.eng._check(self.eng._lib.qt_mps_set_circuit_position(self._p, int(layer), int(depth)))
+
+    def rank_features(self, gate, i: int, cutoff: float, chi_max: int) -> np.ndarray:
+        f = np.zeros(16, dtype=np.float32)
+        self.eng._check(self.eng._lib.qt_rank_features_of(self._p, i - 1, _gate_arg(gate), float(cutoff),
+                                                          int(chi_max), _ptr(f)))
+        return f
+
+    def free(self):
+        if self._p:
+            self.eng._lib.qt_mps_free(self.eng._h, self._p)
+            self._p = C.c_void_p()
+
+    def __del__(self):
+        try:
+            if self.eng._h:
+                self.free()
+        except Exception:
+            pass
+
+
+# ---------------------------------------------------------------------------
+# Julia-named entry points (module level, explicit engine)
+# ---------------------------------------------------------------------------
+
+def contract_svd(engine: Engine, T1, T2, indx, er: float = 0.0):
+    """src/svd.jl:7-38 on the engine."""
+    return engine.contract_svd(T1, T2, indx, er)
+
+
+def switch_(mps: DeviceMPS, i: int):
+    """``switch!(mps, i)``."""
+    mps.switch(i)
+
+
+def apply_2q_(mps: DeviceMPS, gate, i: int, cutoff=None, chi_max=None, mode=None) -> dict:
+    """``apply_2q!(mps, G, i; cutoff, chi_max, mode)``."""
+    return mps.apply_2q(gate, i, cutoff, chi_max, mode)

@@ -1,0 +1,956 @@
+// C ABI of the engine: handle, device-resident MPS, the two-qubit gate +
+// truncated-SVD update in its three modes, and the dense primitives that sit
+// behind contract / contract_svd / svd of the reference.
+#include <cuda_runtime.h>
+#include <cusolverDn.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+
+#include "qt_internal.cuh"
+#include "qt_rank_model.h"
+
+// ---------------------------------------------------------------------------
+// basics
+// ---------------------------------------------------------------------------
+
+int qt_fail(qt_handle* h, int code, const std::string& msg) {
+  if (h) h->err = msg;
+  return code;
+}
+
+int qt_dmalloc(qt_handle* h, void** p, size_t bytes) {
+  cudaError_t e = cudaMallocFromPoolAsync(p, bytes ? bytes : 16, h->pool, h->stream);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return qt_fail(h, QT_ENOMEM, std::string("device allocation of ") + std::to_string(bytes) +
+                                     " bytes failed: " + cudaGetErrorString(e));
+  }
+  return QT_OK;
+}
+
+void qt_dfree(qt_handle* h, void* p) {
+  if (p) cudaFreeAsync(p, h->stream);
+}
+
+static size_t elem_size(int dtype) { return dtype == QT_C64 ? sizeof(float2) : sizeof(double2); }
+
+extern "C" int qt_abi_version(void) { return QT_ABI_VERSION; }
+
+extern "C" int qt_config_default(qt_config* cfg) {
+  if (!cfg) return QT_EINVAL;
+  std::memset(cfg, 0, sizeof(*cfg));
+  cfg->device = 0;
+  cfg->mode = QT_MODE_PLAIN;
+  cfg->cutoff = 0.0;
+  cfg->chi_max = 0;
+  cfg->oversample = 16;
+  cfg->power_iters = 1;
+  cfg->renormalize = 0;
+  cfg->use_rank_model = 1;
+  cfg->max_sweeps = 40;
+  cfg->jacobi_tol = 0.0;     // 0: sqrt(rows) * unit roundoff of the storage type
+  cfg->noise_floor = 0.0;    // 0: 4 * 2^-23 (FP32-level products)
+  cfg->seed = 0x5eed5eedull;
+  cfg->tc_gemm = 0;
+  return QT_OK;
+}
+
+extern "C" int qt_create(qt_handle** out, const qt_config* cfg) {
+  if (!out) return QT_EINVAL;
+  *out = nullptr;
+  qt_handle* h = new qt_handle();
+  if (cfg) h->cfg = *cfg; else qt_config_default(&h->cfg);
+  h->device = h->cfg.device;
+  int rc = QT_OK;
+  do {
+    if (cudaSetDevice(h->device) != cudaSuccess) { rc = QT_ECUDA; break; }
+    if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) { rc = QT_ECUDA; break; }
+    cudaMemPoolProps props;
+    std::memset(&props, 0, sizeof(props));
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = h->device;
+    if (cudaMemPoolCreate(&h->pool, &props) != cudaSuccess) { rc = QT_ECUDA; break; }
+    uint64_t thr = UINT64_MAX;
+    cudaMemPoolSetAttribute(h->pool, cudaMemPoolAttrReleaseThreshold, &thr);
+    if (cudaMalloc(&h->d_flags, sizeof(int) * QT_FLAG_COUNT) != cudaSuccess) { rc = QT_ENOMEM; break; }
+    if (cudaMallocHost(&h->h_flags, sizeof(int) * QT_FLAG_COUNT) != cudaSuccess) { rc = QT_ENOMEM; break; }
+    cudaMemset(h->d_flags, 0, sizeof(int) * QT_FLAG_COUNT);
+    h->rank_model = qt_rank_model_create();
+  } while (0);
+  if (rc != QT_OK) {
+    cudaGetLastError();
+    qt_destroy(h);
+    return rc;
+  }
+  *out = h;
+  return QT_OK;
+}
+
+extern "C" int qt_destroy(qt_handle* h) {
+  if (!h) return QT_OK;
+  cudaSetDevice(h->device);
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  qt_rank_model_destroy(h->rank_model);
+  for (cudaEvent_t e : h->event_pool) cudaEventDestroy(e);
+  for (cudaEvent_t e : h->timers)
+    if (e) cudaEventDestroy(e);
+  if (h->d_flags) cudaFree(h->d_flags);
+  if (h->h_flags) cudaFreeHost(h->h_flags);
+  if (h->pool) cudaMemPoolDestroy(h->pool);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+  return QT_OK;
+}
+
+extern "C" const char* qt_last_error(const qt_handle* h) { return h ? h->err.c_str() : "null handle"; }
+
+// ---------------------------------------------------------------------------
+// timing and profiling
+// ---------------------------------------------------------------------------
+
+static cudaEvent_t pool_event(qt_handle* h) {
+  if (h->event_next == h->event_pool.size()) {
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    h->event_pool.push_back(e);
+  }
+  return h->event_pool[h->event_next++];
+}
+
+void qt_prof_before(qt_handle* h, const char* name) {
+  qt_profile_rec r;
+  r.name = name;
+  r.start = pool_event(h);
+  r.stop = pool_event(h);
+  cudaEventRecord(r.start, h->stream);
+  h->prof_recs.push_back(r);
+}
+
+void qt_prof_after(qt_handle* h) { cudaEventRecord(h->prof_recs.back().stop, h->stream); }
+
+struct prof_agg {
+  std::string name;
+  int64_t launches = 0;
+  double ms = 0;
+};
+static std::vector<prof_agg> g_prof_view;  // last qt_profile_collect result
+
+extern "C" int qt_profile_enable(qt_handle* h, int on) {
+  if (!h) return QT_EINVAL;
+  cudaSetDevice(h->device);
+  cudaStreamSynchronize(h->stream);
+  h->prof = on != 0;
+  h->prof_recs.clear();
+  h->event_next = 0;
+  return QT_OK;
+}
+
+// Aggregate the recorded launches by kernel name; returns the number of kernels.
+extern "C" int qt_profile_collect(qt_handle* h) {
+  if (!h) return QT_EINVAL;
+  cudaSetDevice(h->device);
+  QT_CHECK_CUDA(h, cudaStreamSynchronize(h->stream));
+  g_prof_view.clear();
+  for (const auto& r : h->prof_recs) {
+    float ms = 0;
+    cudaEventElapsedTime(&ms, r.start, r.stop);
+    auto it = std::find_if(g_prof_view.begin(), g_prof_view.end(), [&](const prof_agg& a) { return a.name == r.name; });
+    if (it == g_prof_view.end()) {
+      g_prof_view.push_back(prof_agg());
+      it = g_prof_view.end() - 1;
+      it->name = r.name;
+    }
+    it->launches++;
+    it->ms += ms;
+  }
+  return (int)g_prof_view.size();
+}
+
+extern "C" int qt_profile_get(int idx, char* name, int namelen, int64_t* launches, double* total_ms) {
+  if (idx < 0 || idx >= (int)g_prof_view.size() || !name || namelen < 1) return QT_EINVAL;
+  std::strncpy(name, g_prof_view[idx].name.c_str(), (size_t)namelen - 1);
+  name[namelen - 1] = 0;
+  if (launches) *launches = g_prof_view[idx].launches;
+  if (total_ms) *total_ms = g_prof_view[idx].ms;
+  return QT_OK;
+}
+
+extern "C" int qt_timer_record(qt_handle* h, int slot) {
+  if (!h || slot < 0 || slot >= 8) return QT_EINVAL;
+  cudaSetDevice(h->device);
+  if (!h->timers[slot]) QT_CHECK_CUDA(h, cudaEventCreate(&h->timers[slot]));
+  QT_CHECK_CUDA(h, cudaEventRecord(h->timers[slot], h->stream));
+  return QT_OK;
+}
+
+extern "C" int qt_timer_elapsed(qt_handle* h, int a, int b, double* ms) {
+  if (!h || !ms || a < 0 || b < 0 || a >= 8 || b >= 8 || !h->timers[a] || !h->timers[b]) return QT_EINVAL;
+  QT_CHECK_CUDA(h, cudaEventSynchronize(h->timers[b]));
+  float f = 0;
+  QT_CHECK_CUDA(h, cudaEventElapsedTime(&f, h->timers[a], h->timers[b]));
+  *ms = f;
+  return QT_OK;
+}
+
+extern "C" int qt_sync(qt_handle* h) {
+  if (!h) return QT_EINVAL;
+  cudaSetDevice(h->device);
+  QT_CHECK_CUDA(h, cudaStreamSynchronize(h->stream));
+  return QT_OK;
+}
+
+// Write a 256 MiB device buffer (larger than the 129 MB L2) on the handle's
+// stream so the next step starts from a cold L2.
+extern "C" int qt_l2_flush(qt_handle* h) {
+  if (!h) return QT_EINVAL;
+  cudaSetDevice(h->device);
+  const size_t bytes = (size_t)256 << 20;
+  void* p = nullptr;
+  QT_TRY(qt_dmalloc(h, &p, bytes));
+  QT_CHECK_CUDA(h, cudaMemsetAsync(p, (int)(h->launches & 0xff), bytes, h->stream));
+  qt_dfree(h, p);
+  return QT_OK;
+}
+
+extern "C" void* qt_host_alloc(size_t bytes) {
+  void* p = nullptr;
+  if (cudaMallocHost(&p, bytes ? bytes : 16) != cudaSuccess) return nullptr;
+  return p;
+}
+
+extern "C" int qt_host_free(void* p) {
+  if (p) cudaFreeHost(p);
+  return QT_OK;
+}
+extern "C" int64_t qt_launch_count(const qt_handle* h) { return h ? h->launches : 0; }
+
+// ---------------------------------------------------------------------------
+// MPS objects
+// ---------------------------------------------------------------------------
+
+extern "C" int qt_mps_create(qt_handle* h, int nsites, const int64_t* dims, const void* const* host_sites, int dtype,
+                             qt_mps** out) {
+  if (!h || !out || !dims) return qt_fail(h, QT_EINVAL, "mps_create: null argument");
+  *out = nullptr;
+  if (nsites < 1) return qt_fail(h, QT_EINVAL, "mps_create: need at least one site");
+  if (dtype != QT_C64 && dtype != QT_C128) return qt_fail(h, QT_EINVAL, "mps_create: dtype must be QT_C64 or QT_C128");
+  for (int i = 0; i < nsites; i++) {
+    if (dims[3 * i] < 1 || dims[3 * i + 1] != 2 || dims[3 * i + 2] < 1)
+      return qt_fail(h, QT_EINVAL, "Each site must have dims (chiL, 2, chiR)");
+    if (i > 0 && dims[3 * i] != dims[3 * i - 1])
+      return qt_fail(h, QT_EDIM_MISMATCH, "Dimensions of contraction legs do not match");
+    if (!host_sites && (dims[3 * i] != 1 || dims[3 * i + 2] != 1))
+      return qt_fail(h, QT_EINVAL, "mps_create: the product state needs bond dimension 1");
+  }
+  cudaSetDevice(h->device);
+  qt_mps* m = new qt_mps();
+  m->nsites = nsites;
+  m->dtype = dtype;
+  m->spectrum.resize(nsites > 1 ? nsites - 1 : 0);
+  m->bond_updates.assign(nsites > 1 ? nsites - 1 : 0, 0);
+  const size_t es = elem_size(dtype);
+  for (int i = 0; i < nsites; i++) {
+    m->chil.push_back(dims[3 * i]);
+    m->chir.push_back(dims[3 * i + 2]);
+    const size_t bytes = (size_t)dims[3 * i] * 2 * dims[3 * i + 2] * es;
+    void* p = nullptr;
+    int rc = qt_dmalloc(h, &p, bytes);
+    if (rc != QT_OK) { qt_mps_free(h, m); return rc; }
+    m->site.push_back(p);
+    m->cap.push_back(bytes);
+    if (host_sites) {
+      if (!host_sites[i]) { qt_mps_free(h, m); return qt_fail(h, QT_EINVAL, "mps_create: null site pointer"); }
+      cudaMemcpyAsync(p, host_sites[i], bytes, cudaMemcpyHostToDevice, h->stream);
+    } else {
+      double2 z[2] = {make_double2(1, 0), make_double2(0, 0)};
+      float2 zf[2] = {make_float2(1, 0), make_float2(0, 0)};
+      cudaMemcpyAsync(p, dtype == QT_C128 ? (const void*)z : (const void*)zf, bytes, cudaMemcpyHostToDevice,
+                      h->stream);
+    }
+  }
+  QT_CHECK_CUDA(h, cudaStreamSynchronize(h->stream));
+  *out = m;
+  return QT_OK;
+}
+
+extern "C" int qt_mps_free(qt_handle* h, qt_mps* m) {
+  if (!m) return QT_OK;
+  if (h) {
+    cudaSetDevice(h->device);
+    for (void* p : m->site) qt_dfree(h, p);
+    cudaStreamSynchronize(h->stream);
+  }
+  delete m;
+  return QT_OK;
+}
+
+extern "C" int qt_mps_clone(qt_handle* h, const qt_mps* src, qt_mps** out) {
+  if (!h || !src || !out) return qt_fail(h, QT_EINVAL, "mps_clone: null argument");
+  *out = nullptr;
+  cudaSetDevice(h->device);
+  qt_mps* m = new qt_mps(*src);
+  for (int i = 0; i < src->nsites; i++) {
+    const size_t bytes = (size_t)src->chil[i] * 2 * src->chir[i] * elem_size(src->dtype);
+    void* p = nullptr;
+    int rc = qt_dmalloc(h, &p, bytes);
+    if (rc != QT_OK) {
+      for (int j = 0; j < i; j++) qt_dfree(h, m->site[j]);
+      delete m;
+      return rc;
+    }
+    m->site[i] = p;
+    m->cap[i] = bytes;
+    QT_CHECK_CUDA(h, cudaMemcpyAsync(p, src->site[i], bytes, cudaMemcpyDeviceToDevice, h->stream));
+  }
+  *out = m;
+  return QT_OK;
+}
+
+extern "C" int qt_mps_nsites(const qt_mps* m) { return m ? m->nsites : 0; }
+
+extern "C" int qt_mps_site_dims(const qt_mps* m, int site, int64_t* d) {
+  if (!m || !d) return QT_EINVAL;
+  if (site < 0 || site >= m->nsites) return QT_EBOUNDS;
+  d[0] = m->chil[site];
+  d[1] = 2;
+  d[2] = m->chir[site];
+  return QT_OK;
+}
+
+extern "C" int qt_mps_download(qt_handle* h, const qt_mps* m, int site, void* host) {
+  if (!h || !m || !host) return qt_fail(h, QT_EINVAL, "mps_download: null argument");
+  if (site < 0 || site >= m->nsites) return qt_fail(h, QT_EBOUNDS, "mps_download: site out of range");
+  cudaSetDevice(h->device);
+  const size_t bytes = (size_t)m->chil[site] * 2 * m->chir[site] * elem_size(m->dtype);
+  QT_CHECK_CUDA(h, cudaMemcpyAsync(host, m->site[site], bytes, cudaMemcpyDeviceToHost, h->stream));
+  QT_CHECK_CUDA(h, cudaStreamSynchronize(h->stream));
+  return QT_OK;
+}
+
+static int replace_site(qt_handle* h, qt_mps* m, int site, int64_t cl, int64_t cr, void* buf, size_t bytes) {
+  qt_dfree(h, m->site[site]);
+  m->site[site] = buf;
+  m->cap[site] = bytes;
+  m->chil[site] = cl;
+  m->chir[site] = cr;
+  return QT_OK;
+}
+
+extern "C" int qt_mps_upload_site(qt_handle* h, qt_mps* m, int site, const int64_t* d, const void* host) {
+  if (!h || !m || !d || !host) return qt_fail(h, QT_EINVAL, "mps_upload_site: null argument");
+  if (site < 0 || site >= m->nsites) return qt_fail(h, QT_EBOUNDS, "mps_upload_site: site out of range");
+  if (d[1] != 2 || d[0] < 1 || d[2] < 1) return qt_fail(h, QT_EINVAL, "Each site must have dims (chiL, 2, chiR)");
+  if ((site > 0 && d[0] != m->chir[site - 1]) || (site + 1 < m->nsites && d[2] != m->chil[site + 1]))
+    return qt_fail(h, QT_EDIM_MISMATCH, "Dimensions of contraction legs do not match");
+  cudaSetDevice(h->device);
+  const size_t bytes = (size_t)d[0] * 2 * d[2] * elem_size(m->dtype);
+  void* p = nullptr;
+  QT_TRY(qt_dmalloc(h, &p, bytes));
+  QT_CHECK_CUDA(h, cudaMemcpyAsync(p, host, bytes, cudaMemcpyHostToDevice, h->stream));
+  replace_site(h, m, site, d[0], d[2], p, bytes);
+  QT_CHECK_CUDA(h, cudaStreamSynchronize(h->stream));
+  return QT_OK;
+}
+
+// ---------------------------------------------------------------------------
+// truncated SVD of a device matrix (shared by every mode)
+// ---------------------------------------------------------------------------
+
+namespace {
+
+struct SvdOut {
+  int k = 0, k_cut = 0, sweeps = 0;
+  double norm2 = 0, discarded = 0;
+  std::vector<double> s;  // full computed spectrum, descending
+};
+
+double auto_tol(const qt_handle* h, int64_t rows, bool fp32) {
+  if (h->cfg.jacobi_tol > 0) return h->cfg.jacobi_tol;
+  const double u = fp32 ? 5.96e-8 : 1.11e-16;
+  return std::max(4.0, std::sqrt((double)rows)) * u;
+}
+
+int choose_rank(const qt_handle* h, const std::vector<double>& s, double cutoff, int chi_max, SvdOut* o) {
+  int kc = 1;
+  if (cutoff < 0) kc = (int)s.size();  // no truncation (switch!)
+  else qt_tail_rule_host(s, cutoff, &kc);
+  int k = kc;
+  if (chi_max > 0) k = std::min(k, chi_max);
+  o->k = k;
+  o->k_cut = kc;
+  o->norm2 = 0;
+  o->discarded = 0;
+  for (size_t i = 0; i < s.size(); i++) {
+    o->norm2 += s[i] * s[i];
+    if ((int)i >= k) o->discarded += s[i] * s[i];
+  }
+  (void)h;
+  return QT_OK;
+}
+
+double renorm_scale(const qt_handle* h, const SvdOut& o) {
+  if (!h->cfg.renormalize) return 1.0;
+  const double kept = o.norm2 - o.discarded;
+  return kept > 0 ? std::sqrt(o.norm2 / kept) : 1.0;
+}
+
+// Exact one-sided Jacobi SVD of theta (m x n, ld m, element TS) followed by the
+// tail rule and the split into A' (m x k) and B' (k x n) of element TO.
+// theta is overwritten.  The caller frees Aout/Bout on failure.
+template <typename TS, typename TO>
+int svd_split_jacobi(qt_handle* h, TS* theta, int64_t m, int64_t n, double cutoff, int chi_max, bool fp32_storage,
+                     TO** Aout, TO** Bout, SvdOut* o) {
+  qt_scratch s(h);
+  const bool tr = m < n;
+  const int64_t mm = tr ? n : m, nn = tr ? m : n;
+  TS* X = theta;
+  if (tr) {
+    QT_TRY(s.get(&X, (size_t)mm * nn));
+    QT_TRY(qt_adjoint_copy<TS>(h, theta, m, n, m, X, mm));
+  }
+  TS* V;
+  double* sig;
+  int* perm;
+  QT_TRY(s.get(&V, (size_t)nn * nn));
+  QT_TRY(s.get(&sig, (size_t)nn));
+  QT_TRY(s.get(&perm, (size_t)nn));
+  QT_TRY(qt_jacobi_svd<TS>(h, X, mm, nn, mm, V, nn, auto_tol(h, mm, fp32_storage), h->cfg.max_sweeps, &o->sweeps));
+  QT_TRY(qt_sorted_column_norms<TS>(h, X, mm, nn, mm, sig, perm));
+  o->s.resize(nn);
+  QT_CHECK_CUDA(h, cudaMemcpyAsync(o->s.data(), sig, sizeof(double) * nn, cudaMemcpyDeviceToHost, h->stream));
+  QT_CHECK_CUDA(h, cudaStreamSynchronize(h->stream));
+  QT_TRY(choose_rank(h, o->s, cutoff, chi_max, o));
+  QT_TRY(qt_dmalloc(h, (void**)Aout, sizeof(TO) * m * o->k));
+  QT_TRY(qt_dmalloc(h, (void**)Bout, sizeof(TO) * o->k * n));
+  QT_TRY((qt_absorb<TS, TO>(h, tr ? 1 : 0, X, mm, V, nn, sig, perm, m, n, o->k, renorm_scale(h, *o), *Aout, *Bout)));
+  return QT_OK;
+}
+
+__global__ void scale_columns_kernel(double2* X, int64_t rows, int64_t cols, int64_t ld, const double* s) {
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < rows * cols;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = idx % rows, j = idx / rows;
+    X[i + ld * j] = cscale(X[i + ld * j], s[j]);
+  }
+}
+
+__global__ void iota_kernel(int* p, int n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) p[i] = i;
+}
+
+// Cross-check path: cuSOLVER zgesvd (library) on theta, same rank rule and split.
+template <typename TO>
+int svd_split_cusolver(qt_handle* h, double2* theta, int64_t m, int64_t n, double cutoff, int chi_max, TO** Aout,
+                       TO** Bout, SvdOut* o) {
+  qt_scratch s(h);
+  const bool tr = m < n;
+  const int64_t mm = tr ? n : m, nn = tr ? m : n;  // gesvd needs rows >= cols
+  double2* X = theta;
+  if (tr) {
+    QT_TRY(s.get(&X, (size_t)mm * nn));
+    QT_TRY(qt_adjoint_copy<double2>(h, theta, m, n, m, X, mm));
+  }
+  double2 *U, *VT, *work;
+  double *S, *rwork;
+  int *info, *perm;
+  QT_TRY(s.get(&U, (size_t)mm * nn));
+  QT_TRY(s.get(&VT, (size_t)nn * nn));
+  QT_TRY(s.get(&S, (size_t)nn));
+  QT_TRY(s.get(&rwork, (size_t)nn * 5));
+  QT_TRY(s.get(&info, 1));
+  QT_TRY(s.get(&perm, (size_t)nn));
+  cusolverDnHandle_t cs;
+  if (cusolverDnCreate(&cs) != CUSOLVER_STATUS_SUCCESS) return qt_fail(h, QT_ECUDA, "cusolverDnCreate failed");
+  cusolverDnSetStream(cs, h->stream);
+  int lwork = 0;
+  cusolverDnZgesvd_bufferSize(cs, (int)mm, (int)nn, &lwork);
+  int rc = s.get(&work, (size_t)lwork);
+  if (rc == QT_OK) {
+    if (cusolverDnZgesvd(cs, 'S', 'S', (int)mm, (int)nn, (cuDoubleComplex*)X, (int)mm, S, (cuDoubleComplex*)U,
+                         (int)mm, (cuDoubleComplex*)VT, (int)nn, (cuDoubleComplex*)work, lwork, rwork,
+                         info) != CUSOLVER_STATUS_SUCCESS)
+      rc = qt_fail(h, QT_ECUDA, "cusolverDnZgesvd failed");
+  }
+  h->launches++;
+  cusolverDnDestroy(cs);
+  QT_TRY(rc);
+  // As the transposed split: "Vx" holds unit vectors of the left factor and
+  // "X" holds (right factor) x diag(S).  gesvd: X = U S VT.
+  //   not transposed: theta = U S VT  -> left = U,          right^H = VT^H S
+  //   transposed:     theta = VT^H S U^H -> left = VT^H,     right^H = U S
+  double2 *L, *Rh;
+  QT_TRY(s.get(&L, (size_t)std::max(mm, nn) * nn));
+  QT_TRY(s.get(&Rh, (size_t)std::max(mm, nn) * nn));
+  if (!tr) {
+    QT_CHECK_CUDA(h, cudaMemcpyAsync(L, U, sizeof(double2) * m * nn, cudaMemcpyDeviceToDevice, h->stream));
+    QT_TRY(qt_adjoint_copy<double2>(h, VT, nn, n, nn, Rh, n));
+  } else {
+    QT_TRY(qt_adjoint_copy<double2>(h, VT, nn, m, nn, L, m));
+    QT_CHECK_CUDA(h, cudaMemcpyAsync(Rh, U, sizeof(double2) * n * nn, cudaMemcpyDeviceToDevice, h->stream));
+  }
+  QT_LAUNCH(h, scale_columns_kernel, 256, 256, 0, Rh, n, nn, n, (const double*)S);
+  QT_LAUNCH(h, iota_kernel, 8, 256, 0, perm, (int)nn);
+  o->s.resize(nn);
+  QT_CHECK_CUDA(h, cudaMemcpyAsync(o->s.data(), S, sizeof(double) * nn, cudaMemcpyDeviceToHost, h->stream));
+  QT_CHECK_CUDA(h, cudaStreamSynchronize(h->stream));
+  QT_TRY(choose_rank(h, o->s, cutoff, chi_max, o));
+  QT_TRY(qt_dmalloc(h, (void**)Aout, sizeof(TO) * m * o->k));
+  QT_TRY(qt_dmalloc(h, (void**)Bout, sizeof(TO) * o->k * n));
+  QT_TRY((qt_absorb<double2, TO>(h, 1, Rh, n, L, m, S, perm, m, n, o->k, renorm_scale(h, *o), *Aout, *Bout)));
+  return QT_OK;
+}
+
+__global__ void gather_columns_kernel(const float2* __restrict__ V, int64_t rows, int64_t ldv, const int* __restrict__ perm,
+                                      int k, float2* __restrict__ out) {
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < rows * k;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = idx % rows, j = idx / rows;
+    out[i + rows * j] = V[i + ldv * perm[j]];
+  }
+}
+
+// Chosen mode: FP32-level products, randomized range finder sized by the
+// predicted rank, FP64 orthogonalisation and FP64-angle Jacobi on the small
+// projected matrix; exact FP64 SVD as fallback when the sketch's residual
+// exceeds the effective cutoff.  theta is m x n float2 (ld m).
+template <typename TO>
+int svd_split_chosen(qt_handle* h, float2* theta, int64_t m, int64_t n, double cutoff, int chi_max, int kpred,
+                     TO** Aout, TO** Bout, SvdOut* o, int* sketch, int* fallback, double* residual) {
+  qt_scratch s(h);
+  const int64_t kmin = std::min(m, n);
+  double* dn;
+  QT_TRY(s.get(&dn, 1));
+  QT_TRY(qt_norm2<float2>(h, theta, m * n, dn));
+  double tn2 = 0;
+  QT_CHECK_CUDA(h, cudaMemcpyAsync(&tn2, dn, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  QT_CHECK_CUDA(h, cudaStreamSynchronize(h->stream));
+  const double floor_rel = h->cfg.noise_floor > 0 ? h->cfg.noise_floor : 4.0 * 1.1920929e-7;
+  const double eff_cut = std::max(cutoff, floor_rel * std::sqrt(tn2));
+  int64_t l = (kpred > 0 ? kpred : kmin) + std::max(0, h->cfg.oversample);
+  l = ((l + 7) / 8) * 8;
+  *fallback = 0;
+  *residual = 0;
+  if (l >= kmin || kmin <= 32) {
+    *sketch = 0;
+    QT_TRY((svd_split_jacobi<float2, TO>(h, theta, m, n, eff_cut, chi_max, true, Aout, Bout, o)));
+    return QT_OK;
+  }
+  *sketch = (int)l;
+  const float2 one = make_float2(1, 0), zero = make_float2(0, 0), mone = make_float2(-1, 0);
+  float2 *om, *Y, *Z, *BH, *Vx, *Vk;
+  QT_TRY(s.get(&om, (size_t)n * l));
+  QT_TRY(s.get(&Y, (size_t)m * l));
+  QT_TRY(s.get(&Z, (size_t)n * l));
+  QT_TRY(s.get(&BH, (size_t)n * l));
+  QT_TRY(s.get(&Vx, (size_t)l * l));
+  // range finder: Y = theta Omega, q rounds of subspace iteration
+  QT_TRY(qt_gaussian<float2>(h, om, n, l, n, h->cfg.seed + 0x9E37ull * (++h->sketch_counter)));
+  QT_TRY(qt_cgemm<float2>(h, QT_OP_N, QT_OP_N, m, l, n, one, theta, m, om, n, zero, Y, m));
+  QT_TRY(qt_orthonormalize<float2>(h, Y, m, l));
+  for (int q = 0; q < h->cfg.power_iters; q++) {
+    QT_TRY(qt_cgemm<float2>(h, QT_OP_C, QT_OP_N, n, l, m, one, theta, m, Y, m, zero, Z, n));
+    QT_TRY(qt_orthonormalize<float2>(h, Z, n, l));
+    QT_TRY(qt_cgemm<float2>(h, QT_OP_N, QT_OP_N, m, l, n, one, theta, m, Z, n, zero, Y, m));
+    QT_TRY(qt_orthonormalize<float2>(h, Y, m, l));
+  }
+  // B^H = theta^H Q (n x l); residual theta - Q B
+  QT_TRY(qt_cgemm<float2>(h, QT_OP_C, QT_OP_N, n, l, m, one, theta, m, Y, m, zero, BH, n));
+  QT_TRY(qt_cgemm<float2>(h, QT_OP_N, QT_OP_C, m, n, l, mone, Y, m, BH, n, one, theta, m));
+  QT_TRY(qt_norm2<float2>(h, theta, m * n, dn));
+  // small SVD: one-sided Jacobi on B^H (n x l): B^H Vx = Ut diag(s)
+  double* sig;
+  int* perm;
+  QT_TRY(s.get(&sig, (size_t)l));
+  QT_TRY(s.get(&perm, (size_t)l));
+  QT_TRY(qt_jacobi_svd<float2>(h, BH, n, l, n, Vx, l, auto_tol(h, n, true), h->cfg.max_sweeps, &o->sweeps));
+  QT_TRY(qt_sorted_column_norms<float2>(h, BH, n, l, n, sig, perm));
+  o->s.resize(l);
+  double res2 = 0;
+  QT_CHECK_CUDA(h, cudaMemcpyAsync(o->s.data(), sig, sizeof(double) * l, cudaMemcpyDeviceToHost, h->stream));
+  QT_CHECK_CUDA(h, cudaMemcpyAsync(&res2, dn, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  QT_CHECK_CUDA(h, cudaStreamSynchronize(h->stream));
+  *residual = std::sqrt(res2);
+  // the tail rule sees the sketched spectrum followed by the residual weight
+  std::vector<double> sx = o->s;
+  sx.push_back(*residual);
+  QT_TRY(choose_rank(h, sx, eff_cut, chi_max, o));
+  o->s.pop_back();
+  if (o->k_cut > (int)l) {
+    *fallback = 1;  // the cutoff needs more than the sketch holds
+    return QT_OK;
+  }
+  QT_TRY(s.get(&Vk, (size_t)l * o->k));
+  QT_LAUNCH(h, gather_columns_kernel, 256, 256, 0, Vx, l, l, perm, o->k, Vk);
+  QT_TRY(qt_dmalloc(h, (void**)Aout, sizeof(TO) * m * o->k));
+  QT_TRY(qt_dmalloc(h, (void**)Bout, sizeof(TO) * o->k * n));
+  if (sizeof(TO) == sizeof(float2)) {
+    QT_TRY(qt_cgemm<float2>(h, QT_OP_N, QT_OP_N, m, o->k, l, one, Y, m, Vk, l, zero, (float2*)*Aout, m));
+  } else {
+    float2* Af;
+    QT_TRY(s.get(&Af, (size_t)m * o->k));
+    QT_TRY(qt_cgemm<float2>(h, QT_OP_N, QT_OP_N, m, o->k, l, one, Y, m, Vk, l, zero, Af, m));
+    QT_TRY(qt_convert(h, Af, QT_C64, *Aout, QT_C128, m * o->k));
+  }
+  // right site rows: conj(B^H[:, perm j]) -- absorb's transposed form with X = B^H
+  TO* Adummy;
+  QT_TRY(s.get(&Adummy, 1));
+  QT_TRY((qt_absorb<float2, TO>(h, 1, BH, n, Vx, l, sig, perm, 0, n, o->k, renorm_scale(h, *o), Adummy, *Bout)));
+  return QT_OK;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// the update
+// ---------------------------------------------------------------------------
+
+static bool finite_gate(const double* G) {
+  for (int i = 0; i < 32; i++)
+    if (!std::isfinite(G[i])) return false;
+  return true;
+}
+
+template <typename TO>
+static int update_impl(qt_handle* h, qt_mps* mps, int site, const double* G, double cutoff, int chi_max, int mode,
+                       qt_update_stats* st) {
+  const int64_t cl = mps->chil[site], cm = mps->chir[site], cr = mps->chir[site + 1];
+  const int64_t m = 2 * cl, n = 2 * cr;
+  SvdOut o;
+  TO *An = nullptr, *Bn = nullptr;
+  int sketch = 0, fallback = 0, kpred = -1;
+  double residual = 0;
+  int rc = QT_OK;
+  float feat[QT_MLP_IN];
+  const int kmax = qt_rank_kmax(mps, site, chi_max);
+  qt_rank_features(mps, site, G, cutoff < 0 ? 0.0 : cutoff, chi_max, feat);
+  {
+    qt_scratch s(h);
+    if (mode == QT_MODE_CHOSEN) {
+      float2* th;
+      QT_TRY(s.get(&th, (size_t)m * n));
+      QT_TRY(qt_theta_gate(h, mps->dtype, mps->site[site], mps->site[site + 1], cl, cm, cr, G, 1, th));
+      kpred = qt_rank_model_predict(h, feat, kmax);
+      rc = svd_split_chosen<TO>(h, th, m, n, cutoff, chi_max, kpred, &An, &Bn, &o, &sketch, &fallback, &residual);
+      if (rc == QT_OK && fallback) {
+        qt_dfree(h, An);
+        qt_dfree(h, Bn);
+        An = Bn = nullptr;
+        double2* th64;
+        QT_TRY(s.get(&th64, (size_t)m * n));
+        QT_TRY(qt_theta_gate(h, mps->dtype, mps->site[site], mps->site[site + 1], cl, cm, cr, G, 0, th64));
+        rc = svd_split_jacobi<double2, TO>(h, th64, m, n, cutoff, chi_max, false, &An, &Bn, &o);
+        if (rc != QT_OK) rc = QT_EFALLBACK_FAILED;
+      }
+    } else {
+      double2* th;
+      QT_TRY(s.get(&th, (size_t)m * n));
+      QT_TRY(qt_theta_gate(h, mps->dtype, mps->site[site], mps->site[site + 1], cl, cm, cr, G, 0, th));
+      if (mode == QT_MODE_CUSOLVER) rc = svd_split_cusolver<TO>(h, th, m, n, cutoff, chi_max, &An, &Bn, &o);
+      else rc = svd_split_jacobi<double2, TO>(h, th, m, n, cutoff, chi_max, false, &An, &Bn, &o);
+    }
+  }
+  if (rc != QT_OK) {
+    qt_dfree(h, An);
+    qt_dfree(h, Bn);
+    cudaStreamSynchronize(h->stream);
+    return rc;
+  }
+  const int k = o.k;
+  replace_site(h, mps, site, cl, k, An, sizeof(TO) * m * k);
+  replace_site(h, mps, site + 1, k, cr, Bn, sizeof(TO) * k * n);
+  mps->spectrum[site].assign(o.s.begin(), o.s.begin() + std::min<size_t>(o.s.size(), (size_t)k));
+  mps->bond_updates[site]++;
+  if (mode == QT_MODE_PLAIN && cutoff >= 0) qt_rank_model_log(h, feat, o.k, kmax);
+  QT_CHECK_CUDA(h, cudaStreamSynchronize(h->stream));
+  if (st) {
+    st->rank = k;
+    st->rank_cutoff = o.k_cut;
+    st->predicted_rank = kpred;
+    st->sketch_size = sketch;
+    st->fallback = fallback;
+    st->sweeps = o.sweeps;
+    st->discarded_weight = o.discarded;
+    st->norm2 = o.norm2;
+    st->residual = residual;
+  }
+  return QT_OK;
+}
+
+extern "C" int qt_apply_2q(qt_handle* h, qt_mps* mps, int site, const double* G, double cutoff, int chi_max, int mode,
+                           qt_update_stats* st) {
+  if (!h || !mps || !G) return qt_fail(h, QT_EINVAL, "apply_2q: null argument");
+  if (site < 0 || site + 1 >= mps->nsites) return qt_fail(h, QT_EBOUNDS, "apply_2q: site out of range");
+  if (cutoff < 0) cutoff = h->cfg.cutoff;
+  if (chi_max < 0) chi_max = h->cfg.chi_max;
+  if (mode < 0) mode = h->cfg.mode;
+  if (!(cutoff >= 0)) return qt_fail(h, QT_EINVAL_ERR_NEG, "Error must be positive");
+  if (mode != QT_MODE_PLAIN && mode != QT_MODE_CHOSEN && mode != QT_MODE_CUSOLVER)
+    return qt_fail(h, QT_EINVAL, "apply_2q: unknown mode");
+  if (!finite_gate(G)) return qt_fail(h, QT_ENUMERIC, "apply_2q: non-finite gate entry");
+  cudaSetDevice(h->device);
+  if (mps->dtype == QT_C128) return update_impl<double2>(h, mps, site, G, cutoff, chi_max, mode, st);
+  return update_impl<float2>(h, mps, site, G, cutoff, chi_max, mode, st);
+}
+
+extern "C" int qt_switch(qt_handle* h, qt_mps* mps, int site) {
+  // switch!(mps, i): the swap gate with no truncation, the plain FP64 path
+  if (!h || !mps) return qt_fail(h, QT_EINVAL, "switch: null argument");
+  if (site < 0 || site + 1 >= mps->nsites) return qt_fail(h, QT_EBOUNDS, "switch: site out of range");
+  // the SWAP gate, column-major interleaved: e0->e0, e1->e2, e2->e1, e3->e3
+  double G[32];
+  std::memset(G, 0, sizeof(G));
+  G[2 * (0 + 4 * 0)] = 1;
+  G[2 * (2 + 4 * 1)] = 1;
+  G[2 * (1 + 4 * 2)] = 1;
+  G[2 * (3 + 4 * 3)] = 1;
+  cudaSetDevice(h->device);
+  // no truncation at all: the reference keeps bond_dim = length(S)
+  if (mps->dtype == QT_C128) return update_impl<double2>(h, mps, site, G, -1.0, 0, QT_MODE_PLAIN, nullptr);
+  return update_impl<float2>(h, mps, site, G, -1.0, 0, QT_MODE_PLAIN, nullptr);
+}
+
+extern "C" int qt_expect_z(qt_handle* h, const qt_mps* mps, int site, double* out) {
+  if (!h || !mps || !out) return qt_fail(h, QT_EINVAL, "expect_z: null argument");
+  double num = 0, den = 0;
+  QT_TRY(qt_mps_expect(h, mps, site, 1, &num));
+  QT_TRY(qt_mps_expect(h, mps, 0, 0, &den));
+  *out = num / den;
+  return QT_OK;
+}
+
+extern "C" int qt_expect_zz(qt_handle* h, const qt_mps* mps, int site, double* out) {
+  if (!h || !mps || !out) return qt_fail(h, QT_EINVAL, "expect_zz: null argument");
+  double num = 0, den = 0;
+  QT_TRY(qt_mps_expect(h, mps, site, 2, &num));
+  QT_TRY(qt_mps_expect(h, mps, 0, 0, &den));
+  *out = num / den;
+  return QT_OK;
+}
+
+extern "C" int qt_mps_norm2(qt_handle* h, const qt_mps* mps, double* out) {
+  if (!h || !mps || !out) return qt_fail(h, QT_EINVAL, "mps_norm2: null argument");
+  return qt_mps_expect(h, mps, 0, 0, out);
+}
+
+// ---------------------------------------------------------------------------
+// dense primitives on host buffers
+// ---------------------------------------------------------------------------
+
+namespace {
+
+// Column-major permutation of a host tensor: out[new index] = in[old], where
+// new leg i is old leg perm[i].
+template <typename T>
+void permute_host(const T* in, const std::vector<int64_t>& dims, const std::vector<int>& perm, T* out) {
+  const int nd = (int)dims.size();
+  int64_t total = 1;
+  for (auto d : dims) total *= d;
+  std::vector<int64_t> stride(nd, 1);
+  for (int i = 1; i < nd; i++) stride[i] = stride[i - 1] * dims[i - 1];
+  std::vector<int64_t> nd_dims(nd), idx(nd, 0);
+  for (int i = 0; i < nd; i++) nd_dims[i] = dims[perm[i]];
+  for (int64_t lin = 0; lin < total; lin++) {
+    int64_t src = 0;
+    for (int i = 0; i < nd; i++) src += idx[i] * stride[perm[i]];
+    out[lin] = in[src];
+    for (int i = 0; i < nd; i++) {
+      if (++idx[i] < nd_dims[i]) break;
+      idx[i] = 0;
+    }
+  }
+}
+
+template <typename C>
+int dense_matmul(qt_handle* h, const C* A, int64_t M, int64_t K, const C* B, int64_t N, C* Cout) {
+  qt_scratch s(h);
+  C *dA, *dB, *dC;
+  QT_TRY(s.get(&dA, (size_t)M * K));
+  QT_TRY(s.get(&dB, (size_t)K * N));
+  QT_TRY(s.get(&dC, (size_t)M * N));
+  QT_CHECK_CUDA(h, cudaMemcpyAsync(dA, A, sizeof(C) * M * K, cudaMemcpyHostToDevice, h->stream));
+  QT_CHECK_CUDA(h, cudaMemcpyAsync(dB, B, sizeof(C) * K * N, cudaMemcpyHostToDevice, h->stream));
+  C one, zero;
+  one.x = 1; one.y = 0; zero.x = 0; zero.y = 0;
+  QT_TRY(qt_cgemm<C>(h, QT_OP_N, QT_OP_N, M, N, K, one, dA, M, dB, K, zero, dC, M));
+  QT_CHECK_CUDA(h, cudaMemcpyAsync(Cout, dC, sizeof(C) * M * N, cudaMemcpyDeviceToHost, h->stream));
+  QT_CHECK_CUDA(h, cudaStreamSynchronize(h->stream));
+  return QT_OK;
+}
+
+template <typename C>
+int contract_pair_t(qt_handle* h, int ndA, const int64_t* dA, const C* A, int ndB, const int64_t* dB, const C* B,
+                    int nc, const int* axA, const int* axB, C* out) {
+  std::vector<int64_t> da(dA, dA + ndA), db(dB, dB + ndB);
+  std::vector<char> ca(ndA, 0), cb(ndB, 0);
+  int64_t K = 1;
+  for (int i = 0; i < nc; i++) {
+    if (axA[i] < 0 || axA[i] >= ndA || axB[i] < 0 || axB[i] >= ndB || ca[axA[i]] || cb[axB[i]])
+      return qt_fail(h, QT_EINVAL, "contract_pair: bad axis");
+    if (da[axA[i]] != db[axB[i]]) return qt_fail(h, QT_EDIM_MISMATCH, "Dimensions of contraction legs do not match");
+    ca[axA[i]] = 1;
+    cb[axB[i]] = 1;
+    K *= da[axA[i]];
+  }
+  // A -> [free..., contracted (in axesA order)], B -> [contracted (axesB order), free...]
+  std::vector<int> pa, pb;
+  int64_t M = 1, N = 1;
+  for (int i = 0; i < ndA; i++) if (!ca[i]) { pa.push_back(i); M *= da[i]; }
+  for (int i = 0; i < nc; i++) pa.push_back(axA[i]);
+  for (int i = 0; i < nc; i++) pb.push_back(axB[i]);
+  for (int i = 0; i < ndB; i++) if (!cb[i]) { pb.push_back(i); N *= db[i]; }
+  std::vector<C> Ap((size_t)M * K), Bp((size_t)K * N);
+  permute_host(A, da, pa, Ap.data());
+  permute_host(B, db, pb, Bp.data());
+  return dense_matmul<C>(h, Ap.data(), M, K, Bp.data(), N, out);
+}
+
+}  // namespace
+
+extern "C" int qt_contract_pair(qt_handle* h, int dtype, int ndA, const int64_t* dimsA, const void* A, int ndB,
+                                const int64_t* dimsB, const void* B, int ncontract, const int* axesA, const int* axesB,
+                                void* C) {
+  if (!h || !dimsA || !dimsB || !A || !B || !C || (ncontract > 0 && (!axesA || !axesB)))
+    return qt_fail(h, QT_EINVAL, "contract_pair: null argument");
+  cudaSetDevice(h->device);
+  if (dtype == QT_C128)
+    return contract_pair_t<double2>(h, ndA, dimsA, (const double2*)A, ndB, dimsB, (const double2*)B, ncontract, axesA,
+                                    axesB, (double2*)C);
+  if (dtype == QT_C64)
+    return contract_pair_t<float2>(h, ndA, dimsA, (const float2*)A, ndB, dimsB, (const float2*)B, ncontract, axesA,
+                                   axesB, (float2*)C);
+  return qt_fail(h, QT_EINVAL, "contract_pair: bad dtype");
+}
+
+namespace {
+
+// Exact truncated SVD of a host matrix in FP64 (any dtype), results in FP64.
+int host_truncated_svd64(qt_handle* h, const double2* M, int64_t m, int64_t n, double cutoff, int chi_max, int mode,
+                         std::vector<double2>* U, std::vector<double>* S, std::vector<double2>* Vh, int* k,
+                         double* disc) {
+  qt_scratch s(h);
+  double2* dM;
+  QT_TRY(s.get(&dM, (size_t)m * n));
+  QT_CHECK_CUDA(h, cudaMemcpyAsync(dM, M, sizeof(double2) * m * n, cudaMemcpyHostToDevice, h->stream));
+  SvdOut o;
+  double2 *A = nullptr, *B = nullptr;
+  int rc = (mode == QT_MODE_CUSOLVER) ? svd_split_cusolver<double2>(h, dM, m, n, cutoff, chi_max, &A, &B, &o)
+                                      : svd_split_jacobi<double2, double2>(h, dM, m, n, cutoff, chi_max, false, &A, &B, &o);
+  if (rc == QT_OK) {
+    U->resize((size_t)m * o.k);
+    Vh->resize((size_t)o.k * n);
+    cudaMemcpyAsync(U->data(), A, sizeof(double2) * m * o.k, cudaMemcpyDeviceToHost, h->stream);
+    cudaMemcpyAsync(Vh->data(), B, sizeof(double2) * o.k * n, cudaMemcpyDeviceToHost, h->stream);
+    if (cudaStreamSynchronize(h->stream) != cudaSuccess) rc = qt_fail(h, QT_ECUDA, "svd download failed");
+    S->assign(o.s.begin(), o.s.begin() + o.k);
+    // B = diag(S) Vh: divide the rows back out (exact zeros keep zero rows)
+    for (int j = 0; j < o.k; j++) {
+      const double sj = (*S)[j];
+      const double sc = renorm_scale(h, o);
+      for (int64_t c = 0; c < n; c++) {
+        double2& v = (*Vh)[j + (size_t)o.k * c];
+        const double f = (sj > 0) ? 1.0 / (sj * sc) : 0.0;
+        v.x *= f;
+        v.y *= f;
+      }
+    }
+    *k = o.k;
+    *disc = o.discarded;
+  }
+  qt_dfree(h, A);
+  qt_dfree(h, B);
+  return rc;
+}
+
+}  // namespace
+
+extern "C" int qt_truncated_svd(qt_handle* h, int dtype, int64_t m, int64_t n, const void* M, double cutoff,
+                                int chi_max, int mode, void* U, double* S, void* Vh, int* k, double* discarded) {
+  if (!h || !M || !U || !S || !Vh || !k) return qt_fail(h, QT_EINVAL, "truncated_svd: null argument");
+  if (!(cutoff >= 0)) return qt_fail(h, QT_EINVAL_ERR_NEG, "Error must be positive");
+  if (m < 1 || n < 1) return qt_fail(h, QT_EINVAL, "truncated_svd: empty matrix");
+  cudaSetDevice(h->device);
+  if (mode < 0) mode = QT_MODE_PLAIN;
+  const int64_t kcap = std::min(m, n);
+  std::vector<double2> M64((size_t)m * n), u, vh;
+  std::vector<double> s;
+  for (int64_t i = 0; i < m * n; i++)
+    M64[i] = (dtype == QT_C64) ? make_double2(((const float2*)M)[i].x, ((const float2*)M)[i].y) : ((const double2*)M)[i];
+  int kk = 0;
+  double disc = 0;
+  QT_TRY(host_truncated_svd64(h, M64.data(), m, n, cutoff, chi_max, mode == QT_MODE_CUSOLVER ? mode : QT_MODE_PLAIN,
+                              &u, &s, &vh, &kk, &disc));
+  for (int j = 0; j < kk; j++) S[j] = s[j];
+  for (int64_t j = 0; j < kcap; j++)
+    for (int64_t i = 0; i < m; i++) {
+      const double2 v = (j < kk) ? u[i + (size_t)m * j] : make_double2(0, 0);
+      if (dtype == QT_C64) ((float2*)U)[i + m * j] = make_float2((float)v.x, (float)v.y);
+      else ((double2*)U)[i + m * j] = v;
+    }
+  for (int64_t c = 0; c < n; c++)
+    for (int64_t j = 0; j < kcap; j++) {
+      const double2 v = (j < kk) ? vh[j + (size_t)kk * c] : make_double2(0, 0);
+      if (dtype == QT_C64) ((float2*)Vh)[j + kcap * c] = make_float2((float)v.x, (float)v.y);
+      else ((double2*)Vh)[j + kcap * c] = v;
+    }
+  *k = kk;
+  if (discarded) *discarded = disc;
+  return QT_OK;
+}
+
+extern "C" int qt_contract_svd(qt_handle* h, int dtype, int nd1, const int64_t* dims1, const void* T1, int nd2,
+                               const int64_t* dims2, const void* T2, int i1, int i2, double er, void* out) {
+  // src/svd.jl:7-38.  Argument checks in the reference's order.
+  if (!h || !dims1 || !dims2 || !T1 || !T2 || !out) return qt_fail(h, QT_EINVAL, "contract_svd: null argument");
+  if (!(er >= 0)) return qt_fail(h, QT_EINVAL_ERR_NEG, "Error must be positive");
+  if (i1 < 1 || i2 < 1) return qt_fail(h, QT_EINVAL, "contract_svd: leg numbers are 1-based");
+  const int64_t D1 = (i1 <= nd1) ? dims1[i1 - 1] : 1, D2 = (i2 <= nd2) ? dims2[i2 - 1] : 1;
+  if (D1 != D2) return qt_fail(h, QT_EDIM_MISMATCH, "Dimensions of contraction legs do not match");
+  if (i1 > nd1 || i2 > nd2) return qt_fail(h, QT_ENOTSUP, "contract_svd: trailing singleton legs");
+  if (dtype != QT_C64 && dtype != QT_C128) return qt_fail(h, QT_EINVAL, "contract_svd: bad dtype");
+  cudaSetDevice(h->device);
+  std::vector<int64_t> d1(dims1, dims1 + nd1), d2(dims2, dims2 + nd2);
+  int64_t n1 = 1, n2 = 1;
+  for (auto d : d1) n1 *= d;
+  for (auto d : d2) n2 *= d;
+  std::vector<double2> t1((size_t)n1), t2((size_t)n2);
+  for (int64_t i = 0; i < n1; i++)
+    t1[i] = (dtype == QT_C64) ? make_double2(((const float2*)T1)[i].x, ((const float2*)T1)[i].y) : ((const double2*)T1)[i];
+  for (int64_t i = 0; i < n2; i++)
+    t2[i] = (dtype == QT_C64) ? make_double2(((const float2*)T2)[i].x, ((const float2*)T2)[i].y) : ((const double2*)T2)[i];
+  // T1p = permutedims(T1, [rest..., i1]) reshaped (:, D1); T2p = permutedims(T2, [i2, rest...]) reshaped (D1, :)
+  std::vector<int> p1, p2;
+  for (int i = 0; i < nd1; i++) if (i != i1 - 1) p1.push_back(i);
+  p1.push_back(i1 - 1);
+  p2.push_back(i2 - 1);
+  for (int i = 0; i < nd2; i++) if (i != i2 - 1) p2.push_back(i);
+  std::vector<double2> a((size_t)n1), b((size_t)n2);
+  permute_host(t1.data(), d1, p1, a.data());
+  permute_host(t2.data(), d2, p2, b.data());
+  const int64_t m1 = n1 / D1, m2 = n2 / D1;
+  // two truncated SVDs (src/svd.jl:26-33), then the product chain of :35
+  std::vector<double2> u1, v1, u2, v2;
+  std::vector<double> s1, s2;
+  int k1 = 0, k2 = 0;
+  double dd = 0;
+  QT_TRY(host_truncated_svd64(h, a.data(), m1, D1, er, 0, QT_MODE_PLAIN, &u1, &s1, &v1, &k1, &dd));
+  QT_TRY(host_truncated_svd64(h, b.data(), D1, m2, er, 0, QT_MODE_PLAIN, &u2, &s2, &v2, &k2, &dd));
+  // L = U1 diag(S1) V1h (m1 x D1) ; R = U2 diag(S2) V2h (D1 x m2) ; out = L R
+  std::vector<double2> us1((size_t)m1 * k1), us2((size_t)D1 * k2), L((size_t)m1 * D1), R((size_t)D1 * m2);
+  for (int j = 0; j < k1; j++)
+    for (int64_t i = 0; i < m1; i++) us1[i + m1 * j] = cscale(u1[i + m1 * j], s1[j]);
+  for (int j = 0; j < k2; j++)
+    for (int64_t i = 0; i < D1; i++) us2[i + D1 * j] = cscale(u2[i + D1 * j], s2[j]);
+  QT_TRY(dense_matmul<double2>(h, us1.data(), m1, k1, v1.data(), D1, L.data()));
+  QT_TRY(dense_matmul<double2>(h, us2.data(), D1, k2, v2.data(), m2, R.data()));
+  std::vector<double2> res((size_t)m1 * m2);
+  QT_TRY(dense_matmul<double2>(h, L.data(), m1, D1, R.data(), m2, res.data()));
+  for (int64_t i = 0; i < m1 * m2; i++) {
+    if (dtype == QT_C64) ((float2*)out)[i] = make_float2((float)res[i].x, (float)res[i].y);
+    else ((double2*)out)[i] = res[i];
+  }
+  return QT_OK;
+}

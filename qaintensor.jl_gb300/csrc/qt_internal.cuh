@@ -1,0 +1,214 @@
+// Internal definitions shared by the engine's translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/qaintensor_gb300.h"
+
+// ---------------------------------------------------------------------------
+// handle and MPS objects
+// ---------------------------------------------------------------------------
+
+struct qt_rank_model;  // learned-rank MLP state (k_mlp.cu)
+
+// Per-launch device timing (CUDA events on the handle's stream), grouped by
+// kernel name; enabled with qt_profile_enable.
+struct qt_profile_rec {
+  const char* name;
+  cudaEvent_t start, stop;
+};
+
+struct qt_handle {
+  qt_config cfg;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaMemPool_t pool = nullptr;   // stream-ordered pool owned by the handle
+  std::string err;
+  int64_t launches = 0;           // kernel launches issued through this handle
+  int* d_flags = nullptr;         // device status words (see QT_FLAG_*)
+  int* h_flags = nullptr;         // pinned host mirror
+  qt_rank_model* rank_model = nullptr;
+  uint64_t sketch_counter = 0;    // advances the sketch RNG stream per update
+  bool prof = false;
+  std::vector<qt_profile_rec> prof_recs;
+  std::vector<cudaEvent_t> event_pool;
+  size_t event_next = 0;
+  cudaEvent_t timers[8] = {};
+};
+
+// profiling hooks used by QT_LAUNCH
+void qt_prof_before(qt_handle* h, const char* name);
+void qt_prof_after(qt_handle* h);
+
+enum {
+  QT_FLAG_ROTATED = 0,   // Jacobi: pairs rotated in the current sweep
+  QT_FLAG_NONFINITE = 1, // a kernel met a non-finite value
+  QT_FLAG_CHOL = 2,      // a Cholesky factorisation lost positive definiteness
+  QT_FLAG_COUNT = 8
+};
+
+struct qt_mps {
+  int nsites = 0;
+  int dtype = QT_C128;
+  std::vector<int64_t> chil, chir;
+  std::vector<void*> site;        // device buffers (chiL*2*chiR elements)
+  std::vector<size_t> cap;        // bytes allocated per site
+  std::vector<std::vector<double>> spectrum;  // last kept spectrum per bond (nsites-1)
+  std::vector<int> bond_updates;  // updates applied per bond
+  int circuit_layer = 0;          // caller-set circuit position (rank-model feature)
+  int circuit_depth = 0;
+};
+
+// ---------------------------------------------------------------------------
+// error handling
+// ---------------------------------------------------------------------------
+
+int qt_fail(qt_handle* h, int code, const std::string& msg);
+
+#define QT_CHECK_CUDA(h, call)                                                    \
+  do {                                                                            \
+    cudaError_t e_ = (call);                                                      \
+    if (e_ != cudaSuccess)                                                        \
+      return qt_fail((h), (e_ == cudaErrorMemoryAllocation) ? QT_ENOMEM : QT_ECUDA, \
+                     std::string(#call) + ": " + cudaGetErrorString(e_));         \
+  } while (0)
+
+#define QT_TRY(expr)              \
+  do {                            \
+    int rc_ = (expr);             \
+    if (rc_ != QT_OK) return rc_; \
+  } while (0)
+
+// Launch a kernel on the handle's stream, count it and check the launch.
+#define QT_LAUNCH(h, kernel, grid, block, smem, ...)                                    \
+  do {                                                                                  \
+    if ((h)->prof) qt_prof_before((h), #kernel);                                         \
+    kernel<<<(grid), (block), (smem), (h)->stream>>>(__VA_ARGS__);                      \
+    if ((h)->prof) qt_prof_after((h));                                                   \
+    (h)->launches++;                                                                    \
+    cudaError_t e_ = cudaGetLastError();                                                \
+    if (e_ != cudaSuccess)                                                              \
+      return qt_fail((h), QT_ECUDA, std::string("launch " #kernel ": ") + cudaGetErrorString(e_)); \
+  } while (0)
+
+// ---------------------------------------------------------------------------
+// device memory from the handle's pool
+// ---------------------------------------------------------------------------
+
+int qt_dmalloc(qt_handle* h, void** p, size_t bytes);
+void qt_dfree(qt_handle* h, void* p);
+
+// RAII list of pool allocations released (stream-ordered) at scope exit.
+struct qt_scratch {
+  qt_handle* h;
+  std::vector<void*> ptrs;
+  explicit qt_scratch(qt_handle* hh) : h(hh) {}
+  ~qt_scratch() {
+    for (void* p : ptrs) qt_dfree(h, p);
+  }
+  template <typename T>
+  int get(T** p, size_t count) {
+    void* v = nullptr;
+    int rc = qt_dmalloc(h, &v, count * sizeof(T) + 16);
+    if (rc != QT_OK) return rc;
+    ptrs.push_back(v);
+    *p = static_cast<T*>(v);
+    return QT_OK;
+  }
+};
+
+// ---------------------------------------------------------------------------
+// complex helpers (interleaved {re, im})
+// ---------------------------------------------------------------------------
+
+template <typename T> struct cplx_of;
+template <> struct cplx_of<float> { typedef float2 type; };
+template <> struct cplx_of<double> { typedef double2 type; };
+template <typename C> struct real_of;
+template <> struct real_of<float2> { typedef float type; };
+template <> struct real_of<double2> { typedef double type; };
+
+__host__ __device__ inline double2 mk(double r, double i) { return make_double2(r, i); }
+__host__ __device__ inline float2 mk(float r, float i) { return make_float2(r, i); }
+
+template <typename C> __host__ __device__ inline C czero() { C z; z.x = 0; z.y = 0; return z; }
+template <typename C, typename D> __host__ __device__ inline C ccast(D a) { C z; z.x = a.x; z.y = a.y; return z; }
+template <typename C> __host__ __device__ inline C cconj(C a) { a.y = -a.y; return a; }
+template <typename C> __host__ __device__ inline C cadd(C a, C b) { a.x += b.x; a.y += b.y; return a; }
+template <typename C> __host__ __device__ inline C csub(C a, C b) { a.x -= b.x; a.y -= b.y; return a; }
+template <typename C> __host__ __device__ inline C cmul(C a, C b) {
+  C r; r.x = a.x * b.x - a.y * b.y; r.y = a.x * b.y + a.y * b.x; return r;
+}
+template <typename C, typename R> __host__ __device__ inline C cscale(C a, R s) { a.x *= s; a.y *= s; return a; }
+// acc += a * b
+template <typename C> __host__ __device__ inline void cfma(C& acc, C a, C b) {
+  acc.x = fma(a.x, b.x, acc.x); acc.x = fma(-a.y, b.y, acc.x);
+  acc.y = fma(a.x, b.y, acc.y); acc.y = fma(a.y, b.x, acc.y);
+}
+// acc += conj(a) * b
+template <typename C> __host__ __device__ inline void cfma_conj(C& acc, C a, C b) {
+  acc.x = fma(a.x, b.x, acc.x); acc.x = fma(a.y, b.y, acc.x);
+  acc.y = fma(a.x, b.y, acc.y); acc.y = fma(-a.y, b.x, acc.y);
+}
+template <typename C> __host__ __device__ inline typename real_of<C>::type cabs2(C a) { return a.x * a.x + a.y * a.y; }
+
+// ---------------------------------------------------------------------------
+// launchers implemented in the kernel translation units
+// ---------------------------------------------------------------------------
+
+enum qt_op { QT_OP_N = 0, QT_OP_T = 1, QT_OP_C = 2 };
+
+// k_gemm.cu ------------------------------------------------------------------
+// theta'(2chiL x 2chiR) = G (x) (A_mat . B_mat), gate folded in the epilogue.
+// A (chiL,2,chiM), B (chiM,2,chiR) of element type TI; output of type TO.
+// prec: 0 = FP64 accumulation, 1 = FP32 accumulation.
+int qt_theta_gate(qt_handle* h, int dtype_in, const void* A, const void* B, int64_t chil,
+                  int64_t chim, int64_t chir, const double* G, int prec, void* theta_out);
+// C(M x N) = alpha op(A) op(B) + beta C, column-major; T = float2 or double2.
+template <typename C>
+int qt_cgemm(qt_handle* h, int opA, int opB, int64_t M, int64_t N, int64_t K, C alpha,
+             const C* A, int64_t lda, const C* B, int64_t ldb, C beta, C* Cm, int64_t ldc);
+// element conversions / copies
+int qt_convert(qt_handle* h, const void* src, int src_dtype, void* dst, int dst_dtype, int64_t n);
+template <typename C>
+int qt_adjoint_copy(qt_handle* h, const C* src, int64_t m, int64_t n, int64_t lds, C* dst, int64_t ldd);
+template <typename C>
+int qt_set_identity(qt_handle* h, C* V, int64_t n, int64_t ld);
+// sum |x|^2 over n complex values into *out (device double), FP64 accumulation
+template <typename C>
+int qt_norm2(qt_handle* h, const C* x, int64_t n, double* d_out);
+
+// k_jacobi.cu ----------------------------------------------------------------
+// One-sided block Jacobi SVD of X (mm x nn, mm >= nn) in place: X <- X V with
+// orthogonal columns, V (nn x nn) accumulated.  TS = storage type.
+template <typename TS>
+int qt_jacobi_svd(qt_handle* h, TS* X, int64_t mm, int64_t nn, int64_t ldx, TS* V, int64_t ldv,
+                  double tol, int max_sweeps, int* sweeps_out);
+
+// k_trunc.cu -----------------------------------------------------------------
+// Column norms of X (mm x nn) in FP64; sort descending -> d_sigma (sorted), d_perm.
+template <typename TS>
+int qt_sorted_column_norms(qt_handle* h, const TS* X, int64_t mm, int64_t nn, int64_t ldx,
+                           double* d_sigma, int* d_perm);
+// tail rule on the device-sorted spectrum: returns k (clamped >= 1) and stats
+int qt_tail_rule_host(const std::vector<double>& s, double cutoff, int* k_cutoff);
+// A' columns j < k: Ucols[:, perm[j]] * uscale_j ; B' rows: see k_trunc.cu
+template <typename TS, typename TO>
+int qt_absorb(qt_handle* h, int transposed, const TS* X, int64_t ldx, const TS* Vx, int64_t ldv,
+              const double* d_sigma, const int* d_perm, int64_t m, int64_t n, int k, double sscale,
+              TO* Aout, TO* Bout);
+
+// k_rsvd.cu ------------------------------------------------------------------
+template <typename C>
+int qt_gaussian(qt_handle* h, C* out, int64_t rows, int64_t cols, int64_t ld, uint64_t seed);
+// Block classical Gram-Schmidt with re-orthogonalisation, intra-block shifted
+// CholeskyQR2 (FP64 Gram / Cholesky): Y (m x l, ld m) -> orthonormal columns.
+template <typename C>
+int qt_orthonormalize(qt_handle* h, C* Y, int64_t m, int64_t l);
+
+// k_obs.cu -------------------------------------------------------------------
+int qt_mps_expect(qt_handle* h, const qt_mps* mps, int site, int nops, double* out);
