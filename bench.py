@@ -219,7 +219,7 @@ def bench_ours(args, dist: Dist):
     rng = np.random.default_rng(77 + dist.rank)
     gates = [haar(rng) for _ in range(max(8, args.steps + args.warmup))]
 
-    eng = qt.Engine(mode="chosen", cutoff=CUTOFF, chi_max=chi, device=dev)
+    eng = qt.Engine(mode="chosen", cutoff=CUTOFF, chi_max=chi, device=dev, tc_gemm=1)
     model_path = load_rank_model(eng)
     templates = []
     for a, b, s in pairs:
@@ -315,7 +315,7 @@ def accuracy_check(qt, dev, pair, gate):
     a, b, s = pair
     chi = a.shape[0]
     ex = qt.Engine(mode="plain", cutoff=CUTOFF, chi_max=chi, device=dev)
-    ch = qt.Engine(mode="chosen", cutoff=CUTOFF, chi_max=chi, device=dev)
+    ch = qt.Engine(mode="chosen", cutoff=CUTOFF, chi_max=chi, device=dev, tc_gemm=1)
     load_rank_model(ch)
     m1 = ex.mps([a.astype(np.complex64).astype(np.complex128), b.astype(np.complex64).astype(np.complex128)])
     st1 = m1.apply_2q(gate, 1)

@@ -227,6 +227,26 @@ __global__ void norm2_kernel(const C* __restrict__ x, int64_t n, double* out) {
   }
 }
 
+// theta'(a,o1,o2,b) = sum G[o1+2o2, i1+2i2] theta(a,i1,i2,b), in place; one
+// thread per (a, b) owns the four physical values.
+__global__ void gate_inplace_kernel(float2* __restrict__ th, int chil, int chir, GateParam gp) {
+  const int64_t ldo = 2 * (int64_t)chil;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < (int64_t)chil * chir;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t a = idx % chil, b = idx / chil;
+    float2 v[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) v[q] = th[(a + chil * (q & 1)) + ldo * ((q >> 1) + 2 * b)];
+#pragma unroll
+    for (int o = 0; o < 4; o++) {
+      float2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+      for (int q = 0; q < 4; q++) cfma(acc, ccast<float2>(gp.g[o + 4 * q]), v[q]);
+      th[(a + chil * (o & 1)) + ldo * ((o >> 1) + 2 * b)] = acc;
+    }
+  }
+}
+
 inline int grid1d(int64_t n, int block = 256) {
   int64_t g = (n + block - 1) / block;
   if (g > 152 * 16) g = 152 * 16;
@@ -257,6 +277,13 @@ int qt_theta_gate(qt_handle* h, int dtype_in, const void* A, const void* B, int6
       QT_LAUNCH(h, (theta_gate_kernel<float2, float, float2, 2, 2>), grid, 256, 0, (const float2*)A,
                 (const float2*)B, (int)chil, (int)chim, (int)chir, gp, (float2*)theta_out);
   }
+  return QT_OK;
+}
+
+int qt_apply_gate_inplace(qt_handle* h, float2* theta, int64_t chil, int64_t chir, const double* G) {
+  GateParam gp;
+  for (int e = 0; e < 16; e++) gp.g[e] = make_double2(G[2 * e], G[2 * e + 1]);
+  QT_LAUNCH(h, gate_inplace_kernel, grid1d(chil * chir), 256, 0, theta, (int)chil, (int)chir, gp);
   return QT_OK;
 }
 

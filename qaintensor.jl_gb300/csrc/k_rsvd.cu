@@ -178,8 +178,8 @@ int qt_orthonormalize(qt_handle* h, C* Y, int64_t m, int64_t l) {
     C* Yb = Y + m * j0;
     for (int pass = 0; pass < 2; pass++) {
       if (j0 > 0) {
-        QT_TRY(qt_cgemm<C>(h, QT_OP_C, QT_OP_N, j0, b, m, one, Y, m, Yb, m, zero, coef, j0));
-        QT_TRY(qt_cgemm<C>(h, QT_OP_N, QT_OP_N, m, b, j0, mone, Y, m, coef, j0, one, Yb, m));
+        QT_TRY(qt_gemm_any(h, QT_OP_C, QT_OP_N, j0, b, m, one, Y, m, Yb, m, zero, coef, j0));
+        QT_TRY(qt_gemm_any(h, QT_OP_N, QT_OP_N, m, b, j0, mone, Y, m, coef, j0, one, Yb, m));
       }
       QT_TRY(block_cholqr<C>(h, Yb, m, b, pass == 0, dG));
     }

@@ -368,10 +368,14 @@ struct SvdOut {
   std::vector<double> s;  // full computed spectrum, descending
 };
 
+// Relative orthogonality threshold of the one-sided Jacobi.  The Gram entries
+// of a freshly rotated pair carry rounding noise of about sqrt(rows) u, so
+// the threshold sits a factor 16 above it; the singular values depend on the
+// remaining non-orthogonality only to second order.
 double auto_tol(const qt_handle* h, int64_t rows, bool fp32) {
   if (h->cfg.jacobi_tol > 0) return h->cfg.jacobi_tol;
   const double u = fp32 ? 5.96e-8 : 1.11e-16;
-  return std::max(4.0, std::sqrt((double)rows)) * u;
+  return 16.0 * std::sqrt((double)std::max<int64_t>(rows, 16)) * u;
 }
 
 int choose_rank(const qt_handle* h, const std::vector<double>& s, double cutoff, int chi_max, SvdOut* o) {
@@ -536,8 +540,15 @@ int svd_split_chosen(qt_handle* h, float2* theta, int64_t m, int64_t n, double c
   *residual = 0;
   if (l >= kmin || kmin <= 32) {
     *sketch = 0;
-    QT_TRY((svd_split_jacobi<float2, TO>(h, theta, m, n, eff_cut, chi_max, true, Aout, Bout, o)));
-    return QT_OK;
+    const int rc = svd_split_jacobi<float2, TO>(h, theta, m, n, eff_cut, chi_max, true, Aout, Bout, o);
+    if (rc == QT_ENUMERIC) {  // FP32-storage Jacobi did not settle: exact FP64 path
+      qt_dfree(h, *Aout);
+      qt_dfree(h, *Bout);
+      *Aout = *Bout = nullptr;
+      *fallback = 2;
+      return QT_OK;
+    }
+    return rc;
   }
   *sketch = (int)l;
   const float2 one = make_float2(1, 0), zero = make_float2(0, 0), mone = make_float2(-1, 0);
@@ -549,24 +560,31 @@ int svd_split_chosen(qt_handle* h, float2* theta, int64_t m, int64_t n, double c
   QT_TRY(s.get(&Vx, (size_t)l * l));
   // range finder: Y = theta Omega, q rounds of subspace iteration
   QT_TRY(qt_gaussian<float2>(h, om, n, l, n, h->cfg.seed + 0x9E37ull * (++h->sketch_counter)));
-  QT_TRY(qt_cgemm<float2>(h, QT_OP_N, QT_OP_N, m, l, n, one, theta, m, om, n, zero, Y, m));
+  QT_TRY(qt_gemm_any(h, QT_OP_N, QT_OP_N, m, l, n, one, theta, m, om, n, zero, Y, m));
   QT_TRY(qt_orthonormalize<float2>(h, Y, m, l));
   for (int q = 0; q < h->cfg.power_iters; q++) {
-    QT_TRY(qt_cgemm<float2>(h, QT_OP_C, QT_OP_N, n, l, m, one, theta, m, Y, m, zero, Z, n));
+    QT_TRY(qt_gemm_any(h, QT_OP_C, QT_OP_N, n, l, m, one, theta, m, Y, m, zero, Z, n));
     QT_TRY(qt_orthonormalize<float2>(h, Z, n, l));
-    QT_TRY(qt_cgemm<float2>(h, QT_OP_N, QT_OP_N, m, l, n, one, theta, m, Z, n, zero, Y, m));
+    QT_TRY(qt_gemm_any(h, QT_OP_N, QT_OP_N, m, l, n, one, theta, m, Z, n, zero, Y, m));
     QT_TRY(qt_orthonormalize<float2>(h, Y, m, l));
   }
   // B^H = theta^H Q (n x l); residual theta - Q B
-  QT_TRY(qt_cgemm<float2>(h, QT_OP_C, QT_OP_N, n, l, m, one, theta, m, Y, m, zero, BH, n));
-  QT_TRY(qt_cgemm<float2>(h, QT_OP_N, QT_OP_C, m, n, l, mone, Y, m, BH, n, one, theta, m));
+  QT_TRY(qt_gemm_any(h, QT_OP_C, QT_OP_N, n, l, m, one, theta, m, Y, m, zero, BH, n));
+  QT_TRY(qt_gemm_any(h, QT_OP_N, QT_OP_C, m, n, l, mone, Y, m, BH, n, one, theta, m));
   QT_TRY(qt_norm2<float2>(h, theta, m * n, dn));
   // small SVD: one-sided Jacobi on B^H (n x l): B^H Vx = Ut diag(s)
   double* sig;
   int* perm;
   QT_TRY(s.get(&sig, (size_t)l));
   QT_TRY(s.get(&perm, (size_t)l));
-  QT_TRY(qt_jacobi_svd<float2>(h, BH, n, l, n, Vx, l, auto_tol(h, n, true), h->cfg.max_sweeps, &o->sweeps));
+  {
+    const int rc = qt_jacobi_svd<float2>(h, BH, n, l, n, Vx, l, auto_tol(h, n, true), h->cfg.max_sweeps, &o->sweeps);
+    if (rc == QT_ENUMERIC) {  // the small SVD did not settle: exact FP64 path
+      *fallback = 2;
+      return QT_OK;
+    }
+    QT_TRY(rc);
+  }
   QT_TRY(qt_sorted_column_norms<float2>(h, BH, n, l, n, sig, perm));
   o->s.resize(l);
   double res2 = 0;
@@ -588,11 +606,11 @@ int svd_split_chosen(qt_handle* h, float2* theta, int64_t m, int64_t n, double c
   QT_TRY(qt_dmalloc(h, (void**)Aout, sizeof(TO) * m * o->k));
   QT_TRY(qt_dmalloc(h, (void**)Bout, sizeof(TO) * o->k * n));
   if (sizeof(TO) == sizeof(float2)) {
-    QT_TRY(qt_cgemm<float2>(h, QT_OP_N, QT_OP_N, m, o->k, l, one, Y, m, Vk, l, zero, (float2*)*Aout, m));
+    QT_TRY(qt_gemm_any(h, QT_OP_N, QT_OP_N, m, o->k, l, one, Y, m, Vk, l, zero, (float2*)*Aout, m));
   } else {
     float2* Af;
     QT_TRY(s.get(&Af, (size_t)m * o->k));
-    QT_TRY(qt_cgemm<float2>(h, QT_OP_N, QT_OP_N, m, o->k, l, one, Y, m, Vk, l, zero, Af, m));
+    QT_TRY(qt_gemm_any(h, QT_OP_N, QT_OP_N, m, o->k, l, one, Y, m, Vk, l, zero, Af, m));
     QT_TRY(qt_convert(h, Af, QT_C64, *Aout, QT_C128, m * o->k));
   }
   // right site rows: conj(B^H[:, perm j]) -- absorb's transposed form with X = B^H
@@ -632,7 +650,15 @@ static int update_impl(qt_handle* h, qt_mps* mps, int site, const double* G, dou
     if (mode == QT_MODE_CHOSEN) {
       float2* th;
       QT_TRY(s.get(&th, (size_t)m * n));
-      QT_TRY(qt_theta_gate(h, mps->dtype, mps->site[site], mps->site[site + 1], cl, cm, cr, G, 1, th));
+      if (h->cfg.tc_gemm && mps->dtype == QT_C64 && m >= 64 && n >= 32 && cm >= 32) {
+        // theta = A_mat (2chiL x chiM) . B_mat (chiM x 2chiR) on the tensor cores, then the gate
+        const float2 one = make_float2(1.f, 0.f), zero = make_float2(0.f, 0.f);
+        QT_TRY(qt_cgemm_tc(h, QT_OP_N, QT_OP_N, m, n, cm, one, (const float2*)mps->site[site], m,
+                           (const float2*)mps->site[site + 1], cm, zero, th, m));
+        QT_TRY(qt_apply_gate_inplace(h, th, cl, cr, G));
+      } else {
+        QT_TRY(qt_theta_gate(h, mps->dtype, mps->site[site], mps->site[site + 1], cl, cm, cr, G, 1, th));
+      }
       kpred = qt_rank_model_predict(h, feat, kmax);
       rc = svd_split_chosen<TO>(h, th, m, n, cutoff, chi_max, kpred, &An, &Bn, &o, &sketch, &fallback, &residual);
       if (rc == QT_OK && fallback) {
@@ -775,7 +801,7 @@ int dense_matmul(qt_handle* h, const C* A, int64_t M, int64_t K, const C* B, int
   QT_CHECK_CUDA(h, cudaMemcpyAsync(dB, B, sizeof(C) * K * N, cudaMemcpyHostToDevice, h->stream));
   C one, zero;
   one.x = 1; one.y = 0; zero.x = 0; zero.y = 0;
-  QT_TRY(qt_cgemm<C>(h, QT_OP_N, QT_OP_N, M, N, K, one, dA, M, dB, K, zero, dC, M));
+  QT_TRY(qt_gemm_any(h, QT_OP_N, QT_OP_N, M, N, K, one, dA, M, dB, K, zero, dC, M));
   QT_CHECK_CUDA(h, cudaMemcpyAsync(Cout, dC, sizeof(C) * M * N, cudaMemcpyDeviceToHost, h->stream));
   QT_CHECK_CUDA(h, cudaStreamSynchronize(h->stream));
   return QT_OK;

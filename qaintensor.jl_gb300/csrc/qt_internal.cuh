@@ -48,6 +48,7 @@ enum {
   QT_FLAG_ROTATED = 0,   // Jacobi: pairs rotated in the current sweep
   QT_FLAG_NONFINITE = 1, // a kernel met a non-finite value
   QT_FLAG_CHOL = 2,      // a Cholesky factorisation lost positive definiteness
+  QT_FLAG_OFFMAX = 3,    // Jacobi: largest relative off-diagonal above tol this sweep (float bits)
   QT_FLAG_COUNT = 8
 };
 
@@ -172,6 +173,25 @@ int qt_theta_gate(qt_handle* h, int dtype_in, const void* A, const void* B, int6
 template <typename C>
 int qt_cgemm(qt_handle* h, int opA, int opB, int64_t M, int64_t N, int64_t K, C alpha,
              const C* A, int64_t lda, const C* B, int64_t ldb, C beta, C* Cm, int64_t ldc);
+// k_tcgemm.cu: complex64 GEMM on the tcgen05 tensor cores (split-TF32x3), op in {N, C}
+int qt_cgemm_tc(qt_handle* h, int opA, int opB, int64_t M, int64_t N, int64_t K, float2 alpha, const float2* A,
+                int64_t lda, const float2* B, int64_t ldb, float2 beta, float2* C, int64_t ldc);
+// complex64 GEMM dispatch: tensor cores when cfg.tc_gemm is set and the
+// problem fills a tile, the SIMT kernel otherwise.
+int qt_cgemm_c64(qt_handle* h, int opA, int opB, int64_t M, int64_t N, int64_t K, float2 alpha, const float2* A,
+                 int64_t lda, const float2* B, int64_t ldb, float2 beta, float2* C, int64_t ldc);
+inline int qt_gemm_any(qt_handle* h, int opA, int opB, int64_t M, int64_t N, int64_t K, float2 alpha,
+                       const float2* A, int64_t lda, const float2* B, int64_t ldb, float2 beta, float2* C,
+                       int64_t ldc) {
+  return qt_cgemm_c64(h, opA, opB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc);
+}
+inline int qt_gemm_any(qt_handle* h, int opA, int opB, int64_t M, int64_t N, int64_t K, double2 alpha,
+                       const double2* A, int64_t lda, const double2* B, int64_t ldb, double2 beta, double2* C,
+                       int64_t ldc) {
+  return qt_cgemm<double2>(h, opA, opB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc);
+}
+// theta (2chiL x 2chiR, complex64) <- G applied on the physical legs, in place
+int qt_apply_gate_inplace(qt_handle* h, float2* theta, int64_t chil, int64_t chir, const double* G);
 // element conversions / copies
 int qt_convert(qt_handle* h, const void* src, int src_dtype, void* dst, int dst_dtype, int64_t n);
 template <typename C>
@@ -188,6 +208,11 @@ int qt_norm2(qt_handle* h, const C* x, int64_t n, double* d_out);
 template <typename TS>
 int qt_jacobi_svd(qt_handle* h, TS* X, int64_t mm, int64_t nn, int64_t ldx, TS* V, int64_t ldv,
                   double tol, int max_sweeps, int* sweeps_out);
+// The same with a caller-supplied partial-Gram workspace of qt_jacobi_layout() double2 entries.
+template <typename TS>
+int qt_jacobi_svd_ws(qt_handle* h, TS* X, int64_t mm, int64_t nn, int64_t ldx, TS* V, int64_t ldv, double tol,
+                     int max_sweeps, int* sweeps_out, double2* parts);
+int qt_jacobi_layout(int64_t mm, int64_t nn, int* nb_out, int* chunks_out);
 
 // k_trunc.cu -----------------------------------------------------------------
 // Column norms of X (mm x nn) in FP64; sort descending -> d_sigma (sorted), d_perm.

@@ -25,7 +25,7 @@ def test_randomized_path_matches_exact_truncation(engine, chi):
     # sketched split keeps the exact rank and its truncation error is within
     # 1.1x of the exact SVD's
     rng = np.random.default_rng(chi)
-    a, b, s = O.decay_theta_factors(chi, rng, decay=0.8)
+    a, b, s = O.decay_theta_factors(chi, rng, decay=0.6)
     g = O.haar_unitary(rng)
     cutoff = 1e-3
     ex = O.apply_2q([a.copy(), b.copy()], g, 1, cutoff, 0)
