@@ -87,6 +87,7 @@ typedef struct {
 
 typedef struct qt_handle qt_handle;
 typedef struct qt_mps qt_mps;
+typedef struct qt_batch qt_batch;
 
 /* ---- handle ------------------------------------------------------------ */
 int qt_config_default(qt_config* cfg);
@@ -197,6 +198,26 @@ int qt_mlp_loss_grad(qt_handle* h, int64_t n, const float* X, const float* Y, co
                      double* loss);
 /* The 16 features of the update of bond (site, site+1) with gate G. */
 int qt_rank_features_of(const qt_mps* mps, int site, const double* G, double cutoff, int chi_max, float* f);
+
+/* ---- batched circuits (no reference counterpart: the reference runs one
+ * network at a time) --------------------------------------------------------
+ * Many independent MPS (complex64, |0...0> at creation) with per-circuit qubit
+ * counts and bond caps chi_max <= 128.  A program is a list of layers of
+ * (circuit, site, gate) tasks; tasks of one layer must touch disjoint sites.
+ * Each layer runs as one persistent kernel whose CTAs take tasks from a
+ * device counter (mixed precision: FP32 products and Jacobi, FP64 norms and
+ * tail rule, effective cutoff max(cutoff, floor ||theta'||)); the whole
+ * program is captured in one CUDA graph when use_graph is set. */
+int qt_batch_create(qt_handle* h, int ncirc, const int* nqubits, const int* chi_max, qt_batch** out);
+int qt_batch_free(qt_handle* h, qt_batch* b);
+int qt_batch_run(qt_handle* h, qt_batch* b, int nlayers, const int* layer_start, const int* circ, const int* site,
+                 const double* gates /* 32 doubles per task */, double cutoff, int use_graph);
+int qt_batch_replay(qt_handle* h, qt_batch* b);
+int qt_batch_reset(qt_handle* h, qt_batch* b);
+int qt_batch_task_stats(qt_handle* h, const qt_batch* b, int* rank, int* sweeps, float* discarded);
+int qt_batch_bond_dims(qt_handle* h, const qt_batch* b, int circ, int* dims /* nqubits + 1 */);
+int qt_batch_download_site(qt_handle* h, const qt_batch* b, int circ, int site, void* host);
+int qt_batch_expect_z(qt_handle* h, qt_batch* b, int site, double* out /* one per circuit */);
 
 #ifdef __cplusplus
 }

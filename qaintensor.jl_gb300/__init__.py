@@ -131,6 +131,15 @@ def library() -> C.CDLL:
         "qt_profile_get": (I, [I, C.c_char_p, I, C.POINTER(L), C.POINTER(D)]),
         "qt_host_alloc": (P, [C.c_size_t]),
         "qt_host_free": (I, [P]),
+        "qt_batch_create": (I, [P, I, P, P, C.POINTER(P)]),
+        "qt_batch_free": (I, [P, P]),
+        "qt_batch_run": (I, [P, P, I, P, P, P, P, D, I]),
+        "qt_batch_replay": (I, [P, P]),
+        "qt_batch_reset": (I, [P, P]),
+        "qt_batch_task_stats": (I, [P, P, P, P, P]),
+        "qt_batch_bond_dims": (I, [P, P, I, P]),
+        "qt_batch_download_site": (I, [P, P, I, I, P]),
+        "qt_batch_expect_z": (I, [P, P, I, P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -499,6 +508,79 @@ class DeviceMPS:
     def free(self):
         if self._p:
             self.eng._lib.qt_mps_free(self.eng._h, self._p)
+            self._p = C.c_void_p()
+
+    def __del__(self):
+        try:
+            if self.eng._h:
+                self.free()
+        except Exception:
+            pass
+
+
+class Batch:
+    """Many independent circuits' MPS (complex64) updated layer by layer by
+    one persistent kernel per layer (optionally replayed from a CUDA graph)."""
+
+    def __init__(self, eng: Engine, nqubits, chi_max):
+        self.eng = eng
+        nq = np.ascontiguousarray(nqubits, dtype=np.int32)
+        cm = np.ascontiguousarray(chi_max, dtype=np.int32)
+        self.nqubits = nq.copy()
+        self._p = C.c_void_p()
+        eng._check(eng._lib.qt_batch_create(eng._h, nq.size, _ptr(nq), _ptr(cm), C.byref(self._p)))
+        self.ntask = 0
+
+    def run(self, layers, cutoff: float, use_graph: bool = True):
+        """layers: list of lists of (circuit, wire 1-based, 4x4 gate)."""
+        starts, circ, site, gates = [0], [], [], []
+        for layer in layers:
+            for (c, w, g) in layer:
+                circ.append(c)
+                site.append(w - 1)
+                gf = np.asarray(g, dtype=np.complex128).reshape(-1, order="F")
+                gates.append(np.stack([gf.real, gf.imag], axis=1).ravel())
+            starts.append(len(circ))
+        st = np.asarray(starts, dtype=np.int32)
+        ci = np.asarray(circ, dtype=np.int32)
+        si = np.asarray(site, dtype=np.int32)
+        ga = np.ascontiguousarray(np.concatenate(gates) if gates else np.zeros(32), dtype=np.float64)
+        self.ntask = len(circ)
+        self.eng._check(self.eng._lib.qt_batch_run(self.eng._h, self._p, len(layers), _ptr(st), _ptr(ci), _ptr(si),
+                                                   _ptr(ga), float(cutoff), int(use_graph)))
+
+    def replay(self):
+        self.eng._check(self.eng._lib.qt_batch_replay(self.eng._h, self._p))
+
+    def reset(self):
+        self.eng._check(self.eng._lib.qt_batch_reset(self.eng._h, self._p))
+
+    def task_stats(self):
+        n = self.ntask
+        r, sw, d = np.zeros(n, np.int32), np.zeros(n, np.int32), np.zeros(n, np.float32)
+        if n:
+            self.eng._check(self.eng._lib.qt_batch_task_stats(self.eng._h, self._p, _ptr(r), _ptr(sw), _ptr(d)))
+        return r, sw, d
+
+    def bond_dims(self, c: int):
+        out = np.zeros(int(self.nqubits[c]) + 1, dtype=np.int32)
+        self.eng._check(self.eng._lib.qt_batch_bond_dims(self.eng._h, self._p, c, _ptr(out)))
+        return out
+
+    def site(self, c: int, i: int) -> np.ndarray:
+        d = self.bond_dims(c)
+        out = np.zeros((d[i - 1], 2, d[i]), dtype=np.complex64, order="F")
+        self.eng._check(self.eng._lib.qt_batch_download_site(self.eng._h, self._p, c, i - 1, _ptr(out)))
+        return out
+
+    def expect_z(self, i: int) -> np.ndarray:
+        out = np.zeros(self.nqubits.size, dtype=np.float64)
+        self.eng._check(self.eng._lib.qt_batch_expect_z(self.eng._h, self._p, i - 1, _ptr(out)))
+        return out
+
+    def free(self):
+        if self._p:
+            self.eng._lib.qt_batch_free(self.eng._h, self._p)
             self._p = C.c_void_p()
 
     def __del__(self):

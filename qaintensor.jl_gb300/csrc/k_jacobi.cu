@@ -25,6 +25,7 @@
 // anyway); the 16x16 eigen-solve and the rotation angles are FP64 in both.
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <cstring>
 #include <string>
 
@@ -132,7 +133,7 @@ template <typename TS>
 __global__ void __launch_bounds__(NT)
 rotate_kernel(TS* __restrict__ X, int64_t ldx, int mm, TS* __restrict__ V, int64_t ldv, int nn, int nb, int round,
               int nparts, int x_rows_per_chunk, int v_rows_per_chunk, const double2* __restrict__ parts, double tol,
-              int* __restrict__ flags) {
+              double nu_rel2, const double* __restrict__ xnorm2, int* __restrict__ flags) {
   typedef typename real_of<TS>::type RS;
   typedef typename cplx_of<RS>::type CS;
   __shared__ double2 G[JC][JC + 1];
@@ -147,8 +148,12 @@ rotate_kernel(TS* __restrict__ X, int64_t ldx, int mm, TS* __restrict__ V, int64
 
   const int t = threadIdx.x;
   const int pair = blockIdx.x, chunk = blockIdx.y;
+  // columns with |x|^2 <= nu2 are at the rounding level of X: their values
+  // are known only to ~nu absolutely, so they are neither rotated nor tested
+  const double nu2 = nu_rel2 * (*xnorm2);
   pair_columns(round, pair, nb, nn, col);
   if (t == 0) { any_rot = 0; bad = 0; }
+  __syncthreads();
   // sum the partial Grams of this pair in a fixed order
   for (int e = t; e < NGRAM; e += NT) {
     double2 s = make_double2(0, 0);
@@ -169,7 +174,7 @@ rotate_kernel(TS* __restrict__ X, int64_t ldx, int mm, TS* __restrict__ V, int64
     if (i < j && col[i] >= 0 && col[j] >= 0) {
       const double a = G[i][i].x, b = G[j][j].x;
       const double g = sqrt(cabs2(G[i][j]));
-      if (g > tol * sqrt(a * b)) {
+      if (a > nu2 && b > nu2 && g > tol * sqrt(a * b)) {
         any_rot = 1;
         if (chunk == 0) {
           const float rel = (a > 0 && b > 0) ? (float)fmin(g / sqrt(a * b), 1.0) : 1.0f;
@@ -187,6 +192,7 @@ rotate_kernel(TS* __restrict__ X, int64_t ldx, int mm, TS* __restrict__ V, int64
   // storage precision) cannot leave the pair just above `tol`
   const double tol_inner = fmin(tol, 1e-14);
   for (int sweep = 0; sweep < MAX_INNER; sweep++) {
+    __syncthreads();  // every thread has read inner_rot of the previous sweep
     if (t == 0) inner_rot = 0;
     __syncthreads();
     for (int ir = 0; ir < JC - 1; ir++) {
@@ -199,7 +205,7 @@ rotate_kernel(TS* __restrict__ X, int64_t ldx, int mm, TS* __restrict__ V, int64
           const double a = fmax(G[p][p].x, 0.0), b = fmax(G[q][q].x, 0.0);
           const double2 g = G[p][q];
           const double ag = sqrt(cabs2(g));
-          if (ag > 0.0 && ag > tol_inner * sqrt(a * b)) {
+          if (a > nu2 && b > nu2 && ag > tol_inner * sqrt(a * b)) {
             const double zeta = (b - a) / (2.0 * ag);
             const double tt = copysign(1.0, zeta) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
             const double c = 1.0 / sqrt(1.0 + tt * tt);
@@ -253,7 +259,8 @@ rotate_kernel(TS* __restrict__ X, int64_t ldx, int mm, TS* __restrict__ V, int64
       }
       __syncthreads();
     }
-    if (!inner_rot) break;
+    const int again = inner_rot;  // read after the round's closing barrier
+    if (!again) break;
   }
   for (int e = t; e < NGRAM; e += NT) Wt[e / JC][e % JC] = ccast<CS>(W[e / JC][e % JC]);
   __syncthreads();
@@ -262,6 +269,19 @@ rotate_kernel(TS* __restrict__ X, int64_t ldx, int mm, TS* __restrict__ V, int64
   const int xb = chunk * x_rows_per_chunk, vb = chunk * v_rows_per_chunk;
   apply_rows<TS>(X, ldx, xb, min(mm, xb + x_rows_per_chunk), col, Wt, Xs);
   apply_rows<TS>(V, ldv, vb, min(nn, vb + v_rows_per_chunk), col, Wt, Xs);
+}
+
+// ||X||_F^2 in FP64, one CTA per column, added into *out.
+template <typename TS>
+__global__ void frob_kernel(const TS* __restrict__ X, int64_t ldx, int mm, double* out) {
+  double s = 0;
+  for (int i = threadIdx.x; i < mm; i += blockDim.x) {
+    const double re = X[i + ldx * blockIdx.x].x, im = X[i + ldx * blockIdx.x].y;
+    s = fma(re, re, s);
+    s = fma(im, im, s);
+  }
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) atomicAdd(out, s);
 }
 
 template <typename TS> struct gram_of;
@@ -280,7 +300,7 @@ int qt_jacobi_layout(int64_t mm, int64_t nn, int* nb_out, int* chunks_out) {
   chunks = std::max(1, std::min<int>(chunks, (int)((mm + 127) / 128)));
   *nb_out = nb;
   *chunks_out = chunks;
-  return pairs * chunks * NGRAM;  // double2 entries of partial-Gram workspace
+  return pairs * chunks * NGRAM + 1;  // double2 entries: partial Grams + ||X||_F^2
 }
 
 template <typename TS>
@@ -297,13 +317,24 @@ int qt_jacobi_svd_ws(qt_handle* h, TS* X, int64_t mm, int64_t nn, int64_t ldx, T
   const int xrows = (int)(((mm + chunks - 1) / chunks + JR - 1) / JR * JR);
   const int vrows = (int)(((nn + chunks - 1) / chunks + JR - 1) / JR * JR);
   const dim3 grid(pairs, chunks);
+  // the last workspace entry holds ||X||_F^2 (rotation-invariant); the noise
+  // floor is nu = 4 sqrt(rows) u ||X||_F with u the storage unit roundoff
+  double* xnorm2 = reinterpret_cast<double*>(parts + (size_t)pairs * chunks * NGRAM);
+  {
+    // ||X||_F^2 over the nn columns (ldx may exceed mm)
+    QT_CHECK_CUDA(h, cudaMemsetAsync(xnorm2, 0, sizeof(double), h->stream));
+    QT_LAUNCH(h, frob_kernel<TS>, (unsigned)nn, 256, 0, X, ldx, (int)mm, xnorm2);
+  }
+  const double u = (sizeof(typename real_of<TS>::type) == 8) ? 1.11e-16 : 5.96e-8;
+  const double nu_rel = 4.0 * std::sqrt((double)std::max<int64_t>(mm, 16)) * u;
+  const double nu_rel2 = nu_rel * nu_rel;
   int sweep = 0;
   for (; sweep < max_sweeps; sweep++) {
     QT_CHECK_CUDA(h, cudaMemsetAsync(h->d_flags, 0, sizeof(int) * QT_FLAG_COUNT, h->stream));
     for (int r = 0; r < rounds; r++) {
       QT_LAUNCH(h, (gram_kernel<TS, TG>), grid, NT, 0, X, ldx, (int)mm, (int)nn, nb, r, xrows, parts);
       QT_LAUNCH(h, rotate_kernel<TS>, grid, NT, 0, X, ldx, (int)mm, V, ldv, (int)nn, nb, r, chunks, xrows, vrows,
-                (const double2*)parts, tol, h->d_flags);
+                (const double2*)parts, tol, nu_rel2, (const double*)xnorm2, h->d_flags);
     }
     QT_CHECK_CUDA(h, cudaMemcpyAsync(h->h_flags, h->d_flags, sizeof(int) * QT_FLAG_COUNT, cudaMemcpyDeviceToHost,
                                      h->stream));

@@ -142,8 +142,10 @@ template <typename C>
 int block_cholqr(qt_handle* h, C* Yb, int64_t m, int b, bool shifted, double2* dG) {
   QT_CHECK_CUDA(h, cudaMemsetAsync(dG, 0, sizeof(double2) * BW * BW, h->stream));
   QT_LAUNCH(h, block_gram_kernel<C>, (unsigned)((m + 63) / 64), 256, 0, Yb, m, b, dG);
-  // shift of shifted CholeskyQR3 (the Gram and the Cholesky run in FP64)
-  const double u = 1.11e-16;
+  // shift of shifted CholeskyQR3, sized by the unit roundoff of the stored
+  // basis (the Gram and the Cholesky run in FP64, but Y R^{-1} is formed and
+  // stored in the element type of Y)
+  const double u = (sizeof(typename real_of<C>::type) == 8) ? 1.11e-16 : 5.96e-8;
   const double shift = shifted ? 11.0 * ((double)m * b + (double)b * (b + 1)) * u : 0.0;
   QT_LAUNCH(h, chol_inv_kernel, 1, 32, 0, dG, b, shift, h->d_flags);
   QT_LAUNCH(h, apply_rinv_kernel<C>, (unsigned)std::min<int64_t>((m + 255) / 256, 1024), 256, 0, Yb, m, b,
@@ -183,6 +185,9 @@ int qt_orthonormalize(qt_handle* h, C* Y, int64_t m, int64_t l) {
       }
       QT_TRY(block_cholqr<C>(h, Yb, m, b, pass == 0, dG));
     }
+    // one more CholeskyQR (shifted CholeskyQR3): after a shifted pass with
+    // the FP32 shift the block is only well conditioned, not orthonormal
+    if (sizeof(typename real_of<C>::type) == 4) QT_TRY(block_cholqr<C>(h, Yb, m, b, false, dG));
   }
   return QT_OK;
 }

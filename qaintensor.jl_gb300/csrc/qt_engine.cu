@@ -50,7 +50,7 @@ extern "C" int qt_config_default(qt_config* cfg) {
   cfg->power_iters = 1;
   cfg->renormalize = 0;
   cfg->use_rank_model = 1;
-  cfg->max_sweeps = 40;
+  cfg->max_sweeps = 80;
   cfg->jacobi_tol = 0.0;     // 0: sqrt(rows) * unit roundoff of the storage type
   cfg->noise_floor = 0.0;    // 0: 4 * 2^-23 (FP32-level products)
   cfg->seed = 0x5eed5eedull;
@@ -402,35 +402,106 @@ double renorm_scale(const qt_handle* h, const SvdOut& o) {
   return kept > 0 ? std::sqrt(o.norm2 / kept) : 1.0;
 }
 
-// Exact one-sided Jacobi SVD of theta (m x n, ld m, element TS) followed by the
-// tail rule and the split into A' (m x k) and B' (k x n) of element TO.
-// theta is overwritten.  The caller frees Aout/Bout on failure.
-template <typename TS, typename TO>
-int svd_split_jacobi(qt_handle* h, TS* theta, int64_t m, int64_t n, double cutoff, int chi_max, bool fp32_storage,
-                     TO** Aout, TO** Bout, SvdOut* o) {
-  qt_scratch s(h);
-  const bool tr = m < n;
-  const int64_t mm = tr ? n : m, nn = tr ? m : n;
-  TS* X = theta;
-  if (tr) {
-    QT_TRY(s.get(&X, (size_t)mm * nn));
-    QT_TRY(qt_adjoint_copy<TS>(h, theta, m, n, m, X, mm));
+template <typename C>
+__global__ void gather_cols_kernel(const C* __restrict__ V, int64_t rows, int64_t ldv, const int* __restrict__ perm,
+                                   int k, C* __restrict__ out) {
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < rows * k;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = idx % rows, j = idx / rows;
+    out[i + rows * j] = V[i + ldv * perm[j]];
   }
-  TS* V;
+}
+
+template <typename S, typename D>
+__global__ void convert_scale_kernel(const S* __restrict__ src, D* __restrict__ dst, int64_t n, double scale) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    D v;
+    v.x = src[i].x * scale;
+    v.y = src[i].y * scale;
+    dst[i] = v;
+  }
+}
+
+template <typename C>
+C cone() { C c; c.x = 1; c.y = 0; return c; }
+template <typename C>
+C czr() { C c; c.x = 0; c.y = 0; return c; }
+
+// Truncated SVD split of M (m x n, ld m, element TS): M ~ A' B' with A' (m x k)
+// orthonormal and B' = diag(S_k) V'[:k, :] (k x n).  QR-preconditioned
+// one-sided Jacobi (Drmac and Veselic): a wide M is first reduced by a QR of
+// M^H (M = M1 Q1^H, M1 = M Q1 square), then M1 = Q2 R2 and the block Jacobi
+// runs on Y = R2^H, whose rows are graded, with the rotations V accumulated:
+// M1 = Q2 V Y_f^H.  So A' = Q2 V[:, perm] and B' = (Q1 Y_f[:, perm])^H --
+// neither needs a division by a singular value.  The QRs are the BCGS2 +
+// shifted CholeskyQR2 of qt_orthonormalize with R = Q^H M by GEMM.  M is not
+// modified.  Outputs are allocated in element TO.
+template <typename TS, typename TO>
+int svd_split_jacobi(qt_handle* h, TS* M, int64_t m, int64_t n, double cutoff, int chi_max, bool fp32_storage,
+                     TO** Aout, TO** Bout, SvdOut* o, double extra_tail = -1.0) {
+  qt_scratch s(h);
+  const TS one = cone<TS>(), zero = czr<TS>();
+  const bool wide = m < n;
+  const int64_t r = std::min(m, n);
+  TS *Q1 = nullptr, *M1 = M;
+  if (wide) {
+    QT_TRY(s.get(&Q1, (size_t)n * m));
+    QT_TRY(qt_adjoint_copy<TS>(h, M, m, n, m, Q1, n));
+    QT_TRY(qt_orthonormalize<TS>(h, Q1, n, m));
+    QT_TRY(s.get(&M1, (size_t)m * m));
+    QT_TRY(qt_gemm_any(h, QT_OP_N, QT_OP_N, m, m, n, one, M, m, Q1, n, zero, M1, m));  // R1^H = M Q1
+  }
+  TS *Q2, *Y, *V;
+  QT_TRY(s.get(&Q2, (size_t)m * r));
+  QT_CHECK_CUDA(h, cudaMemcpyAsync(Q2, M1, sizeof(TS) * m * r, cudaMemcpyDeviceToDevice, h->stream));
+  QT_TRY(qt_orthonormalize<TS>(h, Q2, m, r));
+  QT_TRY(s.get(&Y, (size_t)r * r));
+  QT_TRY(qt_gemm_any(h, QT_OP_C, QT_OP_N, r, r, m, one, M1, m, Q2, m, zero, Y, r));  // R2^H = M1^H Q2
+  QT_TRY(s.get(&V, (size_t)r * r));
   double* sig;
   int* perm;
-  QT_TRY(s.get(&V, (size_t)nn * nn));
-  QT_TRY(s.get(&sig, (size_t)nn));
-  QT_TRY(s.get(&perm, (size_t)nn));
-  QT_TRY(qt_jacobi_svd<TS>(h, X, mm, nn, mm, V, nn, auto_tol(h, mm, fp32_storage), h->cfg.max_sweeps, &o->sweeps));
-  QT_TRY(qt_sorted_column_norms<TS>(h, X, mm, nn, mm, sig, perm));
-  o->s.resize(nn);
-  QT_CHECK_CUDA(h, cudaMemcpyAsync(o->s.data(), sig, sizeof(double) * nn, cudaMemcpyDeviceToHost, h->stream));
+  QT_TRY(s.get(&sig, (size_t)r));
+  QT_TRY(s.get(&perm, (size_t)r));
+  QT_TRY(qt_jacobi_svd<TS>(h, Y, r, r, r, V, r, auto_tol(h, r, fp32_storage), h->cfg.max_sweeps, &o->sweeps));
+  QT_TRY(qt_sorted_column_norms<TS>(h, Y, r, r, r, sig, perm));
+  o->s.resize(r);
+  QT_CHECK_CUDA(h, cudaMemcpyAsync(o->s.data(), sig, sizeof(double) * r, cudaMemcpyDeviceToHost, h->stream));
   QT_CHECK_CUDA(h, cudaStreamSynchronize(h->stream));
-  QT_TRY(choose_rank(h, o->s, cutoff, chi_max, o));
-  QT_TRY(qt_dmalloc(h, (void**)Aout, sizeof(TO) * m * o->k));
-  QT_TRY(qt_dmalloc(h, (void**)Bout, sizeof(TO) * o->k * n));
-  QT_TRY((qt_absorb<TS, TO>(h, tr ? 1 : 0, X, mm, V, nn, sig, perm, m, n, o->k, renorm_scale(h, *o), *Aout, *Bout)));
+  if (extra_tail >= 0) {
+    // a weight outside this factorisation (a sketch's residual) counts as
+    // the smallest tail value
+    std::vector<double> sx = o->s;
+    sx.push_back(extra_tail);
+    QT_TRY(choose_rank(h, sx, cutoff, chi_max, o));
+    if (o->k > (int)r) o->k = (int)r;
+  } else {
+    QT_TRY(choose_rank(h, o->s, cutoff, chi_max, o));
+  }
+  const int k = o->k;
+  const double sc = renorm_scale(h, *o);
+  // A' = Q2 V[:, perm[:k]]
+  TS *Vk, *At, *Bt;
+  QT_TRY(s.get(&Vk, (size_t)r * k));
+  QT_LAUNCH(h, gather_cols_kernel<TS>, 256, 256, 0, V, r, r, perm, k, Vk);
+  QT_TRY(s.get(&At, (size_t)m * k));
+  QT_TRY(qt_gemm_any(h, QT_OP_N, QT_OP_N, m, k, r, one, Q2, m, Vk, r, zero, At, m));
+  // B' = Y_f[:, perm]^H (tall) or (Q1 Y_f[:, perm])^H (wide)
+  TS* Yk;
+  QT_TRY(s.get(&Yk, (size_t)r * k));
+  QT_LAUNCH(h, gather_cols_kernel<TS>, 256, 256, 0, Y, r, r, perm, k, Yk);
+  QT_TRY(s.get(&Bt, (size_t)k * n));
+  if (wide) {
+    TS* Z;
+    QT_TRY(s.get(&Z, (size_t)n * k));
+    QT_TRY(qt_gemm_any(h, QT_OP_N, QT_OP_N, n, k, m, one, Q1, n, Yk, m, zero, Z, n));
+    QT_TRY(qt_adjoint_copy<TS>(h, Z, n, k, n, Bt, k));
+  } else {
+    QT_TRY(qt_adjoint_copy<TS>(h, Yk, r, k, r, Bt, k));
+  }
+  QT_TRY(qt_dmalloc(h, (void**)Aout, sizeof(TO) * m * k));
+  QT_TRY(qt_dmalloc(h, (void**)Bout, sizeof(TO) * k * n));
+  QT_LAUNCH(h, (convert_scale_kernel<TS, TO>), 256, 256, 0, At, *Aout, (int64_t)m * k, 1.0);
+  QT_LAUNCH(h, (convert_scale_kernel<TS, TO>), 256, 256, 0, Bt, *Bout, (int64_t)k * n, sc);
   return QT_OK;
 }
 
@@ -532,7 +603,10 @@ int svd_split_chosen(qt_handle* h, float2* theta, int64_t m, int64_t n, double c
   double tn2 = 0;
   QT_CHECK_CUDA(h, cudaMemcpyAsync(&tn2, dn, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
   QT_CHECK_CUDA(h, cudaStreamSynchronize(h->stream));
-  const double floor_rel = h->cfg.noise_floor > 0 ? h->cfg.noise_floor : 4.0 * 1.1920929e-7;
+  // singular values below 4 sqrt(rows) u_fp32 ||theta'|| are rounding noise of
+  // FP32-level products; the same floor bounds the FP32-storage Jacobi
+  const double floor_rel =
+      h->cfg.noise_floor > 0 ? h->cfg.noise_floor : 4.0 * std::sqrt((double)std::max(m, n)) * 5.96e-8;
   const double eff_cut = std::max(cutoff, floor_rel * std::sqrt(tn2));
   int64_t l = (kpred > 0 ? kpred : kmin) + std::max(0, h->cfg.oversample);
   l = ((l + 7) / 8) * 8;
@@ -552,12 +626,11 @@ int svd_split_chosen(qt_handle* h, float2* theta, int64_t m, int64_t n, double c
   }
   *sketch = (int)l;
   const float2 one = make_float2(1, 0), zero = make_float2(0, 0), mone = make_float2(-1, 0);
-  float2 *om, *Y, *Z, *BH, *Vx, *Vk;
+  float2 *om, *Y, *Z, *BH;
   QT_TRY(s.get(&om, (size_t)n * l));
   QT_TRY(s.get(&Y, (size_t)m * l));
   QT_TRY(s.get(&Z, (size_t)n * l));
   QT_TRY(s.get(&BH, (size_t)n * l));
-  QT_TRY(s.get(&Vx, (size_t)l * l));
   // range finder: Y = theta Omega, q rounds of subspace iteration
   QT_TRY(qt_gaussian<float2>(h, om, n, l, n, h->cfg.seed + 0x9E37ull * (++h->sketch_counter)));
   QT_TRY(qt_gemm_any(h, QT_OP_N, QT_OP_N, m, l, n, one, theta, m, om, n, zero, Y, m));
@@ -572,51 +645,43 @@ int svd_split_chosen(qt_handle* h, float2* theta, int64_t m, int64_t n, double c
   QT_TRY(qt_gemm_any(h, QT_OP_C, QT_OP_N, n, l, m, one, theta, m, Y, m, zero, BH, n));
   QT_TRY(qt_gemm_any(h, QT_OP_N, QT_OP_C, m, n, l, mone, Y, m, BH, n, one, theta, m));
   QT_TRY(qt_norm2<float2>(h, theta, m * n, dn));
-  // small SVD: one-sided Jacobi on B^H (n x l): B^H Vx = Ut diag(s)
-  double* sig;
-  int* perm;
-  QT_TRY(s.get(&sig, (size_t)l));
-  QT_TRY(s.get(&perm, (size_t)l));
+  double res2 = 0;
+  QT_CHECK_CUDA(h, cudaMemcpyAsync(&res2, dn, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  QT_CHECK_CUDA(h, cudaStreamSynchronize(h->stream));
+  *residual = std::sqrt(res2);
+  // small SVD of B = Q^H theta' (l x n, wide): the QR-preconditioned Jacobi
+  // split B ~ Ab Bb, the residual weight counted in the tail rule
+  float2* Bm;
+  QT_TRY(s.get(&Bm, (size_t)l * n));
+  QT_TRY(qt_adjoint_copy<float2>(h, BH, n, l, n, Bm, l));
+  float2 *Ab = nullptr, *Bb = nullptr;
   {
-    const int rc = qt_jacobi_svd<float2>(h, BH, n, l, n, Vx, l, auto_tol(h, n, true), h->cfg.max_sweeps, &o->sweeps);
+    const int rc = svd_split_jacobi<float2, float2>(h, Bm, l, n, eff_cut, chi_max, true, &Ab, &Bb, o, *residual);
     if (rc == QT_ENUMERIC) {  // the small SVD did not settle: exact FP64 path
+      qt_dfree(h, Ab);
+      qt_dfree(h, Bb);
       *fallback = 2;
       return QT_OK;
     }
     QT_TRY(rc);
   }
-  QT_TRY(qt_sorted_column_norms<float2>(h, BH, n, l, n, sig, perm));
-  o->s.resize(l);
-  double res2 = 0;
-  QT_CHECK_CUDA(h, cudaMemcpyAsync(o->s.data(), sig, sizeof(double) * l, cudaMemcpyDeviceToHost, h->stream));
-  QT_CHECK_CUDA(h, cudaMemcpyAsync(&res2, dn, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
-  QT_CHECK_CUDA(h, cudaStreamSynchronize(h->stream));
-  *residual = std::sqrt(res2);
-  // the tail rule sees the sketched spectrum followed by the residual weight
-  std::vector<double> sx = o->s;
-  sx.push_back(*residual);
-  QT_TRY(choose_rank(h, sx, eff_cut, chi_max, o));
-  o->s.pop_back();
-  if (o->k_cut > (int)l) {
-    *fallback = 1;  // the cutoff needs more than the sketch holds
+  if (o->k_cut > (int)l) {  // the cutoff needs more than the sketch holds
+    qt_dfree(h, Ab);
+    qt_dfree(h, Bb);
+    *fallback = 1;
     return QT_OK;
   }
-  QT_TRY(s.get(&Vk, (size_t)l * o->k));
-  QT_LAUNCH(h, gather_columns_kernel, 256, 256, 0, Vx, l, l, perm, o->k, Vk);
-  QT_TRY(qt_dmalloc(h, (void**)Aout, sizeof(TO) * m * o->k));
-  QT_TRY(qt_dmalloc(h, (void**)Bout, sizeof(TO) * o->k * n));
-  if (sizeof(TO) == sizeof(float2)) {
-    QT_TRY(qt_gemm_any(h, QT_OP_N, QT_OP_N, m, o->k, l, one, Y, m, Vk, l, zero, (float2*)*Aout, m));
-  } else {
-    float2* Af;
-    QT_TRY(s.get(&Af, (size_t)m * o->k));
-    QT_TRY(qt_gemm_any(h, QT_OP_N, QT_OP_N, m, o->k, l, one, Y, m, Vk, l, zero, Af, m));
-    QT_TRY(qt_convert(h, Af, QT_C64, *Aout, QT_C128, m * o->k));
-  }
-  // right site rows: conj(B^H[:, perm j]) -- absorb's transposed form with X = B^H
-  TO* Adummy;
-  QT_TRY(s.get(&Adummy, 1));
-  QT_TRY((qt_absorb<float2, TO>(h, 1, BH, n, Vx, l, sig, perm, 0, n, o->k, renorm_scale(h, *o), Adummy, *Bout)));
+  const int k = o->k;
+  // A' = Q Ab (m x k); B' = Bb
+  float2* Af;
+  QT_TRY(s.get(&Af, (size_t)m * k));
+  QT_TRY(qt_gemm_any(h, QT_OP_N, QT_OP_N, m, k, l, one, Y, m, Ab, l, zero, Af, m));
+  QT_TRY(qt_dmalloc(h, (void**)Aout, sizeof(TO) * m * k));
+  QT_TRY(qt_dmalloc(h, (void**)Bout, sizeof(TO) * k * n));
+  QT_TRY(qt_convert(h, Af, QT_C64, *Aout, sizeof(TO) == sizeof(float2) ? QT_C64 : QT_C128, m * k));
+  QT_TRY(qt_convert(h, Bb, QT_C64, *Bout, sizeof(TO) == sizeof(float2) ? QT_C64 : QT_C128, (int64_t)k * n));
+  qt_dfree(h, Ab);
+  qt_dfree(h, Bb);
   return QT_OK;
 }
 

@@ -54,7 +54,13 @@ def test_trained_rank_model_shrinks_the_sketch(engine):
             t0 = time.perf_counter()
             st = m.apply_2q(g, 1, cutoff, 0)
             dt = time.perf_counter() - t0
-            assert st["rank"] == ex.rank, (which, st, ex.rank)
+            # FP32-level spectra may move the rank by one at a near-tie of the
+            # tail rule; the truncation itself must stay as good as the exact one
+            assert abs(st["rank"] - ex.rank) <= 1, (which, st, ex.rank)
+            th = O.apply_gate_to_theta(O.theta_of(a.astype(np.complex64).astype(complex),
+                                                  b.astype(np.complex64).astype(complex)), g, chi, chi)
+            err = np.linalg.norm(th - O.theta_of(m.site(1).astype(complex), m.site(2).astype(complex)))
+            assert err <= 1.1 * np.sqrt(ex.discarded_weight) + 2e-6, (which, err, np.sqrt(ex.discarded_weight))
             sk.append(st["sketch_size"] or 2 * chi)
             if which == "with":
                 t_with += dt
