@@ -34,14 +34,17 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
+METRIC = "2q gate+SVD updates/s at \u03c7=1024: chosen vs plain FP64 GPU at |\u0394E|\u22641e-6"
 CHI = 1024
 CUTOFF = 1e-6
 DECAY = 0.97
 PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
-# FP64 / FP32 FMA throughput of this machine's GB300, measured by the project's
-# FMA-loop probe (MEASURED_PEAKS.json has HBM and bf16 only).
-FP64_PEAK_TFLOPS = 1.199
-FP32_PEAK_TFLOPS = 70.11
+
+
+def workload_config(chi: int, world: int) -> dict:
+    return {"workload": f"single-bond 2q gate+SVD update, theta (chi,2,2,chi) chi={chi}, spectrum {DECAY}^k unit "
+                        f"norm, Haar gate, cutoff {CUTOFF}, chi_max {chi}",
+            "parallelism": f"replicas x{world}", "l2": "256 MiB device write between steps"}
 
 
 def parse():
@@ -188,7 +191,7 @@ def load_rank_model(eng):
     return None
 
 
-def run_updates(eng, templates, gates, steps, flush, spectra):
+def run_updates(eng, templates, gates, steps, flush):
     """steps updates; returns (device ms, list of stats)."""
     stats = []
     eng.sync()
@@ -200,14 +203,6 @@ def run_updates(eng, templates, gates, steps, flush, spectra):
         m.free()
     eng.timer_record(1)
     return eng.timer_elapsed(0, 1), stats
-
-
-def flop_model(chi, stats):
-    """Algorithmic real flops of one update (see the measurement notes):
-    contraction 8*(2chi)*chi*(2chi), gate 8*16*chi^2, and the SVD part."""
-    n = 2 * chi
-    w_c = 8.0 * n * chi * n + 128.0 * chi * chi
-    return w_c
 
 
 def bench_ours(args, dist: Dist):
@@ -237,7 +232,7 @@ def bench_ours(args, dist: Dist):
     clocks = ClockSampler(dev)
     clocks.start()
     l0 = eng.launches
-    ms, stats = run_updates(eng, templates, gates[args.warmup:], args.steps, flush, None)
+    ms, stats = run_updates(eng, templates, gates[args.warmup:], args.steps, flush)
     launches = eng.launches - l0
     clk = clocks.stop()
     dist.barrier()
@@ -247,12 +242,16 @@ def bench_ours(args, dist: Dist):
 
     # per-kernel device times over the same workload (events around every launch)
     eng.profile_enable(True)
-    run_updates(eng, templates, gates[args.warmup:], min(args.steps, 3), flush, None)
+    w0 = eng.work_counters()
+    n_prof = min(args.steps, 3)
+    run_updates(eng, templates, gates[args.warmup:], n_prof, flush)
+    w1 = eng.work_counters()
     prof = eng.profile_collect()
     eng.profile_enable(False)
+    work = {k: (w1[k] - w0[k]) / n_prof for k in w0}  # per update
 
     out = {"value": value, "ms": ms_max, "stats": stats, "launches": launches, "clocks": clk, "profile": prof,
-           "model": model_path}
+           "model": model_path, "work": work, "n_prof": n_prof}
 
     # end-to-end through the host-buffer API
     a64 = [eng.pinned_empty((chi, 2, chi), np.complex64) for _ in range(2)]
@@ -303,7 +302,7 @@ def time_mode(qt, dev, pairs, gates, mode, steps):
     m = tmpl[0].clone()
     m.apply_2q(gates[0], 1)  # warm-up
     m.free()
-    ms, stats = run_updates(eng, tmpl, gates[1:], steps, lambda: None, None)
+    ms, stats = run_updates(eng, tmpl, gates[1:], steps, lambda: None)
     for t in tmpl:
         t.free()
     eng.close()
@@ -370,27 +369,46 @@ def cpu_baseline(chi, pair, gate):
 # roofline
 # ---------------------------------------------------------------------------
 
-def roofline(prof, chi, stats, steps_profiled):
+def load_peaks():
+    try:
+        with open(PEAKS_FILE) as f:
+            return json.load(f), "measured"
+    except (OSError, ValueError):
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def roofline(prof, work, n_prof):
+    """Roofline of the dominant kernel (largest total device time in the
+    profiled updates), from the engine's algorithmic work counters:
+      pair_round_kernel (one-launch Jacobi round): HBM-class bound; bytes = X
+        columns read once per round + rotated pairs' X written and V rows
+        read and written;
+      tc_gemm_kernel: tensor bound; 24 M N K TF32 flops per complex product,
+        peak = half the measured dense bf16 rate (TF32 runs at half the bf16
+        tensor rate)."""
     if not prof:
         return None
+    peaks, src = load_peaks()
     name, launches, ms = prof[0]
-    kind = name
-    # algorithmic work per launch of the dominant kernel
-    if "jacobi_pair_kernel" in name:
-        # a round of the one-sided block Jacobi: every CTA forms one 16-column
-        # Gram (FP64: 8 flops per complex MAC over the rows of the matrix)
-        rows = 2 * chi
-        l = stats[0]["sketch_size"] or 2 * chi
-        pairs = max(1, (l // 8 + (l // 8) % 2) // 2)
-        work = pairs * 8.0 * rows * (16 * 17 / 2)
-        peak, unit, bound = FP64_PEAK_TFLOPS, "TFLOP/s", "fp64"
-        achieved = work / (ms / launches * 1e-3) / 1e12
-    elif "cgemm_kernel" in name or "theta_gate" in name:
-        return {"kernel": name, "note": "per-launch shapes vary; see profiles/"}
-    else:
-        return {"kernel": name}
-    return {"kernel": kind, "bound": bound, "achieved": achieved, "peak": peak, "unit": unit,
-            "frac": achieved / peak, "traffic": None, "peak_source": "project FMA-loop probe (not in MEASURED_PEAKS.json)"}
+    per_launch_s = ms / 1e3 / launches
+    if name.startswith("pair_round_kernel") or name.startswith("(gram_kernel") or name.startswith("apply_kernel"):
+        n_launch = work["jacobi_rounds"]
+        if n_launch <= 0:
+            return {"kernel": name, "note": "no Jacobi work recorded"}
+        bytes_per_launch = work["jacobi_bytes"] / n_launch
+        achieved = bytes_per_launch / per_launch_s / 1e9
+        peak = peaks["hbm_gbs"]
+        return {"kernel": name, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": None, "bytes_per_launch": bytes_per_launch,
+                "peak_source": f"{src} hbm_gbs", "note": "X and V of the round are L2-resident (<= 67 MB at 2048^2)"}
+    if name.startswith("tc_gemm_kernel"):
+        n_launch = work["tc_launches"]
+        flops_per_launch = work["tc_flops"] / max(n_launch, 1)
+        achieved = flops_per_launch / per_launch_s / 1e12
+        peak = peaks["bf16_tflops"] / 2
+        return {"kernel": name, "bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                "frac": achieved / peak, "traffic": None, "peak_source": f"{src} bf16_tflops / 2 (TF32)"}
+    return {"kernel": name, "note": "no work model for this kernel"}
 
 
 # ---------------------------------------------------------------------------
@@ -414,10 +432,10 @@ def bench_reference(args, dist: Dist):
         oracle.apply_2q([pair[0].copy(), pair[1].copy()], gates[warm + i], 1, CUTOFF, chi)
     dt = time.perf_counter() - t0
     v = steps / dt
-    return {"metric": "2q gate+SVD updates/s at chi=1024", "value": v, "unit": "updates/s", "n_gpus": 0,
+    return {"metric": METRIC, "value": v, "unit": "updates/s", "n_gpus": 0,
             "steps": steps, "warmup": warm, "ms_per_step": dt / steps * 1e3, "higher_is_better": True,
             "impl": "reference", "dtype": "c128", "data": "synthetic",
-            "config": {"workload": f"single-bond update chi={chi}, spectrum {DECAY}^k, Haar gate, cutoff {CUTOFF}"},
+            "config": workload_config(chi, 1),
             "cpu_baseline": {"value": v, "unit": "updates/s", "cores": os.cpu_count(), "kind": "port",
                              "sample": f"{steps} timed update(s) at chi={chi} (steps capped at 2 to bound the run)"},
             "e2e": {"value": v, "unit": "updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -438,15 +456,13 @@ def main():
         stats = res["stats"]
         prof = res["profile"]
         line = {
-            "metric": "2q gate+SVD updates/s at chi=1024 (mixed-precision + learned-rank path)",
+            "metric": METRIC,
             "value": res["value"], "unit": "updates/s", "n_gpus": dist.world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": res["ms"] / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "c64 storage, fp32-level products, fp64 small SVD",
+            "scaling": "weak", "vs_baseline": None, "dtype": "c64",
             "data": "synthetic (seeded decaying-spectrum theta, Haar gates)",
-            "config": {"workload": f"single-bond 2q gate+SVD update, theta (chi,2,2,chi) chi={args.chi}, "
-                                   f"spectrum {DECAY}^k unit norm, Haar gate, cutoff {CUTOFF}, chi_max {args.chi}",
-                       "parallelism": f"replicas x{dist.world}", "l2": "256 MiB device write between steps",
-                       "rank_model": res["model"]},
+            "config": dict(workload_config(args.chi, dist.world),
+                           rank_model=os.path.relpath(res["model"], ROOT) if res["model"] else None),
             "gpu_launches": res["launches"],
             "clocks": res["clocks"],
             "e2e": res["e2e"],
@@ -454,7 +470,7 @@ def main():
             "accuracy": res["accuracy"],
             "kernels": [{"name": n, "launches": c, "ms": round(t, 3)} for n, c, t in prof[:8]],
         }
-        line["roofline"] = roofline(prof, args.chi, stats, min(args.steps, 3))
+        line["roofline"] = roofline(prof, res["work"], res["n_prof"])
         if "plain" in res:
             line["plain_fp64_gpu"] = res["plain"]
             line["cusolver_fp64_gpu"] = res["cusolver"]

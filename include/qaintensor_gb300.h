@@ -71,6 +71,8 @@ typedef struct {
                               below the FP32-level arithmetic and are not resolved */
   uint64_t seed;           /* sketch RNG seed */
   int tc_gemm;             /* chosen mode: 1 = tcgen05 split-TF32x3 products, 0 = FP32 SIMT */
+  int jacobi_kernel;       /* 0 = one launch per Jacobi round (cluster-resident pair rows) where
+                              the rows fit shared memory, 1 = always the three-kernel round */
 } qt_config;
 
 typedef struct {
@@ -97,6 +99,13 @@ const char* qt_last_error(const qt_handle* h);
 int qt_abi_version(void);
 /* Kernel launches issued by this handle since creation (a monotone counter). */
 int64_t qt_launch_count(const qt_handle* h);
+/* Algorithmic work issued by this handle since creation (no counterpart in
+ * the reference; measurement hook): out[0] bytes of X and V the Jacobi rounds
+ * must move (every pair's columns read once per round; rotated pairs written
+ * back, their V rows read and written), out[1] Jacobi rounds, out[2] TF32
+ * flops of the tensor-core GEMMs (24 M N K per complex product), out[3] their
+ * launches. */
+int qt_work_counters(const qt_handle* h, double* out);
 
 /* ---- measurement helpers ------------------------------------------------ */
 /* CUDA events on the handle's stream: record into slot 0..7, elapsed a -> b. */
@@ -125,11 +134,24 @@ int qt_contract_pair(qt_handle* h, int dtype,
                      int ndB, const int64_t* dimsB, const void* B,
                      int ncontract, const int* axesA, const int* axesB, void* C);
 
+/* C = alpha op(A) op(B) + beta C, column-major host buffers, op in
+ * {QT_OP_N = 0, QT_OP_C = 2 (conjugate transpose)}; alpha and beta are
+ * {re, im}.  complex64: the tcgen05 split-TF32x3 kernel when cfg.tc_gemm is
+ * set and the product fills a tile, FP32 SIMT otherwise; complex128: FP64
+ * SIMT.  The GEMM of the pairwise contraction (TensorOperations' BLAS gemm
+ * under src/contract.jl:257,263) exposed with explicit operands. */
+int qt_gemm(qt_handle* h, int dtype, int opA, int opB, int64_t M, int64_t N, int64_t K,
+            const double* alpha, const void* A, int64_t lda, const void* B, int64_t ldb,
+            const double* beta, void* C, int64_t ldc);
+
 /* Thin SVD of the m x n matrix M truncated by the tail rule of src/svd.jl:29-33
  * (cutoff = er) and chi_max: U (m x k), S (k), Vh (k x n).  Outputs are sized
  * for kcap = min(m, n) columns/rows; *k receives the kept rank.  Replaces the
  * svd() calls at src/svd.jl:26-27, src/switch.jl (svd of the swapped pair),
- * src/mps.jl:63,73, src/mpo.jl:53,62, src/decompose.jl:26,38. */
+ * src/mps.jl:63,73, src/mpo.jl:53,62, src/decompose.jl:26,38.
+ * mode PLAIN: FP64 one-sided Jacobi; CUSOLVER: zgesvd; CHOSEN with a
+ * complex64 M: FP32-storage Jacobi, cutoff floored at 4 sqrt(max(m,n))
+ * 5.96e-8 ||M||_F (values below are FP32 rounding noise). */
 int qt_truncated_svd(qt_handle* h, int dtype, int64_t m, int64_t n, const void* M,
                      double cutoff, int chi_max, int mode,
                      void* U, double* S, void* Vh, int* k, double* discarded);
@@ -172,6 +194,19 @@ int qt_switch(qt_handle* h, qt_mps* mps, int site);
 int qt_expect_z(qt_handle* h, const qt_mps* mps, int site, double* out);
 int qt_expect_zz(qt_handle* h, const qt_mps* mps, int site, double* out);
 int qt_mps_norm2(qt_handle* h, const qt_mps* mps, double* out);
+
+/* MPO on the device MPS.  W[i] is MPO site i, (bl, 2, 2, br) complex128
+ * column-major (out leg 2, in leg 3, as src/mpo.jl:66), dims 4 per site; end
+ * sites have bl = 1 / br = 1.  qt_mps_apply_mpo contracts the MPO into the
+ * MPS (bond chi*b), replacing the lazy wiring of apply_MPO (src/mpo.jl:184-216)
+ * followed by contract.  qt_mps_compress left-canonicalises with QRs,
+ * optionally normalises, then truncates right to left by the tail rule of
+ * src/svd.jl:29-33 and chi_max (ranks/discarded: nsites-1 entries, may be
+ * NULL).  qt_mps_expect_mpo returns <psi|H|psi>/<psi|psi>. */
+int qt_mps_apply_mpo(qt_handle* h, qt_mps* mps, const double* const* W, const int64_t* dims);
+int qt_mps_compress(qt_handle* h, qt_mps* mps, double cutoff, int chi_max, int mode, int normalize, int* ranks,
+                    double* discarded);
+int qt_mps_expect_mpo(qt_handle* h, const qt_mps* mps, const double* const* W, const int64_t* dims, double* out);
 
 /* Context for the rank model: the spectrum last kept at a bond (the engine
  * records it after every update; callers that built the MPS elsewhere may

@@ -61,7 +61,8 @@ class QtConfig(C.Structure):
     _fields_ = [("device", C.c_int), ("mode", C.c_int), ("cutoff", C.c_double), ("chi_max", C.c_int),
                 ("oversample", C.c_int), ("power_iters", C.c_int), ("renormalize", C.c_int),
                 ("use_rank_model", C.c_int), ("max_sweeps", C.c_int), ("jacobi_tol", C.c_double),
-                ("noise_floor", C.c_double), ("seed", C.c_uint64), ("tc_gemm", C.c_int)]
+                ("noise_floor", C.c_double), ("seed", C.c_uint64), ("tc_gemm", C.c_int),
+                ("jacobi_kernel", C.c_int)]
 
 
 class QtUpdateStats(C.Structure):
@@ -92,6 +93,8 @@ def library() -> C.CDLL:
         "qt_last_error": (C.c_char_p, [P]),
         "qt_abi_version": (I, []),
         "qt_launch_count": (L, [P]),
+        "qt_work_counters": (I, [P, C.POINTER(D)]),
+        "qt_gemm": (I, [P, I, I, I, L, L, L, C.POINTER(D), P, L, P, L, C.POINTER(D), P, L]),
         "qt_contract_pair": (I, [P, I, I, C.POINTER(L), P, I, C.POINTER(L), P, I, C.POINTER(I), C.POINTER(I), P]),
         "qt_truncated_svd": (I, [P, I, L, L, P, D, I, I, P, C.POINTER(D), P, C.POINTER(I), C.POINTER(D)]),
         "qt_contract_svd": (I, [P, I, I, C.POINTER(L), P, I, C.POINTER(L), P, I, I, D, P]),
@@ -140,6 +143,9 @@ def library() -> C.CDLL:
         "qt_batch_bond_dims": (I, [P, P, I, P]),
         "qt_batch_download_site": (I, [P, P, I, I, P]),
         "qt_batch_expect_z": (I, [P, P, I, P]),
+        "qt_mps_apply_mpo": (I, [P, P, C.POINTER(P), C.POINTER(L)]),
+        "qt_mps_compress": (I, [P, P, D, I, I, I, P, P]),
+        "qt_mps_expect_mpo": (I, [P, P, C.POINTER(P), C.POINTER(L), C.POINTER(D)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -234,6 +240,12 @@ class Engine:
         self._check(self._lib.qt_timer_elapsed(self._h, a, b, C.byref(ms)))
         return ms.value
 
+    def work_counters(self) -> dict:
+        """Cumulative algorithmic work: Jacobi bytes/rounds, tensor-core TF32 flops/launches."""
+        out = (C.c_double * 4)()
+        self._check(self._lib.qt_work_counters(self._h, out))
+        return {"jacobi_bytes": out[0], "jacobi_rounds": out[1], "tc_flops": out[2], "tc_launches": out[3]}
+
     def sync(self):
         self._check(self._lib.qt_sync(self._h))
 
@@ -317,6 +329,22 @@ class Engine:
         self._check(self._lib.qt_contract_pair(self._h, _dtype_code(dt), A.ndim, dA, _ptr(A), B.ndim, dB, _ptr(B), nc,
                                                (C.c_int * nc)(*axesA), (C.c_int * nc)(*axesB), _ptr(out)))
         return out
+
+    def gemm(self, A: np.ndarray, B: np.ndarray, opA: str = "N", opB: str = "N", alpha=1.0, beta=0.0, out=None):
+        """alpha op(A) op(B) + beta out on the device (op "N" or "C"); complex64 or complex128."""
+        dt = np.result_type(A.dtype, B.dtype, np.complex64)
+        A = np.asfortranarray(A.astype(dt))
+        B = np.asfortranarray(B.astype(dt))
+        M = A.shape[0] if opA == "N" else A.shape[1]
+        K = A.shape[1] if opA == "N" else A.shape[0]
+        N = B.shape[1] if opB == "N" else B.shape[0]
+        R = np.zeros((M, N), dtype=dt, order="F") if out is None else np.array(out, dtype=dt, order="F")
+        alp = (C.c_double * 2)(float(np.real(alpha)), float(np.imag(alpha)))
+        bet = (C.c_double * 2)(float(np.real(beta)), float(np.imag(beta)))
+        ops = {"N": 0, "C": 2}
+        self._check(self._lib.qt_gemm(self._h, _dtype_code(dt), ops[opA], ops[opB], M, N, K, alp, _ptr(A), A.shape[0],
+                                      _ptr(B), B.shape[0], bet, _ptr(R), M))
+        return R
 
     def truncated_svd(self, M: np.ndarray, cutoff: float = 0.0, chi_max: int = 0, mode: str = "plain"):
         """Exact truncated SVD (tail rule of src/svd.jl:29-33): (U, S, Vh, k, discarded)."""
@@ -499,6 +527,33 @@ class DeviceMPS:
     def set_circuit_position(self, layer: int, depth: int):
         self.eng._check(self.eng._lib.qt_mps_set_circuit_position(self._p, int(layer), int(depth)))
 
+    @staticmethod
+    def _mpo_args(mpo):
+        ws = [np.asfortranarray(np.asarray(w, dtype=np.complex128)) for w in mpo]
+        dims = (C.c_int64 * (4 * len(ws)))(*[d for w in ws for d in w.shape])
+        ptrs = (C.c_void_p * len(ws))(*[w.ctypes.data for w in ws])
+        return ws, ptrs, dims
+
+    def apply_mpo(self, mpo):
+        """Contract MPO sites (bL, out, in, bR) into this MPS (bond chi*b)."""
+        ws, ptrs, dims = self._mpo_args(mpo)
+        self.eng._check(self.eng._lib.qt_mps_apply_mpo(self.eng._h, self._p, ptrs, dims))
+
+    def compress(self, cutoff: float, chi_max: int, mode: str = "plain", normalize: bool = True):
+        """QR left-canonicalisation, optional normalisation, right-to-left truncation."""
+        n = self.nsites
+        ranks = np.zeros(max(n - 1, 1), dtype=np.int32)
+        disc = np.zeros(max(n - 1, 1), dtype=np.float64)
+        self.eng._check(self.eng._lib.qt_mps_compress(self.eng._h, self._p, float(cutoff), int(chi_max), MODES[mode],
+                                                      int(normalize), _ptr(ranks), _ptr(disc)))
+        return ranks[: n - 1], disc[: n - 1]
+
+    def expect_mpo(self, mpo) -> float:
+        ws, ptrs, dims = self._mpo_args(mpo)
+        out = C.c_double()
+        self.eng._check(self.eng._lib.qt_mps_expect_mpo(self.eng._h, self._p, ptrs, dims, C.byref(out)))
+        return out.value
+
     def rank_features(self, gate, i: int, cutoff: float, chi_max: int) -> np.ndarray:
         f = np.zeros(16, dtype=np.float32)
         self.eng._check(self.eng._lib.qt_rank_features_of(self._p, i - 1, _gate_arg(gate), float(cutoff),
@@ -608,3 +663,76 @@ def switch_(mps: DeviceMPS, i: int):
 def apply_2q_(mps: DeviceMPS, gate, i: int, cutoff=None, chi_max=None, mode=None) -> dict:
     """``apply_2q!(mps, G, i; cutoff, chi_max, mode)``."""
     return mps.apply_2q(gate, i, cutoff, chi_max, mode)
+
+
+# ---------------------------------------------------------------------------
+# Network-level drivers of the reference over the engine's GPU primitives
+# ---------------------------------------------------------------------------
+
+def contract_rep(tensors, contractions, openidx) -> List[List[int]]:
+    """``contract_rep`` of src/contract.jl:39-60: ``contractions[i]`` (a list of
+    1-based (tensor, leg) pairs) gets label i + 1, open leg i gets
+    -(i + 1 + #contractions)."""
+    labels = [[0] * np.ndim(t) for t in tensors]
+    for i, summ in enumerate(contractions, 1):
+        for (t, leg) in summ:
+            labels[t - 1][leg - 1] = i
+    nc = len(contractions)
+    for i, (t, leg) in enumerate(openidx, 1):
+        if labels[t - 1][leg - 1] != 0:
+            raise QaintensorError("an open leg is also contracted")
+        labels[t - 1][leg - 1] = -i - nc
+    if any(v == 0 for l in labels for v in l):
+        raise QaintensorError("a leg is neither contracted nor open")
+    return labels
+
+
+def contract(engine: "Engine", tensors, contractions, openidx) -> np.ndarray:
+    """``contract(net)`` of src/contract.jl:242-264 (optimize=false) with every
+    pairwise product on the GPU (``qt_contract_pair``).  The schedule is
+    TensorOperations.ncon's: positive labels in ascending order, each step
+    contracting every label the two operands share; a label repeated on one
+    tensor is traced (a product with the identity); disconnected parts are
+    joined by outer products; the result's axes run -1, -2, ...  The final
+    axis order is a host-side transpose of the result (layout only)."""
+    if len(tensors) == 1:
+        return np.transpose(np.asarray(tensors[0]), [leg - 1 for (_, leg) in openidx])
+    labels = contract_rep(tensors, contractions, openidx)
+    work = [(np.asarray(t), list(l)) for t, l in zip(tensors, labels)]
+    for lab in sorted({v for l in labels for v in l if v > 0}):
+        holders = [k for k, (_, l) in enumerate(work) if lab in l]
+        if not holders:
+            continue  # consumed by an earlier multi-label step
+        if len(holders) == 1:
+            t, l = work[holders[0]]
+            a, b = [i for i, v in enumerate(l) if v == lab]
+            eye = np.eye(t.shape[a], dtype=np.result_type(t.dtype, np.complex64))
+            t = engine.contract_pair(t, eye, [a, b], [0, 1])
+            work[holders[0]] = (t, [v for i, v in enumerate(l) if i not in (a, b)])
+            continue
+        ka, kb = holders
+        (ta, la), (tb, lb) = work[ka], work[kb]
+        common = [v for v in la if v > 0 and v in lb]
+        t = engine.contract_pair(ta, tb, [la.index(v) for v in common], [lb.index(v) for v in common])
+        l = [v for v in la if v not in common] + [v for v in lb if v not in common]
+        work = [w for k, w in enumerate(work) if k not in (ka, kb)] + [(t, l)]
+    t, l = work[0]
+    for tb, lb in work[1:]:
+        t = engine.contract_pair(t, tb, [], [])
+        l = l + lb
+    return np.transpose(t, sorted(range(len(l)), key=lambda i: -l[i])) if l else t
+
+
+def contract_svd_mps(engine: "Engine", tensors, contractions=(), er: float = 0.0) -> np.ndarray:
+    """``contract_svd_mps(tn; er)`` of src/mps.jl:190-201: the left-to-right
+    chain of ``contract_svd`` over the MPS sites, each on the GPU."""
+    if not er >= 0:
+        raise QaintensorError("Error must be positive", QT_EINVAL_ERR_NEG)
+    n = len(tensors)
+    for summ in contractions:
+        if sorted(map(tuple, summ)) == sorted([(n, 3), (1, 1)]):
+            raise QaintensorError("Function doesn't support periodic boundary conditions for now", QT_EPERIODIC)
+    t = np.asarray(tensors[0])
+    for j in range(1, n):
+        t = engine.contract_svd(t, tensors[j], (t.ndim, 1), er)
+    return t

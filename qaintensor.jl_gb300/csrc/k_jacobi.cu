@@ -7,17 +7,17 @@
 //
 // Columns are split into blocks of JW = 8.  One sweep is a round-robin
 // tournament over the blocks; a round processes every block pair (16
-// columns) at once in two kernels:
+// columns) at once in three kernels:
 //   gram   -- grid (pair, row chunk): the 16x16 Gram of the pair over one row
 //             chunk, written as a partial (no atomics: the reduction below
 //             runs in a fixed order, so results are reproducible);
-//   rotate -- grid (pair, row chunk): sums the partials, tests the pair
-//             against `tol` (relative), diagonalises the Gram with a cyclic
-//             two-sided Jacobi in FP64 whose 2x2 rotations use the
-//             relative-accuracy formula (tan from zeta = (beta-alpha)/(2|gamma|),
-//             the smaller root), and applies the 16x16 unitary to its row
-//             chunk of X and of V.  Every chunk solves the same 16x16 problem
-//             with the same arithmetic, so all chunks apply the same unitary.
+//   eig    -- grid (pair): sums the partials, tests the pair against `tol`
+//             (relative), and diagonalises the Gram with a cyclic two-sided
+//             Jacobi in FP64 whose 2x2 rotations use the relative-accuracy
+//             formula (tan from zeta = (beta-alpha)/(2|gamma|), the smaller
+//             root); the 16x16 unitary goes to global memory;
+//   apply  -- grid (pair, row chunk): applies that unitary to its row chunk
+//             of X and of V.
 // A sweep in which no pair rotates ends the iteration.
 //
 // Storage / Gram accumulation: double2 / FP64 for the exact path; float2 /
@@ -29,7 +29,13 @@
 #include <cstring>
 #include <string>
 
+#include <cooperative_groups.h>
+
+#include <type_traits>
+
 #include "qt_internal.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace {
 
@@ -129,27 +135,244 @@ __device__ void apply_rows(TS* __restrict__ M, int64_t ld, int r_begin, int r_en
   }
 }
 
-template <typename TS>
+// Shared state of the 16x16 pair diagonalisation: the Gram and the rotation
+// angles in FP64 (the relative accuracy of the small columns lives in the
+// Gram's small entries, which an FP32 update would swamp with the rounding
+// of the large ones); the accumulated unitary W in RW (the storage
+// precision, in which it is applied).
+template <typename RW>
+struct pair_eig_shared {
+  typedef typename cplx_of<RW>::type CW;
+  double2 G[JC][JC + 1];  // the pair's Gram, driven to diagonal
+  CW W[JC][JC + 1];       // accumulated unitary
+  int rp[JC / 2], rq[JC / 2], ron[JC / 2];
+  double rc[JC / 2], rt[JC / 2], ra[JC / 2], rb[JC / 2];
+  double2 rse[JC / 2];    // s e^{i phi}
+  int inner_rot;
+};
+
+// Cyclic two-sided Jacobi on sh.G (Hermitian 16x16, every thread of the CTA
+// calls it), W accumulating the rotations.  Each 2x2 rotation uses the
+// relative-accuracy formula: tan from zeta = (beta-alpha)/(2|gamma|), the
+// smaller root.  Columns with |x|^2 <= nu2 are at the rounding level of X and
+// are neither rotated nor tested.
+template <typename RW>
+__device__ void diagonalise_pair(pair_eig_shared<RW>& sh, const int* col, double tol_inner, double nu2) {
+  typedef typename cplx_of<RW>::type CW;
+  const int t = threadIdx.x;
+  for (int sweep = 0; sweep < MAX_INNER; sweep++) {
+    __syncthreads();  // every thread has read inner_rot of the previous sweep
+    if (t == 0) sh.inner_rot = 0;
+    __syncthreads();
+    for (int ir = 0; ir < JC - 1; ir++) {
+      if (t < JC / 2) {
+        int p, q;
+        tournament(ir, t, JC, p, q);
+        sh.rp[t] = p; sh.rq[t] = q; sh.ron[t] = 0;
+        if (col[p] >= 0 && col[q] >= 0) {
+          // the running diagonal is clamped at zero (see the update below)
+          const double a = fmax(sh.G[p][p].x, 0.0), b = fmax(sh.G[q][q].x, 0.0);
+          const double2 g = sh.G[p][q];
+          const double ag = sqrt(cabs2(g));
+          if (a > nu2 && b > nu2 && ag > tol_inner * sqrt(a * b)) {
+            const double zeta = (b - a) / (2.0 * ag);
+            const double tt = copysign(1.0, zeta) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+            const double c = 1.0 / sqrt(1.0 + tt * tt);
+            const double sa = c * tt / ag;  // s / |gamma|: s e^{i phi} = sa * gamma
+            sh.ron[t] = 1; sh.rc[t] = c; sh.rt[t] = tt * ag; sh.ra[t] = a; sh.rb[t] = b;
+            sh.rse[t] = make_double2(sa * g.x, sa * g.y);
+            sh.inner_rot = 1;
+          }
+        }
+      }
+      __syncthreads();
+      // columns p, q of G and W:  [x_p, x_q] <- [c x_p - conj(se) x_q,  se x_p + c x_q]
+      {
+        const int task = t & 127, k = task >> 4, r = task & 15;
+        if (sh.ron[k]) {
+          const int p = sh.rp[k], q = sh.rq[k];
+          const double c = sh.rc[k];
+          const double2 se = sh.rse[k];
+          if (t < 128) {
+            const double2 xp = sh.G[r][p], xq = sh.G[r][q];
+            sh.G[r][p] = csub(cscale(xp, c), cmul(cconj(se), xq));
+            sh.G[r][q] = cadd(cmul(se, xp), cscale(xq, c));
+          } else {
+            const CW cw = ccast<CW>(make_double2(c, 0.0));
+            const CW sew = ccast<CW>(se);
+            const CW xp = sh.W[r][p], xq = sh.W[r][q];
+            sh.W[r][p] = csub(cmul(cw, xp), cmul(cconj(sew), xq));
+            sh.W[r][q] = cadd(cmul(sew, xp), cmul(cw, xq));
+          }
+        }
+      }
+      __syncthreads();
+      // rows p, q of G:  [g_p; g_q] <- [c g_p - se g_q;  conj(se) g_p + c g_q]
+      if (t < 128) {
+        const int k = t >> 4, r = t & 15;
+        if (sh.ron[k]) {
+          const int p = sh.rp[k], q = sh.rq[k];
+          const double c = sh.rc[k];
+          const double2 se = sh.rse[k];
+          const double2 gp = sh.G[p][r], gq = sh.G[q][r];
+          sh.G[p][r] = csub(cscale(gp, c), cmul(se, gq));
+          sh.G[q][r] = cadd(cmul(cconj(se), gp), cscale(gq, c));
+        }
+      }
+      __syncthreads();
+      if (t < JC / 2 && sh.ron[t]) {
+        // The rotated 2x2 block is diag(alpha - t|gamma|, beta + t|gamma|).
+        // For nearly parallel columns of very different norms alpha - t|gamma|
+        // cancels and can round below zero; it is clamped at zero so no NaN
+        // reaches a later comparison (the next outer sweep recomputes the
+        // Gram from the rotated vectors themselves).
+        const int p = sh.rp[t], q = sh.rq[t];
+        sh.G[p][q] = make_double2(0, 0);
+        sh.G[q][p] = make_double2(0, 0);
+        sh.G[p][p] = make_double2(fmax(sh.ra[t] - sh.rt[t], 0.0), 0);
+        sh.G[q][q] = make_double2(sh.rb[t] + sh.rt[t], 0);
+      }
+      __syncthreads();
+    }
+    const int again = sh.inner_rot;  // read after the round's closing barrier
+    if (!again) break;
+  }
+  __syncthreads();
+}
+
+// FP32 variant for FP32 storage: the two-sided Jacobi runs on the scaled
+// Gram Ghat = D^{-1/2} G D^{-1/2} (unit diagonal, off-diagonals are the
+// cosines between columns) with the diagonal D tracked separately.  The
+// cosines are O(1) numbers, so FP32 keeps each one accurate to ~u of its
+// own pair whatever the spread of the column norms -- the property the
+// unscaled FP32 Gram loses -- and the rotations are correct to FP32 level
+// right down to the FP32 tolerance.  A rotation J of pair (p, q) acts on
+// Ghat through Jt = D^{1/2} J D'^{-1/2}: Jt_pp = c sqrt(a/a'),
+// Jt_qp = -s e^{-i phi} sqrt(b/a'), Jt_pq = s e^{i phi} sqrt(a/b'),
+// Jt_qq = c sqrt(b/b'), with a' = a - t|gamma|, b' = b + t|gamma|.
+struct pair_eig_scaled {
+  float d[JC];            // current diagonal of G
+  float2 G[JC][JC + 1];   // scaled Gram (diagonal implicit 1)
+  float2 W[JC][JC + 1];   // accumulated unitary
+  int rp[JC / 2], rq[JC / 2], ron[JC / 2];
+  float rc[JC / 2], na[JC / 2], nb[JC / 2], kpp[JC / 2], kqq[JC / 2];
+  float2 rse[JC / 2], kqp[JC / 2], kpq[JC / 2];
+  int inner_rot;
+};
+
+__device__ void diagonalise_scaled(pair_eig_scaled& sh, const int* col, float tol_inner, float nu2) {
+  const int t = threadIdx.x;
+  for (int sweep = 0; sweep < MAX_INNER; sweep++) {
+    __syncthreads();  // every thread has read inner_rot of the previous sweep
+    if (t == 0) sh.inner_rot = 0;
+    __syncthreads();
+    for (int ir = 0; ir < JC - 1; ir++) {
+      if (t < JC / 2) {
+        int p, q;
+        tournament(ir, t, JC, p, q);
+        sh.rp[t] = p; sh.rq[t] = q; sh.ron[t] = 0;
+        const float a = sh.d[p], b = sh.d[q];
+        const float2 gs = sh.G[p][q];
+        const float ags = sqrtf(gs.x * gs.x + gs.y * gs.y);
+        if (col[p] >= 0 && col[q] >= 0 && a > nu2 && b > nu2 && ags > tol_inner) {
+          const float ag = ags * sqrtf(a) * sqrtf(b);  // |gamma|
+          const float zeta = (b - a) / (2.f * ag);
+          const float tt = copysignf(1.f, zeta) / (fabsf(zeta) + sqrtf(1.f + zeta * zeta));
+          const float c = 1.f / sqrtf(1.f + tt * tt), sn = c * tt;
+          const float2 e = make_float2(gs.x / ags, gs.y / ags);
+          const float a2 = fmaxf(a - tt * ag, 0.f), b2 = b + tt * ag;
+          const bool live = a2 > nu2;  // a column driven to the noise level is frozen
+          const float ra = live ? sqrtf(a / a2) : 0.f, rb = live ? sqrtf(b / a2) : 0.f;
+          const float sa = sqrtf(a / b2), sb = sqrtf(b / b2);
+          sh.ron[t] = 1; sh.rc[t] = c; sh.na[t] = a2; sh.nb[t] = b2;
+          sh.rse[t] = make_float2(sn * e.x, sn * e.y);
+          sh.kpp[t] = c * ra;
+          sh.kqp[t] = make_float2(-sn * e.x * rb, sn * e.y * rb);  // -s conj(e) sqrt(b/a')
+          sh.kpq[t] = make_float2(sn * e.x * sa, sn * e.y * sa);   //  s e sqrt(a/b')
+          sh.kqq[t] = c * sb;
+          sh.inner_rot = 1;
+        }
+      }
+      __syncthreads();
+      // columns p, q: Ghat (rows r outside the pair) and W (all rows)
+      {
+        const int task = t & 127, k = task >> 4, r = task & 15;
+        if (sh.ron[k]) {
+          const int p = sh.rp[k], q = sh.rq[k];
+          if (t < 128) {
+            if (r != p && r != q) {
+              const float2 xp = sh.G[r][p], xq = sh.G[r][q];
+              sh.G[r][p] = cadd(cscale(xp, sh.kpp[k]), cmul(sh.kqp[k], xq));
+              sh.G[r][q] = cadd(cmul(sh.kpq[k], xp), cscale(xq, sh.kqq[k]));
+            }
+          } else {
+            const float c = sh.rc[k];
+            const float2 se = sh.rse[k];
+            const float2 xp = sh.W[r][p], xq = sh.W[r][q];
+            sh.W[r][p] = csub(cscale(xp, c), cmul(cconj(se), xq));
+            sh.W[r][q] = cadd(cmul(se, xp), cscale(xq, c));
+          }
+        }
+      }
+      __syncthreads();
+      // rows p, q of Ghat (columns outside the pair): Jt^H from the left
+      if (t < 128) {
+        const int k = t >> 4, r = t & 15;
+        if (sh.ron[k]) {
+          const int p = sh.rp[k], q = sh.rq[k];
+          if (r != p && r != q) {
+            const float2 gp = sh.G[p][r], gq = sh.G[q][r];
+            sh.G[p][r] = cadd(cscale(gp, sh.kpp[k]), cmul(cconj(sh.kqp[k]), gq));
+            sh.G[q][r] = cadd(cmul(cconj(sh.kpq[k]), gp), cscale(gq, sh.kqq[k]));
+          }
+        }
+      }
+      __syncthreads();
+      if (t < JC / 2 && sh.ron[t]) {
+        const int p = sh.rp[t], q = sh.rq[t];
+        sh.G[p][q] = make_float2(0.f, 0.f);
+        sh.G[q][p] = make_float2(0.f, 0.f);
+        sh.d[p] = sh.na[t];
+        sh.d[q] = sh.nb[t];
+      }
+      __syncthreads();
+    }
+    const int again = sh.inner_rot;  // read after the round's closing barrier
+    if (!again) break;
+  }
+  __syncthreads();
+  // W is a product of FP32 rotations, unitary to a few u per rotation; one
+  // Newton-Schulz step W <- W (1.5 I - 0.5 W^H W) brings it back to ~u so
+  // that column norms do not drift over the sweeps (Ghat is free now)
+  {
+    const int i = t >> 4, j = t & 15;
+    float2 p = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int r = 0; r < JC; r++) cfma_conj(p, sh.W[r][i], sh.W[r][j]);
+    sh.G[i][j] = make_float2((i == j ? 1.5f : 0.f) - 0.5f * p.x, -0.5f * p.y);
+    __syncthreads();
+    float2 w = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int k = 0; k < JC; k++) cfma(w, sh.W[i][k], sh.G[k][j]);
+    __syncthreads();
+    sh.W[i][j] = w;
+    __syncthreads();
+  }
+}
+
+// One CTA per block pair: sum the partial Grams, test the pair, and when it
+// needs rotating diagonalise its 16x16 Gram; the unitary goes to wout[pair]
+// and the decision to rot[pair] (the apply kernel reads both).
 __global__ void __launch_bounds__(NT)
-rotate_kernel(TS* __restrict__ X, int64_t ldx, int mm, TS* __restrict__ V, int64_t ldv, int nn, int nb, int round,
-              int nparts, int x_rows_per_chunk, int v_rows_per_chunk, const double2* __restrict__ parts, double tol,
-              double nu_rel2, const double* __restrict__ xnorm2, int* __restrict__ flags) {
-  typedef typename real_of<TS>::type RS;
-  typedef typename cplx_of<RS>::type CS;
-  __shared__ double2 G[JC][JC + 1];
-  __shared__ double2 W[JC][JC + 1];
-  __shared__ CS Wt[JC][JC + 1];
-  __shared__ TS Xs[JR][JC + 1];
+eig_kernel(int nn, int nb, int round, int nparts, const double2* __restrict__ parts, double tol, double nu_rel2,
+           const double* __restrict__ xnorm2, double2* __restrict__ wout, int* __restrict__ rot,
+           int* __restrict__ flags) {
+  __shared__ pair_eig_shared<double> sh;
   __shared__ int col[JC];
-  __shared__ int rp[JC / 2], rq[JC / 2], ron[JC / 2];
-  __shared__ double rc[JC / 2], rs[JC / 2], rt[JC / 2], ra[JC / 2], rb[JC / 2];
-  __shared__ double2 re[JC / 2];
-  __shared__ int any_rot, inner_rot, bad;
+  __shared__ int any_rot, bad;
 
   const int t = threadIdx.x;
-  const int pair = blockIdx.x, chunk = blockIdx.y;
-  // columns with |x|^2 <= nu2 are at the rounding level of X: their values
-  // are known only to ~nu absolutely, so they are neither rotated nor tested
+  const int pair = blockIdx.x;
   const double nu2 = nu_rel2 * (*xnorm2);
   pair_columns(round, pair, nb, nn, col);
   if (t == 0) { any_rot = 0; bad = 0; }
@@ -158,13 +381,16 @@ rotate_kernel(TS* __restrict__ X, int64_t ldx, int mm, TS* __restrict__ V, int64
   for (int e = t; e < NGRAM; e += NT) {
     double2 s = make_double2(0, 0);
     for (int c = 0; c < nparts; c++) s = cadd(s, parts[((size_t)pair * nparts + c) * NGRAM + e]);
-    G[e / JC][e % JC] = s;
-    W[e / JC][e % JC] = make_double2((e / JC) == (e % JC) ? 1.0 : 0.0, 0.0);
+    sh.G[e / JC][e % JC] = s;
+    sh.W[e / JC][e % JC] = make_double2((e / JC) == (e % JC) ? 1.0 : 0.0, 0.0);
     if (!isfinite(s.x) || !isfinite(s.y)) bad = 1;
   }
   __syncthreads();
   if (bad) {
-    if (t == 0 && chunk == 0) atomicOr(&flags[QT_FLAG_NONFINITE], 1);
+    if (t == 0) {
+      atomicOr(&flags[QT_FLAG_NONFINITE], 1);
+      rot[pair] = 0;
+    }
     return;
   }
   // is this pair already orthogonal to tol?  (the largest relative
@@ -172,103 +398,236 @@ rotate_kernel(TS* __restrict__ X, int64_t ldx, int mm, TS* __restrict__ V, int64
   for (int e = t; e < NGRAM; e += NT) {
     const int i = e / JC, j = e % JC;
     if (i < j && col[i] >= 0 && col[j] >= 0) {
-      const double a = G[i][i].x, b = G[j][j].x;
-      const double g = sqrt(cabs2(G[i][j]));
+      const double a = sh.G[i][i].x, b = sh.G[j][j].x;
+      const double g = sqrt(cabs2(sh.G[i][j]));
       if (a > nu2 && b > nu2 && g > tol * sqrt(a * b)) {
         any_rot = 1;
-        if (chunk == 0) {
-          const float rel = (a > 0 && b > 0) ? (float)fmin(g / sqrt(a * b), 1.0) : 1.0f;
-          atomicMax(&flags[QT_FLAG_OFFMAX], __float_as_int(rel));
-        }
+        const float rel = (a > 0 && b > 0) ? (float)fmin(g / sqrt(a * b), 1.0) : 1.0f;
+        atomicMax(&flags[QT_FLAG_OFFMAX], __float_as_int(rel));
       }
     }
   }
   __syncthreads();
+  if (t == 0) rot[pair] = any_rot;
   if (!any_rot) return;
-  if (t == 0 && chunk == 0) atomicAdd(&flags[QT_FLAG_ROTATED], 1);
+  if (t == 0) atomicAdd(&flags[QT_FLAG_ROTATED], 1);
+  // diagonalised well below the outer threshold so that the rounding of the
+  // applied rotation (in the storage precision) cannot leave the pair just
+  // above `tol`
+  diagonalise_pair<double>(sh, col, fmin(tol, 1e-14), nu2);
+  for (int e = t; e < NGRAM; e += NT) wout[(size_t)pair * NGRAM + e] = sh.W[e / JC][e % JC];
+}
 
-  // cyclic two-sided Jacobi on the 16x16 Gram, diagonalised well below the
-  // outer threshold so that the rounding of the applied rotation (in the
-  // storage precision) cannot leave the pair just above `tol`
-  const double tol_inner = fmin(tol, 1e-14);
-  for (int sweep = 0; sweep < MAX_INNER; sweep++) {
-    __syncthreads();  // every thread has read inner_rot of the previous sweep
-    if (t == 0) inner_rot = 0;
-    __syncthreads();
-    for (int ir = 0; ir < JC - 1; ir++) {
-      if (t < JC / 2) {
-        int p, q;
-        tournament(ir, t, JC, p, q);
-        rp[t] = p; rq[t] = q; ron[t] = 0;
-        if (col[p] >= 0 && col[q] >= 0) {
-          // the running diagonal is clamped at zero (see the update below)
-          const double a = fmax(G[p][p].x, 0.0), b = fmax(G[q][q].x, 0.0);
-          const double2 g = G[p][q];
-          const double ag = sqrt(cabs2(g));
-          if (a > nu2 && b > nu2 && ag > tol_inner * sqrt(a * b)) {
-            const double zeta = (b - a) / (2.0 * ag);
-            const double tt = copysign(1.0, zeta) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
-            const double c = 1.0 / sqrt(1.0 + tt * tt);
-            ron[t] = 1; rc[t] = c; rs[t] = c * tt; rt[t] = tt * ag; ra[t] = a; rb[t] = b;
-            re[t] = make_double2(g.x / ag, g.y / ag);  // e^{i phi}
-            inner_rot = 1;
+// out[r, col[c]] = sum_k Xs[k*lds + r] W[k][c] for r < nrows: each thread a
+// 4-row x 4-column tile (rows lane + 32 i, columns 4 cq + j), so one shared
+// load of X feeds four complex FMAs and the global stores run along rows.
+template <typename TS>
+__device__ void rotate_rows(const TS* __restrict__ Xs, int lds, int nrows, TS* __restrict__ out, int64_t ld,
+                            const int* col, const TS (*W)[JC + 1]) {
+  const int t = threadIdx.x, lane = t & 31, cq = (t >> 5) & 3, rg = t >> 7;
+  for (int r0 = rg * 128; r0 < nrows; r0 += 256) {
+    TS acc[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+#pragma unroll
+      for (int j = 0; j < 4; j++) acc[i][j] = czero<TS>();
+#pragma unroll 4
+    for (int k = 0; k < JC; k++) {
+      TS w[4], x[4];
+#pragma unroll
+      for (int j = 0; j < 4; j++) w[j] = W[k][cq * 4 + j];
+#pragma unroll
+      for (int i = 0; i < 4; i++) {
+        const int r = r0 + lane + 32 * i;
+        x[i] = (r < nrows) ? Xs[k * lds + r] : czero<TS>();
+      }
+#pragma unroll
+      for (int i = 0; i < 4; i++)
+#pragma unroll
+        for (int j = 0; j < 4; j++) cfma(acc[i][j], x[i], w[j]);
+    }
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+      const int r = r0 + lane + 32 * i;
+      if (r >= nrows) continue;
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        const int c = col[cq * 4 + j];
+        if (c >= 0) out[r + ld * c] = acc[i][j];
+      }
+    }
+  }
+}
+
+// rows [0, nrows) of the pair's columns of M -> Xs (column c at Xs + c*lds)
+template <typename TS>
+__device__ void stage_rows(const TS* __restrict__ M, int64_t ld, int nrows, int rows_alloc, const int* col,
+                           TS* __restrict__ Xs, int lds) {
+  for (int idx = threadIdx.x; idx < JC * rows_alloc; idx += NT) {
+    const int c = idx / rows_alloc, rr = idx - c * rows_alloc;
+    TS v = czero<TS>();
+    if (rr < nrows && col[c] >= 0) v = M[rr + ld * col[c]];
+    Xs[c * lds + rr] = v;
+  }
+}
+
+// One round of the sweep in one launch.  A thread-block cluster of `csize`
+// CTAs owns one block pair; CTA q of the cluster holds rows
+// [q*xrows_c, (q+1)*xrows_c) of the pair's 16 columns of X in shared memory.
+// Each CTA forms its partial Gram (accumulated in the storage precision: each
+// entry is then accurate relative to its own column norms), the partials are
+// summed in FP64 over the cluster through distributed shared memory in rank
+// order, CTA 0 of the cluster tests the pair and diagonalises the Gram, the
+// other CTAs copy its unitary through distributed shared memory, and every
+// CTA rotates its own rows of X and its share of the rows of V.
+template <typename TS>
+__global__ void __launch_bounds__(NT)
+pair_round_kernel(TS* __restrict__ X, int64_t ldx, int mm, TS* __restrict__ V, int64_t ldv, int nn, int nb, int round,
+                  int csize, int xrows_c, int vrows_c, int lds, double tol, double tol_inner, double nu_rel2,
+                  const double* __restrict__ xnorm2, int* __restrict__ flags) {
+  typedef typename real_of<TS>::type RE;
+  extern __shared__ __align__(16) unsigned char dyn_smem[];
+  TS* Xs = reinterpret_cast<TS*>(dyn_smem);
+  constexpr bool F32 = sizeof(RE) == 4;
+  __shared__ typename std::conditional<F32, pair_eig_scaled, pair_eig_shared<double>>::type sh;
+  __shared__ TS gpart[NGRAM];
+  __shared__ int col[JC];
+  __shared__ int any_rot, bad;
+  cg::cluster_group cluster = cg::this_cluster();
+  const int crank = (int)cluster.block_rank();
+  const int pair = blockIdx.x / csize;
+  const int t = threadIdx.x;
+  pair_columns(round, pair, nb, nn, col);
+  if (t == 0) { any_rot = 0; bad = 0; }
+  __syncthreads();
+  const int xb = crank * xrows_c;
+  const int xr = max(0, min(mm, xb + xrows_c) - xb);
+  stage_rows<TS>(X + xb, ldx, xr, xrows_c, col, Xs, lds);
+  __syncthreads();
+  // partial Gram over this CTA's rows (upper triangle, mirrored)
+  if (t < JC * (JC + 1) / 2) {
+    int r = 0, rem = t;
+    while (rem >= JC - r) { rem -= JC - r; r++; }
+    const int gi = r, gj = r + rem;
+    const TS* xi = Xs + gi * lds;
+    const TS* xj = Xs + gj * lds;
+    TS a0 = czero<TS>(), a1 = czero<TS>();
+    int rr = 0;
+    for (; rr + 1 < xr; rr += 2) {
+      cfma_conj(a0, xi[rr], xj[rr]);
+      cfma_conj(a1, xi[rr + 1], xj[rr + 1]);
+    }
+    if (rr < xr) cfma_conj(a0, xi[rr], xj[rr]);
+    const TS a = cadd(a0, a1);
+    gpart[gi * JC + gj] = a;
+    gpart[gj * JC + gi] = cconj(a);
+  }
+  cluster.sync();
+  const double nu2 = nu_rel2 * (*xnorm2);
+  if (crank == 0) {
+    if constexpr (F32) {
+      // FP64 sums of the partials, then the scaled FP32 Gram
+      __shared__ double dd[JC];
+      if (t < JC) {
+        double s = 0;
+        for (int q = 0; q < csize; q++) s += (double)cluster.map_shared_rank(gpart, q)[t * JC + t].x;
+        dd[t] = s;
+        sh.d[t] = (float)s;
+        if (!isfinite(s)) bad = 1;
+      }
+      __syncthreads();
+      for (int e = t; e < NGRAM; e += NT) {
+        const int i = e / JC, j = e % JC;
+        double2 s = make_double2(0, 0);
+        for (int q = 0; q < csize; q++) s = cadd(s, ccast<double2>(cluster.map_shared_rank(gpart, q)[e]));
+        if (!isfinite(s.x) || !isfinite(s.y)) bad = 1;
+        float2 v = make_float2(0.f, 0.f);
+        if (i != j && dd[i] > nu2 && dd[j] > nu2) {
+          const double sc = 1.0 / sqrt(dd[i] * dd[j]);
+          v = make_float2((float)(s.x * sc), (float)(s.y * sc));
+        }
+        sh.G[i][j] = v;
+        sh.W[i][j] = make_float2(i == j ? 1.f : 0.f, 0.f);
+      }
+    } else {
+      for (int e = t; e < NGRAM; e += NT) {
+        double2 s = make_double2(0, 0);
+        for (int q = 0; q < csize; q++) s = cadd(s, ccast<double2>(cluster.map_shared_rank(gpart, q)[e]));
+        sh.G[e / JC][e % JC] = s;
+        sh.W[e / JC][e % JC] = mk((RE)((e / JC) == (e % JC) ? 1 : 0), (RE)0);
+        if (!isfinite(s.x) || !isfinite(s.y)) bad = 1;
+      }
+    }
+  }
+  cluster.sync();  // the partials have been read: CTAs 1.. may leave or move on
+  if (crank == 0) {
+    // is this pair already orthogonal to tol?  (the largest relative
+    // off-diagonal above tol is recorded as float bits)
+    if (!bad) {
+      for (int e = t; e < NGRAM; e += NT) {
+        const int i = e / JC, j = e % JC;
+        if (i < j && col[i] >= 0 && col[j] >= 0) {
+          double rel = 0;
+          bool live;
+          if constexpr (F32) {
+            live = sh.d[i] > nu2 && sh.d[j] > nu2;
+            rel = sqrt((double)cabs2(sh.G[i][j]));
+          } else {
+            const double a = sh.G[i][i].x, b = sh.G[j][j].x;
+            live = a > nu2 && b > nu2;
+            if (live) rel = sqrt(cabs2(sh.G[i][j])) / sqrt(a * b);
+          }
+          if (live && rel > tol) {
+            any_rot = 1;
+            atomicMax(&flags[QT_FLAG_OFFMAX], __float_as_int((float)fmin(rel, 1.0)));
           }
         }
       }
-      __syncthreads();
-      // columns p, q of G and W:  [x_p, x_q] <- [c x_p - s e^{-i phi} x_q,  s e^{i phi} x_p + c x_q]
-      {
-        const int task = t & 127, k = task >> 4, r = task & 15;
-        if (ron[k]) {
-          double2 (*M)[JC + 1] = (t < 128) ? G : W;
-          const int p = rp[k], q = rq[k];
-          const double c = rc[k], s = rs[k];
-          const double2 e = re[k];
-          const double2 xp = M[r][p], xq = M[r][q];
-          const double2 sem = make_double2(s * e.x, -s * e.y), sep = make_double2(s * e.x, s * e.y);
-          M[r][p] = csub(cscale(xp, c), cmul(sem, xq));
-          M[r][q] = cadd(cmul(sep, xp), cscale(xq, c));
-        }
-      }
-      __syncthreads();
-      // rows p, q of G:  [g_p; g_q] <- [c g_p - s e^{i phi} g_q;  s e^{-i phi} g_p + c g_q]
-      if (t < 128) {
-        const int k = t >> 4, r = t & 15;
-        if (ron[k]) {
-          const int p = rp[k], q = rq[k];
-          const double c = rc[k], s = rs[k];
-          const double2 e = re[k];
-          const double2 gp = G[p][r], gq = G[q][r];
-          const double2 sep = make_double2(s * e.x, s * e.y), sem = make_double2(s * e.x, -s * e.y);
-          G[p][r] = csub(cscale(gp, c), cmul(sep, gq));
-          G[q][r] = cadd(cmul(sem, gp), cscale(gq, c));
-        }
-      }
-      __syncthreads();
-      if (t < JC / 2 && ron[t]) {
-        // The rotated 2x2 block is diag(alpha - t|gamma|, beta + t|gamma|).
-        // For nearly parallel columns of very different norms alpha - t|gamma|
-        // cancels and can round below zero; it is clamped at zero so no NaN
-        // reaches a later comparison (the next outer sweep recomputes the
-        // Gram from the rotated vectors themselves).
-        const int p = rp[t], q = rq[t];
-        G[p][q] = make_double2(0, 0);
-        G[q][p] = make_double2(0, 0);
-        G[p][p] = make_double2(fmax(ra[t] - rt[t], 0.0), 0);
-        G[q][q] = make_double2(rb[t] + rt[t], 0);
-      }
-      __syncthreads();
+    } else if (t == 0) {
+      atomicOr(&flags[QT_FLAG_NONFINITE], 1);
     }
-    const int again = inner_rot;  // read after the round's closing barrier
-    if (!again) break;
+    __syncthreads();
+    if (any_rot) {
+      if (t == 0) atomicAdd(&flags[QT_FLAG_ROTATED], 1);
+      if constexpr (F32) diagonalise_scaled(sh, col, (float)tol_inner, (float)nu2);
+      else diagonalise_pair<RE>(sh, col, tol_inner, nu2);
+    }
   }
-  for (int e = t; e < NGRAM; e += NT) Wt[e / JC][e % JC] = ccast<CS>(W[e / JC][e % JC]);
+  cluster.sync();  // CTA 0's decision and unitary are ready
+  if (crank != 0) {
+    if (t == 0) any_rot = *cluster.map_shared_rank(&any_rot, 0);
+    for (int e = t; e < NGRAM; e += NT) sh.W[e / JC][e % JC] = cluster.map_shared_rank(&sh.W[0][0], 0)[(e / JC) * (JC + 1) + e % JC];
+  }
+  cluster.sync();  // CTA 0 stays resident until every copy is done
+  if (!any_rot) return;  // the same decision in every CTA of the cluster
+  rotate_rows<TS>(Xs, lds, xr, X + xb, ldx, col, sh.W);
+  __syncthreads();  // Xs is reused for V
+  if (V == nullptr) return;  // no accumulated rotations wanted
+  const int vb = crank * vrows_c;
+  const int vr = max(0, min(nn, vb + vrows_c) - vb);
+  stage_rows<TS>(V + vb, ldv, vr, vrows_c, col, Xs, lds);
   __syncthreads();
+  rotate_rows<TS>(Xs, lds, vr, V + vb, ldv, col, sh.W);
+}
 
-  // apply the 16x16 unitary to this chunk's rows of X and of V
+// grid (pair, row chunk): apply the pair's unitary to this chunk's rows of X and V.
+template <typename TS>
+__global__ void __launch_bounds__(NT)
+apply_kernel(TS* __restrict__ X, int64_t ldx, int mm, TS* __restrict__ V, int64_t ldv, int nn, int nb, int round,
+             int x_rows_per_chunk, int v_rows_per_chunk, const double2* __restrict__ win, const int* __restrict__ rot) {
+  typedef typename real_of<TS>::type RS;
+  typedef typename cplx_of<RS>::type CS;
+  __shared__ CS Wt[JC][JC + 1];
+  __shared__ TS Xs[JR][JC + 1];
+  __shared__ int col[JC];
+  const int pair = blockIdx.x, chunk = blockIdx.y;
+  if (!rot[pair]) return;
+  pair_columns(round, pair, nb, nn, col);
+  for (int e = threadIdx.x; e < NGRAM; e += NT) Wt[e / JC][e % JC] = ccast<CS>(win[(size_t)pair * NGRAM + e]);
+  __syncthreads();
   const int xb = chunk * x_rows_per_chunk, vb = chunk * v_rows_per_chunk;
   apply_rows<TS>(X, ldx, xb, min(mm, xb + x_rows_per_chunk), col, Wt, Xs);
-  apply_rows<TS>(V, ldv, vb, min(nn, vb + v_rows_per_chunk), col, Wt, Xs);
+  if (V) apply_rows<TS>(V, ldv, vb, min(nn, vb + v_rows_per_chunk), col, Wt, Xs);
 }
 
 // ||X||_F^2 in FP64, one CTA per column, added into *out.
@@ -300,7 +659,52 @@ int qt_jacobi_layout(int64_t mm, int64_t nn, int* nb_out, int* chunks_out) {
   chunks = std::max(1, std::min<int>(chunks, (int)((mm + 127) / 128)));
   *nb_out = nb;
   *chunks_out = chunks;
-  return pairs * chunks * NGRAM + 1;  // double2 entries: partial Grams + ||X||_F^2
+  // double2 entries: partial Grams, ||X||_F^2, one 16x16 unitary per pair, rotate flags
+  return pairs * chunks * NGRAM + 1 + pairs * NGRAM + (pairs + 1) / 2;
+}
+
+// Cluster shape of the one-launch round: the smallest cluster (<= 8 CTAs)
+// whose row slice of the 16 pair columns fits in FUSED_SMEM bytes of shared
+// memory, widened while the grid would leave SMs idle.  0 = does not fit.
+constexpr size_t FUSED_SMEM = 100 * 1024;
+static int fused_shape(int64_t mm, int pairs, size_t elem, int* rows_c, int* lds, size_t* smem) {
+  int csize = 0;
+  for (int c = 1; c <= 8; c *= 2) {
+    const int64_t rc = (mm + c - 1) / c;
+    if ((size_t)(((rc + 15) / 16) * 16 + 1) * JC * elem <= FUSED_SMEM) { csize = c; break; }
+  }
+  if (csize == 0) return 0;
+  while (csize < 8 && (int64_t)pairs * csize < 152 && (mm + 2 * csize - 1) / (2 * csize) >= 64) csize *= 2;
+  const int64_t rc = (mm + csize - 1) / csize;
+  *rows_c = (int)rc;
+  *lds = (int)(((rc + 15) / 16) * 16 + 1);  // odd multiple-of-16-plus-one stride: conflict-free Gram reads
+  *smem = (size_t)(*lds) * JC * elem;
+  return csize;
+}
+
+template <typename TS>
+static int launch_pair_round(qt_handle* h, int csize, int pairs, size_t smem, TS* X, int64_t ldx, int mm, TS* V,
+                             int64_t ldv, int nn, int nb, int round, int xrows_c, int vrows_c, int lds, double tol,
+                             double tol_inner, double nu_rel2, const double* xnorm2) {
+  cudaLaunchConfig_t lc = {};
+  lc.gridDim = dim3((unsigned)(pairs * csize));
+  lc.blockDim = dim3(NT);
+  lc.dynamicSmemBytes = smem;
+  lc.stream = h->stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = (unsigned)csize;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  lc.attrs = attr;
+  lc.numAttrs = 1;
+  if (h->prof) qt_prof_before(h, "pair_round_kernel<TS>");
+  const cudaError_t e = cudaLaunchKernelEx(&lc, pair_round_kernel<TS>, X, ldx, mm, V, ldv, nn, nb, round, csize,
+                                           xrows_c, vrows_c, lds, tol, tol_inner, nu_rel2, xnorm2, h->d_flags);
+  if (h->prof) qt_prof_after(h);
+  h->launches++;
+  if (e != cudaSuccess) return qt_fail(h, QT_ECUDA, std::string("launch pair_round_kernel: ") + cudaGetErrorString(e));
+  return QT_OK;
 }
 
 template <typename TS>
@@ -308,7 +712,7 @@ int qt_jacobi_svd_ws(qt_handle* h, TS* X, int64_t mm, int64_t nn, int64_t ldx, T
                      int max_sweeps, int* sweeps_out, double2* parts) {
   typedef typename gram_of<TS>::type TG;
   if (mm < nn) return qt_fail(h, QT_EINVAL, "jacobi: needs rows >= columns");
-  QT_TRY(qt_set_identity<TS>(h, V, nn, ldv));
+  if (V) QT_TRY(qt_set_identity<TS>(h, V, nn, ldv));
   *sweeps_out = 0;
   if (nn <= 1) return QT_OK;
   int nb = 0, chunks = 1;
@@ -318,27 +722,57 @@ int qt_jacobi_svd_ws(qt_handle* h, TS* X, int64_t mm, int64_t nn, int64_t ldx, T
   const int vrows = (int)(((nn + chunks - 1) / chunks + JR - 1) / JR * JR);
   const dim3 grid(pairs, chunks);
   // the last workspace entry holds ||X||_F^2 (rotation-invariant); the noise
-  // floor is nu = 4 sqrt(rows) u ||X||_F with u the storage unit roundoff
+  // floor nu (below) is relative to ||X||_F
   double* xnorm2 = reinterpret_cast<double*>(parts + (size_t)pairs * chunks * NGRAM);
+  double2* wbuf = parts + (size_t)pairs * chunks * NGRAM + 1;
+  int* rotf = reinterpret_cast<int*>(wbuf + (size_t)pairs * NGRAM);
   {
     // ||X||_F^2 over the nn columns (ldx may exceed mm)
     QT_CHECK_CUDA(h, cudaMemsetAsync(xnorm2, 0, sizeof(double), h->stream));
     QT_LAUNCH(h, frob_kernel<TS>, (unsigned)nn, 256, 0, X, ldx, (int)mm, xnorm2);
   }
-  const double u = (sizeof(typename real_of<TS>::type) == 8) ? 1.11e-16 : 5.96e-8;
-  const double nu_rel = 4.0 * std::sqrt((double)std::max<int64_t>(mm, 16)) * u;
+  const bool fp32 = sizeof(typename real_of<TS>::type) == 4;
+  const double u = fp32 ? 5.96e-8 : 1.11e-16;
+  // FP32 storage: only columns at the storage resolution of the whole matrix
+  // are frozen -- a chi_max-bound truncation keeps values within a few
+  // sqrt(rows) u of the norm, and those columns must still be orthogonalised
+  const double nu_rel = fp32 ? 4.0 * u : 4.0 * std::sqrt((double)std::max<int64_t>(mm, 16)) * u;
   const double nu_rel2 = nu_rel * nu_rel;
+  // one-launch rounds when the pair's rows fit a cluster's shared memory
+  int xrows_c = 0, lds = 0;
+  size_t smem = 0;
+  const int csize = (h->cfg.jacobi_kernel == 1) ? 0 : fused_shape(mm, pairs, sizeof(TS), &xrows_c, &lds, &smem);
+  const int vrows_c = csize ? (int)((nn + csize - 1) / csize) : 0;
+  // the inner eigen-solve is driven well below the outer threshold so that the
+  // rounding of the applied rotation cannot leave the pair just above `tol`
+  const double tol_inner = fp32 ? tol / 16.0 : std::min(tol, 1e-14);
+  if (csize)
+    QT_CHECK_CUDA(h, cudaFuncSetAttribute(pair_round_kernel<TS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)smem));
   int sweep = 0;
   for (; sweep < max_sweeps; sweep++) {
     QT_CHECK_CUDA(h, cudaMemsetAsync(h->d_flags, 0, sizeof(int) * QT_FLAG_COUNT, h->stream));
     for (int r = 0; r < rounds; r++) {
+      if (csize) {
+        QT_TRY(launch_pair_round<TS>(h, csize, pairs, smem, X, ldx, (int)mm, V, ldv, (int)nn, nb, r, xrows_c, vrows_c,
+                                     lds, tol, tol_inner, nu_rel2, xnorm2));
+        continue;
+      }
       QT_LAUNCH(h, (gram_kernel<TS, TG>), grid, NT, 0, X, ldx, (int)mm, (int)nn, nb, r, xrows, parts);
-      QT_LAUNCH(h, rotate_kernel<TS>, grid, NT, 0, X, ldx, (int)mm, V, ldv, (int)nn, nb, r, chunks, xrows, vrows,
-                (const double2*)parts, tol, nu_rel2, (const double*)xnorm2, h->d_flags);
+      QT_LAUNCH(h, eig_kernel, pairs, NT, 0, (int)nn, nb, r, chunks, (const double2*)parts, tol, nu_rel2,
+                (const double*)xnorm2, wbuf, rotf, h->d_flags);
+      QT_LAUNCH(h, apply_kernel<TS>, grid, NT, 0, X, ldx, (int)mm, V, ldv, (int)nn, nb, r, xrows, vrows,
+                (const double2*)wbuf, (const int*)rotf);
     }
     QT_CHECK_CUDA(h, cudaMemcpyAsync(h->h_flags, h->d_flags, sizeof(int) * QT_FLAG_COUNT, cudaMemcpyDeviceToHost,
                                      h->stream));
     QT_CHECK_CUDA(h, cudaStreamSynchronize(h->stream));
+    {
+      const double es = (double)sizeof(TS);
+      h->work_jacobi_rounds += rounds;
+      h->work_jacobi_bytes += (double)rounds * (double)mm * (double)nn * es +
+                              (double)h->h_flags[QT_FLAG_ROTATED] * JC * es * ((double)mm + (V ? 2.0 * (double)nn : 0.0));
+    }
     if (h->h_flags[QT_FLAG_NONFINITE]) return qt_fail(h, QT_ENUMERIC, "jacobi: non-finite value in the matrix");
     if (h->h_flags[QT_FLAG_ROTATED] == 0) break;
   }

@@ -45,36 +45,58 @@ __global__ void gaussian_kernel(C* __restrict__ out, int64_t rows, int64_t cols,
   }
 }
 
-// Partial Gram of the b (<= 32) columns of Yb over a 64-row slice, added into
-// G (b x b, FP64, full matrix) with atomics.
+// Gram of the b (<= 32) columns of Yb, added into G (32 x 32, upper
+// triangle, FP64) with atomics.  Each CTA sums GR rows at a time over a grid-strided
+// set of row tiles; the per-tile partial sums run in the element precision of
+// Y (each entry then carries a relative error of a few u of its own column
+// norms) and are accumulated across tiles and CTAs in FP64.
+constexpr int GR = 16;
 template <typename C>
 __global__ void __launch_bounds__(256) block_gram_kernel(const C* __restrict__ Y, int64_t m, int b, double2* __restrict__ G) {
-  __shared__ double2 Ys[64][BW + 1];
-  const int64_t r0 = blockIdx.x * 64;
-  for (int idx = threadIdx.x; idx < 64 * BW; idx += 256) {
-    const int rr = idx % 64, c = idx / 64;
-    double2 v = make_double2(0, 0);
-    if (r0 + rr < m && c < b) v = ccast<double2>(Y[(r0 + rr) + m * (int64_t)c]);
-    Ys[rr][c] = v;
+  __shared__ C Ys[GR][BW + 1];
+  // thread t owns entries e = t + 256 h (h = 0..3) of the 32 x 32 Gram: i = e % 32, j = e / 32
+  double2 acc[4];
+#pragma unroll
+  for (int h = 0; h < 4; h++) acc[h] = make_double2(0, 0);
+  for (int64_t r0 = (int64_t)blockIdx.x * GR; r0 < m; r0 += (int64_t)gridDim.x * GR) {
+    for (int idx = threadIdx.x; idx < GR * BW; idx += 256) {
+      const int rr = idx % GR, c = idx / GR;
+      C v = czero<C>();
+      if (r0 + rr < m && c < b) v = Y[(r0 + rr) + m * (int64_t)c];
+      Ys[rr][c] = v;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int h = 0; h < 4; h++) {
+      const int e = threadIdx.x + 256 * h;
+      const int i = e % BW, j = e / BW;
+      if (i <= j && j < b) {
+        C s = czero<C>();
+#pragma unroll
+        for (int rr = 0; rr < GR; rr++) cfma_conj(s, Ys[rr][i], Ys[rr][j]);
+        acc[h] = cadd(acc[h], ccast<double2>(s));
+      }
+    }
+    __syncthreads();
   }
-  __syncthreads();
-  for (int e = threadIdx.x; e < b * b; e += 256) {
-    const int i = e % b, j = e / b;
-    if (i > j) continue;
-    double2 acc = make_double2(0, 0);
-    for (int rr = 0; rr < 64; rr++) cfma_conj(acc, Ys[rr][i], Ys[rr][j]);
-    atomicAdd(&G[i + BW * j].x, acc.x);
-    atomicAdd(&G[i + BW * j].y, acc.y);
+#pragma unroll
+  for (int h = 0; h < 4; h++) {
+    const int e = threadIdx.x + 256 * h;
+    const int i = e % BW, j = e / BW;
+    if (i <= j && j < b) {
+      atomicAdd(&G[i + BW * j].x, acc[h].x);
+      atomicAdd(&G[i + BW * j].y, acc[h].y);
+    }
   }
 }
 
-// Cholesky G = R^H R (R upper) in FP64 on one warp, then Rinv = R^{-1}.
-// `shift` adds shift * trace(G) to the diagonal first.  A non-positive pivot
-// sets QT_FLAG_CHOL and is replaced by a tiny positive value.  Thread t owns
-// column t of R and of Rinv.
-__global__ void chol_inv_kernel(double2* __restrict__ G, int b, double shift, int* __restrict__ flags) {
+// Cholesky G = R^H R (R upper) in FP64 on one warp; R replaces the upper
+// triangle of G.  `shift` adds shift * trace(G) to the diagonal first.  A
+// non-positive pivot sets QT_FLAG_CHOL and is replaced by a tiny positive
+// value.  Thread t owns column t.
+__global__ void chol_kernel(double2* __restrict__ G, int b, double shift, int* __restrict__ flags) {
   __shared__ double2 R[BW][BW + 1];
-  __shared__ double2 Ri[BW][BW + 1];
+  __shared__ double rdiag[BW];  // 1 / R[k][k]: one division per pivot
   __shared__ double tr;
   const int t = threadIdx.x;  // 32 threads
   if (t == 0) {
@@ -94,46 +116,49 @@ __global__ void chol_inv_kernel(double2* __restrict__ G, int b, double shift, in
         atomicOr(&flags[QT_FLAG_CHOL], 1);
         d = fabs(tr) * 1e-30 + 1e-300;
       }
-      R[k][k] = make_double2(sqrt(d), 0.0);
+      const double r = sqrt(d);
+      R[k][k] = make_double2(r, 0.0);
+      rdiag[k] = 1.0 / r;
     }
     __syncwarp();
-    if (t > k && t < b) R[k][t] = cscale(R[k][t], 1.0 / R[k][k].x);
+    if (t > k && t < b) R[k][t] = cscale(R[k][t], rdiag[k]);
     __syncwarp();
     // trailing update of the upper triangle: A[i][t] -= conj(R[k][i]) R[k][t], k < i <= t
     if (t > k && t < b)
       for (int i = k + 1; i <= t; i++) R[i][t] = csub(R[i][t], cmul(cconj(R[k][i]), R[k][t]));
     __syncwarp();
   }
-  // upper-triangular inverse by back substitution, column t
-  for (int i = 0; i < BW; i++) Ri[i][t] = make_double2(0, 0);
-  if (t < b) {
-    for (int i = t; i >= 0; i--) {
-      double2 s = make_double2(i == t ? 1.0 : 0.0, 0.0);
-      for (int j = i + 1; j <= t; j++) s = csub(s, cmul(R[i][j], Ri[j][t]));
-      Ri[i][t] = cscale(s, 1.0 / R[i][i].x);
-    }
-  }
-  __syncwarp();
-  for (int i = 0; i < BW; i++) G[i + BW * t] = Ri[i][t];
+  for (int i = 0; i < BW; i++) G[i + BW * t] = (i <= t) ? R[i][t] : make_double2(0, 0);
 }
 
-// Yb <- Yb Rinv (Rinv upper triangular b x b, FP64 entries).
+// Yb <- Yb R^{-1} (R upper triangular b x b): each thread forward-substitutes
+// one row (y R = x, y_j = (x_j - sum_{k<j} y_k R_kj) / R_jj) in the element
+// precision of Y, with R rounded to it.
 template <typename C>
-__global__ void __launch_bounds__(256) apply_rinv_kernel(C* __restrict__ Y, int64_t m, int b, const double2* __restrict__ Ri) {
-  __shared__ double2 Rs[BW][BW + 1];
-  for (int e = threadIdx.x; e < BW * BW; e += 256) Rs[e % BW][e / BW] = (e % BW < b && e / BW < b) ? Ri[e] : make_double2(0, 0);
+__global__ void __launch_bounds__(128) apply_rinv_kernel(C* __restrict__ Y, int64_t m, int b, const double2* __restrict__ R) {
+  typedef typename real_of<C>::type RS;
+  __shared__ C Rs[BW][BW + 1];
+  __shared__ RS rinv[BW];
+  for (int e = threadIdx.x; e < BW * BW; e += blockDim.x) {
+    const int i = e % BW, j = e / BW;
+    Rs[i][j] = (i < b && j < b) ? ccast<C>(R[e]) : czero<C>();
+  }
+  for (int j = threadIdx.x; j < BW; j += blockDim.x) rinv[j] = (j < b) ? (RS)(1.0 / R[j + BW * j].x) : (RS)0;
   __syncthreads();
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
-    double2 y[BW];
+    C y[BW];
 #pragma unroll
-    for (int k = 0; k < BW; k++) y[k] = (k < b) ? ccast<double2>(Y[i + m * (int64_t)k]) : make_double2(0, 0);
+    for (int j = 0; j < BW; j++) {
+      if (j >= b) break;
+      C s = Y[i + m * (int64_t)j];
 #pragma unroll
-    for (int j = BW - 1; j >= 0; j--) {
-      if (j >= b) continue;
-      double2 s = make_double2(0, 0);
-#pragma unroll
-      for (int k = 0; k <= j; k++) cfma(s, y[k], Rs[k][j]);
-      Y[i + m * (int64_t)j] = ccast<C>(s);
+      for (int k = 0; k < j; k++) {
+        const C r = Rs[k][j];
+        s.x -= y[k].x * r.x - y[k].y * r.y;
+        s.y -= y[k].x * r.y + y[k].y * r.x;
+      }
+      y[j] = cscale(s, rinv[j]);
+      Y[i + m * (int64_t)j] = y[j];
     }
   }
 }
@@ -141,14 +166,15 @@ __global__ void __launch_bounds__(256) apply_rinv_kernel(C* __restrict__ Y, int6
 template <typename C>
 int block_cholqr(qt_handle* h, C* Yb, int64_t m, int b, bool shifted, double2* dG) {
   QT_CHECK_CUDA(h, cudaMemsetAsync(dG, 0, sizeof(double2) * BW * BW, h->stream));
-  QT_LAUNCH(h, block_gram_kernel<C>, (unsigned)((m + 63) / 64), 256, 0, Yb, m, b, dG);
+  const unsigned gg = (unsigned)std::min<int64_t>((m + GR - 1) / GR, 2 * 152);
+  QT_LAUNCH(h, block_gram_kernel<C>, gg, 256, 0, Yb, m, b, dG);
   // shift of shifted CholeskyQR3, sized by the unit roundoff of the stored
   // basis (the Gram and the Cholesky run in FP64, but Y R^{-1} is formed and
   // stored in the element type of Y)
   const double u = (sizeof(typename real_of<C>::type) == 8) ? 1.11e-16 : 5.96e-8;
   const double shift = shifted ? 11.0 * ((double)m * b + (double)b * (b + 1)) * u : 0.0;
-  QT_LAUNCH(h, chol_inv_kernel, 1, 32, 0, dG, b, shift, h->d_flags);
-  QT_LAUNCH(h, apply_rinv_kernel<C>, (unsigned)std::min<int64_t>((m + 255) / 256, 1024), 256, 0, Yb, m, b,
+  QT_LAUNCH(h, chol_kernel, 1, 32, 0, dG, b, shift, h->d_flags);
+  QT_LAUNCH(h, apply_rinv_kernel<C>, (unsigned)std::min<int64_t>((m + 127) / 128, 4 * 152), 128, 0, Yb, m, b,
             (const double2*)dG);
   return QT_OK;
 }

@@ -15,9 +15,14 @@
 // so D[:, 2n] = re C[:, n] and D[:, 2n+1] = im C[:, n] (the lo*lo terms are
 // dropped).  The gather kernels write the planes K-major (row-major M x K),
 // TMA (128B swizzle) stages 128x32 / 256x32 FP32 tiles through a 4-deep
-// mbarrier ring, one elected thread issues tcgen05.mma kind::tf32 with the
-// accumulator in TMEM (128 lanes x 256 columns), and four epilogue warps
-// read TMEM with tcgen05.ld and write interleaved complex64 directly.
+// mbarrier ring, and one elected thread issues tcgen05.mma kind::tf32 into
+// TMEM.  The tensor core's FP32 accumulation loses about one ulp of the
+// running sum per MMA step (measured: a relative error growing linearly with
+// K, ~1e-7 per step), so the K loop is cut into chunks of CK k-blocks (8 MMA
+// steps) accumulated alternately in two TMEM buffers (2 x 256 columns); eight
+// epilogue warps drain each finished chunk with tcgen05.ld into FP32
+// registers (round-to-nearest adds) while the next chunk accumulates in the
+// other buffer, then write interleaved complex64 directly.
 // Every mbarrier wait is bounded by a %globaltimer limit; on expiry the CTA
 // records QT_FLAG_TIMEOUT-style status, drains its copies (bounded), frees
 // TMEM and returns.
@@ -38,8 +43,10 @@ constexpr int A_TILE = BM * BK * 4;          // 16 KiB
 constexpr int B_TILE = BN * BK * 4;          // 32 KiB
 constexpr int STAGE_BYTES = A_TILE + B_TILE;
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
-constexpr int NTHREADS = 192;                // warp 0 TMA, warp 1 MMA, warps 2-5 epilogue
-constexpr uint32_t TMEM_COLS = 256;
+constexpr int NTHREADS = 320;                // warp 0 TMA, warp 1 MMA, warps 2-9 epilogue
+constexpr int NEPI = 8;                      // epilogue warps: two per TMEM sub-partition
+constexpr int CK = 2;                        // k-blocks per accumulation chunk
+constexpr uint32_t TMEM_COLS = 512;          // two 256-column accumulator buffers
 constexpr unsigned long long WAIT_NS = 2000000000ull;  // 2 s per wait
 constexpr int NSEG = 6;
 __constant__ int kSegA[NSEG] = {0, 0, 2, 1, 1, 3};
@@ -63,6 +70,10 @@ __device__ __forceinline__ unsigned long long now_ns() {
 
 __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
 __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
@@ -140,20 +151,25 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
   unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + STAGES * STAGE_BYTES);
   uint64_t* empty = full + STAGES;
-  uint64_t* accum = empty + STAGES;
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(accum + 1);
+  uint64_t* accf = empty + STAGES;  // chunk accumulated in buffer b (MMA -> epilogue)
+  uint64_t* acce = accf + 2;        // buffer b drained (epilogue -> MMA)
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(acce + 2);
   int* fail = reinterpret_cast<int*>(tmem_slot + 1);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
   const int nkb_seg = p.Kp / BK, nkb = nkb_seg * NSEG;
+  const int nch = (nkb + CK - 1) / CK;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; s++) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
     }
-    mbar_init(accum, 1);
+    for (int b = 0; b < 2; b++) {
+      mbar_init(&accf[b], 1);
+      mbar_init(&acce[b], NEPI);
+    }
     *fail = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -188,47 +204,68 @@ tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
   } else if (warp == 1) {
     if (lane == 0) {
       bool ok = true;
-      for (int kb = 0; kb < nkb && ok; kb++) {
-        const int s = kb % STAGES;
-        if (!mbar_wait(&full[s], (kb / STAGES) & 1)) { *fail = 1; ok = false; break; }
+      for (int c = 0; c < nch && ok; c++) {
+        const int b = c & 1;
+        // buffer b is free once the epilogue drained chunk c - 2
+        if (c >= 2 && !mbar_wait(&acce[b], ((c >> 1) - 1) & 1)) { *fail = 1; break; }
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        const uint32_t a0 = smem_u32(smem + s * STAGE_BYTES), b0 = smem_u32(smem + s * STAGE_BYTES + A_TILE);
+        const uint32_t dt = tmem + (uint32_t)(b * 256);
+        const int kb_end = min(nkb, (c + 1) * CK);
+        for (int kb = c * CK; kb < kb_end; kb++) {
+          const int s = kb % STAGES;
+          if (!mbar_wait(&full[s], (kb / STAGES) & 1)) { *fail = 1; ok = false; break; }
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          const uint32_t a0 = smem_u32(smem + s * STAGE_BYTES), b0 = smem_u32(smem + s * STAGE_BYTES + A_TILE);
 #pragma unroll
-        for (int k = 0; k < BK / 8; k++)  // kind::tf32 consumes K = 8 (32 bytes) per instruction
-          umma_tf32(tmem, sdesc(a0 + 32 * k), sdesc(b0 + 32 * k), (kb | k) != 0 ? 1u : 0u);
-        umma_commit(&empty[s]);
+          for (int k = 0; k < BK / 8; k++)  // kind::tf32 consumes K = 8 (32 bytes) per instruction
+            umma_tf32(dt, sdesc(a0 + 32 * k), sdesc(b0 + 32 * k), (kb != c * CK || k != 0) ? 1u : 0u);
+          umma_commit(&empty[s]);
+        }
+        if (ok) umma_commit(&accf[b]);
       }
-      umma_commit(accum);
     }
   } else {
-    // epilogue: warp w reads TMEM lanes 32*(w % 4) .. +31 (its sub-partition)
-    const int quarter = warp & 3;
-    const bool ok = mbar_wait(accum, 0);
-    if (!ok) *fail = 1;
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    if (ok && !*(volatile int*)fail) {
-      const int row = quarter * 32 + lane;
-      const int m = m0 + row;
-      const bool use_beta = (p.beta.x != 0.f || p.beta.y != 0.f);
-#pragma unroll 1
-      for (int c0 = 0; c0 < BN; c0 += 32) {
-        uint32_t r[32];
-        tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)c0, r);
-        if (m < p.M) {
+    // epilogue: warp w drains TMEM lanes 32*(w % 4) .. +31 (its sub-partition),
+    // columns 128*h .. +127 of the buffer, h = (w - 2) / 4
+    const int quarter = warp & 3, half = (warp - 2) >> 2;
+    float acc[128];
 #pragma unroll
-          for (int j = 0; j < 16; j++) {
-            const int n = (n0 + c0) / 2 + j;
-            if (n < p.N) {
-              const float re = __uint_as_float(r[2 * j]), im = __uint_as_float(r[2 * j + 1]);
-              float2 v = make_float2(p.alpha.x * re - p.alpha.y * im, p.alpha.x * im + p.alpha.y * re);
-              float2* dst = p.C + m + p.ldc * (int64_t)n;
-              if (use_beta) {
-                const float2 o = *dst;
-                v.x += p.beta.x * o.x - p.beta.y * o.y;
-                v.y += p.beta.x * o.y + p.beta.y * o.x;
-              }
-              *dst = v;
+    for (int i = 0; i < 128; i++) acc[i] = 0.f;
+    bool ok = true;
+#pragma unroll 1
+    for (int c = 0; c < nch; c++) {
+      const int b = c & 1;
+      if (!mbar_wait(&accf[b], (c >> 1) & 1)) { *fail = 1; ok = false; break; }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t base = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(b * 256 + half * 128);
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        uint32_t r[32];
+        tmem_ld32(base + (uint32_t)(q * 32), r);
+#pragma unroll
+        for (int i = 0; i < 32; i++) acc[q * 32 + i] += __uint_as_float(r[i]);
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&acce[b]);
+    }
+    if (ok && !*(volatile int*)fail) {
+      const int m = m0 + quarter * 32 + lane;
+      const bool use_beta = (p.beta.x != 0.f || p.beta.y != 0.f);
+      if (m < p.M) {
+#pragma unroll
+        for (int j = 0; j < 64; j++) {
+          const int n = (n0 + half * 128) / 2 + j;
+          if (n < p.N) {
+            const float re = acc[2 * j], im = acc[2 * j + 1];
+            float2 v = make_float2(p.alpha.x * re - p.alpha.y * im, p.alpha.x * im + p.alpha.y * re);
+            float2* dst = p.C + m + p.ldc * (int64_t)n;
+            if (use_beta) {
+              const float2 o = *dst;
+              v.x += p.beta.x * o.x - p.beta.y * o.y;
+              v.y += p.beta.x * o.y + p.beta.y * o.x;
             }
+            *dst = v;
           }
         }
       }
@@ -357,11 +394,13 @@ int qt_cgemm_tc(qt_handle* h, int opA, int opB, int64_t M, int64_t N, int64_t K,
   const int64_t Mp = round_up(M, BM), N2p = round_up(2 * N, BN), Kp = round_up(std::max<int64_t>(K, 1), BK);
   qt_scratch s(h);
   float *pa, *pb;
-  int* status;
+  int* status = h->d_status;  // sticky: checked by qt_check_status where the caller synchronises
   QT_TRY(s.get(&pa, (size_t)4 * Mp * Kp));
   QT_TRY(s.get(&pb, (size_t)4 * N2p * Kp));
-  QT_TRY(s.get(&status, 1));
-  QT_CHECK_CUDA(h, cudaMemsetAsync(status, 0, sizeof(int), h->stream));
+  if (!status) {
+    QT_TRY(s.get(&status, 1));
+    QT_CHECK_CUDA(h, cudaMemsetAsync(status, 0, sizeof(int), h->stream));
+  }
   {
     dim3 grid((unsigned)(Kp / 32), (unsigned)(Mp / 32));
     QT_LAUNCH(h, gather_a_kernel, grid, dim3(32, 8), 0, A, lda, opA == QT_OP_C ? 1 : 0, (int)M, (int)K, (int)Mp,
@@ -385,9 +424,13 @@ int qt_cgemm_tc(qt_handle* h, int opA, int opB, int64_t M, int64_t N, int64_t K,
   p.alpha = alpha; p.beta = beta; p.C = C; p.ldc = ldc; p.status = status;
   dim3 grid((unsigned)(Mp / BM), (unsigned)(N2p / BN));
   QT_LAUNCH(h, tc_gemm_kernel, grid, NTHREADS, SMEM_BYTES, ma, mb, p);
-  int hs = 0;
-  QT_CHECK_CUDA(h, cudaMemcpyAsync(&hs, status, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
-  QT_CHECK_CUDA(h, cudaStreamSynchronize(h->stream));
-  if (hs) return qt_fail(h, QT_ETIMEOUT, "tc gemm: a pipeline wait timed out");
+  h->work_tc_flops += 24.0 * (double)M * (double)N * (double)K;
+  h->work_tc_launches += 1;
+  if (status != h->d_status) {  // a handle without a status word: check here
+    int hs = 0;
+    QT_CHECK_CUDA(h, cudaMemcpyAsync(&hs, status, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    QT_CHECK_CUDA(h, cudaStreamSynchronize(h->stream));
+    if (hs) return qt_fail(h, QT_ETIMEOUT, "tc gemm: a pipeline wait timed out");
+  }
   return QT_OK;
 }

@@ -21,6 +21,16 @@ int qt_fail(qt_handle* h, int code, const std::string& msg) {
   return code;
 }
 
+int qt_check_status(qt_handle* h) {
+  if (!h->d_status) return QT_OK;
+  int hs = 0;
+  QT_CHECK_CUDA(h, cudaMemcpyAsync(&hs, h->d_status, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+  QT_CHECK_CUDA(h, cudaStreamSynchronize(h->stream));
+  if (!hs) return QT_OK;
+  QT_CHECK_CUDA(h, cudaMemsetAsync(h->d_status, 0, sizeof(int), h->stream));
+  return qt_fail(h, QT_ETIMEOUT, "tc gemm: a pipeline wait timed out");
+}
+
 int qt_dmalloc(qt_handle* h, void** p, size_t bytes) {
   cudaError_t e = cudaMallocFromPoolAsync(p, bytes ? bytes : 16, h->pool, h->stream);
   if (e != cudaSuccess) {
@@ -39,6 +49,15 @@ static size_t elem_size(int dtype) { return dtype == QT_C64 ? sizeof(float2) : s
 
 extern "C" int qt_abi_version(void) { return QT_ABI_VERSION; }
 
+extern "C" int qt_work_counters(const qt_handle* h, double* out) {
+  if (!h || !out) return QT_EINVAL;
+  out[0] = h->work_jacobi_bytes;
+  out[1] = h->work_jacobi_rounds;
+  out[2] = h->work_tc_flops;
+  out[3] = h->work_tc_launches;
+  return QT_OK;
+}
+
 extern "C" int qt_config_default(qt_config* cfg) {
   if (!cfg) return QT_EINVAL;
   std::memset(cfg, 0, sizeof(*cfg));
@@ -55,6 +74,7 @@ extern "C" int qt_config_default(qt_config* cfg) {
   cfg->noise_floor = 0.0;    // 0: 4 * 2^-23 (FP32-level products)
   cfg->seed = 0x5eed5eedull;
   cfg->tc_gemm = 0;
+  cfg->jacobi_kernel = 0;
   return QT_OK;
 }
 
@@ -79,6 +99,8 @@ extern "C" int qt_create(qt_handle** out, const qt_config* cfg) {
     if (cudaMalloc(&h->d_flags, sizeof(int) * QT_FLAG_COUNT) != cudaSuccess) { rc = QT_ENOMEM; break; }
     if (cudaMallocHost(&h->h_flags, sizeof(int) * QT_FLAG_COUNT) != cudaSuccess) { rc = QT_ENOMEM; break; }
     cudaMemset(h->d_flags, 0, sizeof(int) * QT_FLAG_COUNT);
+    if (cudaMalloc(&h->d_status, sizeof(int)) != cudaSuccess) { rc = QT_ENOMEM; break; }
+    cudaMemset(h->d_status, 0, sizeof(int));
     h->rank_model = qt_rank_model_create();
   } while (0);
   if (rc != QT_OK) {
@@ -99,6 +121,7 @@ extern "C" int qt_destroy(qt_handle* h) {
   for (cudaEvent_t e : h->timers)
     if (e) cudaEventDestroy(e);
   if (h->d_flags) cudaFree(h->d_flags);
+  if (h->d_status) cudaFree(h->d_status);
   if (h->h_flags) cudaFreeHost(h->h_flags);
   if (h->pool) cudaMemPoolDestroy(h->pool);
   if (h->stream) cudaStreamDestroy(h->stream);
@@ -505,6 +528,131 @@ int svd_split_jacobi(qt_handle* h, TS* M, int64_t m, int64_t n, double cutoff, i
   return QT_OK;
 }
 
+// out[:, j] = X[:, perm[j]] / sigma_j (zero columns stay zero).
+template <typename C>
+__global__ void gather_unit_cols_kernel(const C* __restrict__ X, int64_t rows, int64_t ldx, const int* __restrict__ perm,
+                                        const double* __restrict__ sig, int k, C* __restrict__ out) {
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < rows * k;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = idx % rows, j = idx / rows;
+    const double s = sig[j];
+    const typename real_of<C>::type inv = (typename real_of<C>::type)(s > 0 ? 1.0 / s : 0.0);
+    out[i + rows * j] = cscale(X[i + ldx * perm[j]], inv);
+  }
+}
+
+// out[j] = ||row j of B|| (B: k x n, ld k) in FP64, one CTA per row.
+__global__ void row_norms_kernel(const float2* __restrict__ B, int k, int64_t n, double* __restrict__ out) {
+  const int j = blockIdx.x;
+  double s = 0;
+  for (int64_t c = threadIdx.x; c < n; c += blockDim.x) {
+    const float2 v = B[j + (int64_t)k * c];
+    s = fma((double)v.x, (double)v.x, s);
+    s = fma((double)v.y, (double)v.y, s);
+  }
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  __shared__ double red[32];
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double tot = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) tot += red[w];
+    out[j] = sqrt(tot);
+  }
+}
+
+// W = 1.5 I - 0.5 G (k x k): one Newton-Schulz step towards G^{-1/2}.
+__global__ void newton_schulz_kernel(const float2* __restrict__ G, int k, float2* __restrict__ W) {
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < (int64_t)k * k;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = idx % k, j = idx / k;
+    const float2 g = G[idx];
+    W[idx] = make_float2((i == j ? 1.5f : 0.f) - 0.5f * g.x, -0.5f * g.y);
+  }
+}
+
+// Chosen-mode noise floor: singular values whose tail lies below
+// floor_rel ||theta'||_F are rounding noise of complex64 storage and of the
+// FP32-level (split-TF32x3) products: 4 sqrt(max(m, n)) u_fp32.
+double fp32_floor_rel(const qt_handle* h, int64_t m, int64_t n) {
+  return h->cfg.noise_floor > 0 ? h->cfg.noise_floor : 4.0 * std::sqrt((double)std::max(m, n)) * 5.96e-8;
+}
+
+// FP32-storage truncated split of theta (m x n, ld m, not modified): the
+// one-sided block Jacobi runs on theta itself (tall or square) or on
+// theta^H (wide), with no QR preconditioning -- theta' may be numerically
+// rank-deficient at FP32 resolution, where a Cholesky-based QR breaks down
+// while Jacobi only stops rotating the noise-level columns.
+//   tall/square: X = theta V (V not accumulated); A' = unit columns of X for
+//     the k largest norms;
+//   wide: X = theta^H V, V (m x m) accumulated; A' = V[:, perm].
+// Either A' is orthonormal only to the Jacobi tolerance (FP32: ~1e-5); one
+// Newton-Schulz step A' <- A' (1.5 I - 0.5 A'^H A') makes it orthonormal to
+// FP32 rounding, and B' = A'^H theta is the exact projection onto it (both
+// tensor-core GEMMs), so A' B' carries no error beyond the truncation.
+// `extra_tail` (>= 0) is a weight outside this factorisation (a sketch's
+// residual), counted as the smallest tail value of the rank rule.
+template <typename TO>
+int svd_split_direct32(qt_handle* h, const float2* theta, int64_t m, int64_t n, double cutoff, int chi_max,
+                       TO** Aout, TO** Bout, SvdOut* o, double extra_tail = -1.0) {
+  qt_scratch s(h);
+  const bool wide = m < n;
+  const int64_t rows = wide ? n : m, cols = wide ? m : n;
+  float2 *X, *V = nullptr;
+  QT_TRY(s.get(&X, (size_t)rows * cols));
+  if (wide) {
+    QT_TRY(qt_adjoint_copy<float2>(h, theta, m, n, m, X, n));
+    QT_TRY(s.get(&V, (size_t)cols * cols));
+  } else {
+    QT_CHECK_CUDA(h, cudaMemcpyAsync(X, theta, sizeof(float2) * m * n, cudaMemcpyDeviceToDevice, h->stream));
+  }
+  QT_TRY(qt_jacobi_svd<float2>(h, X, rows, cols, rows, V, cols, auto_tol(h, rows, true), h->cfg.max_sweeps,
+                               &o->sweeps));
+  double* sig;
+  int* perm;
+  QT_TRY(s.get(&sig, (size_t)cols));
+  QT_TRY(s.get(&perm, (size_t)cols));
+  QT_TRY(qt_sorted_column_norms<float2>(h, X, rows, cols, rows, sig, perm));
+  o->s.resize(cols);
+  QT_CHECK_CUDA(h, cudaMemcpyAsync(o->s.data(), sig, sizeof(double) * cols, cudaMemcpyDeviceToHost, h->stream));
+  QT_CHECK_CUDA(h, cudaStreamSynchronize(h->stream));
+  if (extra_tail >= 0) {
+    std::vector<double> sx = o->s;
+    sx.push_back(extra_tail);
+    QT_TRY(choose_rank(h, sx, cutoff, chi_max, o));
+    if (o->k > (int)cols) o->k = (int)cols;
+  } else {
+    QT_TRY(choose_rank(h, o->s, cutoff, chi_max, o));
+  }
+  const int k = o->k;
+  const double sc = renorm_scale(h, *o);
+  const float2 one = make_float2(1, 0), zero = make_float2(0, 0);
+  float2 *At, *Bt;
+  QT_TRY(s.get(&At, (size_t)m * k));
+  QT_TRY(s.get(&Bt, (size_t)k * n));
+  float2 *A0, *G, *W;
+  QT_TRY(s.get(&A0, (size_t)m * k));
+  QT_TRY(s.get(&G, (size_t)k * k));
+  QT_TRY(s.get(&W, (size_t)k * k));
+  if (!wide) QT_LAUNCH(h, gather_unit_cols_kernel<float2>, 256, 256, 0, X, m, m, perm, sig, k, A0);
+  else QT_LAUNCH(h, gather_cols_kernel<float2>, 256, 256, 0, V, m, m, perm, k, A0);
+  QT_TRY(qt_gemm_any(h, QT_OP_C, QT_OP_N, k, k, m, one, A0, m, A0, m, zero, G, k));
+  QT_LAUNCH(h, newton_schulz_kernel, 256, 256, 0, G, k, W);
+  QT_TRY(qt_gemm_any(h, QT_OP_N, QT_OP_N, m, k, k, one, A0, m, W, k, zero, At, m));
+  QT_TRY(qt_gemm_any(h, QT_OP_C, QT_OP_N, k, n, m, one, At, m, theta, m, zero, Bt, k));
+  {
+    // the kept values as reported: norms of the rows of B' = A'^H theta (an
+    // exact projection, free of the small drift of the Jacobi column norms)
+    QT_LAUNCH(h, row_norms_kernel, (unsigned)k, 256, 0, Bt, k, n, sig);
+    QT_CHECK_CUDA(h, cudaMemcpyAsync(o->s.data(), sig, sizeof(double) * k, cudaMemcpyDeviceToHost, h->stream));
+  }
+  QT_TRY(qt_dmalloc(h, (void**)Aout, sizeof(TO) * m * k));
+  QT_TRY(qt_dmalloc(h, (void**)Bout, sizeof(TO) * k * n));
+  QT_LAUNCH(h, (convert_scale_kernel<float2, TO>), 256, 256, 0, At, *Aout, (int64_t)m * k, 1.0);
+  QT_LAUNCH(h, (convert_scale_kernel<float2, TO>), 256, 256, 0, Bt, *Bout, (int64_t)k * n, sc);
+  return QT_OK;
+}
+
 __global__ void scale_columns_kernel(double2* X, int64_t rows, int64_t cols, int64_t ld, const double* s) {
   for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < rows * cols;
        idx += (int64_t)gridDim.x * blockDim.x) {
@@ -579,19 +727,13 @@ int svd_split_cusolver(qt_handle* h, double2* theta, int64_t m, int64_t n, doubl
   return QT_OK;
 }
 
-__global__ void gather_columns_kernel(const float2* __restrict__ V, int64_t rows, int64_t ldv, const int* __restrict__ perm,
-                                      int k, float2* __restrict__ out) {
-  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < rows * k;
-       idx += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t i = idx % rows, j = idx / rows;
-    out[i + rows * j] = V[i + ldv * perm[j]];
-  }
-}
 
 // Chosen mode: FP32-level products, randomized range finder sized by the
-// predicted rank, FP64 orthogonalisation and FP64-angle Jacobi on the small
-// projected matrix; exact FP64 SVD as fallback when the sketch's residual
-// exceeds the effective cutoff.  theta is m x n float2 (ld m).
+// predicted rank, FP32-storage one-sided Jacobi on the small projected matrix
+// (FP64 Gram/angles); exact FP64 SVD as fallback when the tail rule needs
+// more values than the sketch holds, when the sketch basis lost rank, or when
+// the Jacobi does not settle.  theta is m x n float2 (ld m); it is
+// overwritten by the sketch residual.
 template <typename TO>
 int svd_split_chosen(qt_handle* h, float2* theta, int64_t m, int64_t n, double cutoff, int chi_max, int kpred,
                      TO** Aout, TO** Bout, SvdOut* o, int* sketch, int* fallback, double* residual) {
@@ -603,19 +745,24 @@ int svd_split_chosen(qt_handle* h, float2* theta, int64_t m, int64_t n, double c
   double tn2 = 0;
   QT_CHECK_CUDA(h, cudaMemcpyAsync(&tn2, dn, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
   QT_CHECK_CUDA(h, cudaStreamSynchronize(h->stream));
-  // singular values below 4 sqrt(rows) u_fp32 ||theta'|| are rounding noise of
-  // FP32-level products; the same floor bounds the FP32-storage Jacobi
-  const double floor_rel =
-      h->cfg.noise_floor > 0 ? h->cfg.noise_floor : 4.0 * std::sqrt((double)std::max(m, n)) * 5.96e-8;
-  const double eff_cut = std::max(cutoff, floor_rel * std::sqrt(tn2));
+  const double eff_cut = std::max(cutoff, fp32_floor_rel(h, m, n) * std::sqrt(tn2));
   int64_t l = (kpred > 0 ? kpred : kmin) + std::max(0, h->cfg.oversample);
+  // A rank predicted at the chi_max cap is pinned there by a spectrum that
+  // is still decaying slowly at the cap; a sketch of cap + oversample then
+  // misses the kept space by far more than the exact truncation does, so the
+  // sketch is widened to twice the cap (or the whole matrix).
+  const bool cap_bound = chi_max > 0 && chi_max < kmin && kpred > 0 && kpred + h->cfg.oversample >= 0.9 * chi_max;
+  if (cap_bound) l = std::max<int64_t>(l, 2 * (int64_t)chi_max);
   l = ((l + 7) / 8) * 8;
   *fallback = 0;
   *residual = 0;
-  if (l >= kmin || kmin <= 32) {
+  // A sketch of three quarters of the matrix or more saves less in the small
+  // SVD than its range finder and orthogonalisation cost: factor theta'
+  // directly.
+  if (4 * l >= 3 * kmin || kmin <= 32) {
     *sketch = 0;
-    const int rc = svd_split_jacobi<float2, TO>(h, theta, m, n, eff_cut, chi_max, true, Aout, Bout, o);
-    if (rc == QT_ENUMERIC) {  // FP32-storage Jacobi did not settle: exact FP64 path
+    const int rc = svd_split_direct32<TO>(h, theta, m, n, eff_cut, chi_max, Aout, Bout, o);
+    if (rc == QT_ENUMERIC) {  // the FP32-storage Jacobi did not settle: exact FP64 path
       qt_dfree(h, *Aout);
       qt_dfree(h, *Bout);
       *Aout = *Bout = nullptr;
@@ -631,6 +778,7 @@ int svd_split_chosen(qt_handle* h, float2* theta, int64_t m, int64_t n, double c
   QT_TRY(s.get(&Y, (size_t)m * l));
   QT_TRY(s.get(&Z, (size_t)n * l));
   QT_TRY(s.get(&BH, (size_t)n * l));
+  QT_CHECK_CUDA(h, cudaMemsetAsync(h->d_flags + QT_FLAG_CHOL, 0, sizeof(int), h->stream));
   // range finder: Y = theta Omega, q rounds of subspace iteration
   QT_TRY(qt_gaussian<float2>(h, om, n, l, n, h->cfg.seed + 0x9E37ull * (++h->sketch_counter)));
   QT_TRY(qt_gemm_any(h, QT_OP_N, QT_OP_N, m, l, n, one, theta, m, om, n, zero, Y, m));
@@ -641,6 +789,17 @@ int svd_split_chosen(qt_handle* h, float2* theta, int64_t m, int64_t n, double c
     QT_TRY(qt_gemm_any(h, QT_OP_N, QT_OP_N, m, l, n, one, theta, m, Z, n, zero, Y, m));
     QT_TRY(qt_orthonormalize<float2>(h, Y, m, l));
   }
+  {
+    // a Cholesky pivot that vanished means the sketch held fewer than l
+    // numerically independent directions: the basis is not trustworthy
+    int chol = 0;
+    QT_CHECK_CUDA(h, cudaMemcpyAsync(&chol, h->d_flags + QT_FLAG_CHOL, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    QT_CHECK_CUDA(h, cudaStreamSynchronize(h->stream));
+    if (chol) {
+      *fallback = 3;
+      return QT_OK;
+    }
+  }
   // B^H = theta^H Q (n x l); residual theta - Q B
   QT_TRY(qt_gemm_any(h, QT_OP_C, QT_OP_N, n, l, m, one, theta, m, Y, m, zero, BH, n));
   QT_TRY(qt_gemm_any(h, QT_OP_N, QT_OP_C, m, n, l, mone, Y, m, BH, n, one, theta, m));
@@ -649,14 +808,14 @@ int svd_split_chosen(qt_handle* h, float2* theta, int64_t m, int64_t n, double c
   QT_CHECK_CUDA(h, cudaMemcpyAsync(&res2, dn, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
   QT_CHECK_CUDA(h, cudaStreamSynchronize(h->stream));
   *residual = std::sqrt(res2);
-  // small SVD of B = Q^H theta' (l x n, wide): the QR-preconditioned Jacobi
-  // split B ~ Ab Bb, the residual weight counted in the tail rule
+  // small SVD of B = Q^H theta' (l x n, wide), the residual weight counted in
+  // the tail rule
   float2* Bm;
   QT_TRY(s.get(&Bm, (size_t)l * n));
   QT_TRY(qt_adjoint_copy<float2>(h, BH, n, l, n, Bm, l));
   float2 *Ab = nullptr, *Bb = nullptr;
   {
-    const int rc = svd_split_jacobi<float2, float2>(h, Bm, l, n, eff_cut, chi_max, true, &Ab, &Bb, o, *residual);
+    const int rc = svd_split_direct32<float2>(h, Bm, l, n, eff_cut, chi_max, &Ab, &Bb, o, *residual);
     if (rc == QT_ENUMERIC) {  // the small SVD did not settle: exact FP64 path
       qt_dfree(h, Ab);
       qt_dfree(h, Bb);
@@ -665,7 +824,8 @@ int svd_split_chosen(qt_handle* h, float2* theta, int64_t m, int64_t n, double c
     }
     QT_TRY(rc);
   }
-  if (o->k_cut > (int)l) {  // the cutoff needs more than the sketch holds
+  const bool held_by_cap = chi_max > 0 && chi_max + std::max(0, h->cfg.oversample) <= l;
+  if (o->k_cut > (int)l && !held_by_cap) {  // the cutoff needs more than the sketch holds
     qt_dfree(h, Ab);
     qt_dfree(h, Bb);
     *fallback = 1;
@@ -686,6 +846,50 @@ int svd_split_chosen(qt_handle* h, float2* theta, int64_t m, int64_t n, double c
 }
 
 }  // namespace
+
+// Truncated split M (m x n, device, element of `dtype`) ~ A (m x k) B (k x n),
+// A orthonormal, B = diag(S) V^H; A, B are pool allocations the caller frees.
+// Plain mode runs the exact FP64 path; chosen mode on complex64 keeps FP32
+// storage.
+int qt_split_device(qt_handle* h, int dtype, const void* M, int64_t m, int64_t n, double cutoff, int chi_max, int mode,
+                    void** A, void** B, int* k, double* discarded) {
+  SvdOut o;
+  *A = *B = nullptr;
+  int rc;
+  if (dtype == QT_C128) {
+    qt_scratch s(h);
+    double2* Mc;
+    QT_TRY(s.get(&Mc, (size_t)m * n));
+    QT_CHECK_CUDA(h, cudaMemcpyAsync(Mc, M, sizeof(double2) * m * n, cudaMemcpyDeviceToDevice, h->stream));
+    rc = svd_split_jacobi<double2, double2>(h, Mc, m, n, cutoff, chi_max, false, (double2**)A, (double2**)B, &o);
+  } else if (mode == QT_MODE_CHOSEN) {
+    qt_scratch s(h);
+    double* dn;
+    QT_TRY(s.get(&dn, 1));
+    QT_TRY(qt_norm2<float2>(h, (const float2*)M, m * n, dn));
+    double n2 = 0;
+    QT_CHECK_CUDA(h, cudaMemcpyAsync(&n2, dn, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    QT_CHECK_CUDA(h, cudaStreamSynchronize(h->stream));
+    rc = svd_split_direct32<float2>(h, (const float2*)M, m, n, std::max(cutoff, fp32_floor_rel(h, m, n) * std::sqrt(n2)),
+                                    chi_max, (float2**)A, (float2**)B, &o);
+  } else {
+    qt_scratch s(h);
+    double2* Mc;
+    QT_TRY(s.get(&Mc, (size_t)m * n));
+    QT_TRY(qt_convert(h, M, QT_C64, Mc, QT_C128, m * n));
+    rc = svd_split_jacobi<double2, float2>(h, Mc, m, n, cutoff, chi_max, false, (float2**)A, (float2**)B, &o);
+  }
+  if (rc == QT_OK) rc = qt_check_status(h);
+  if (rc != QT_OK) {
+    qt_dfree(h, *A);
+    qt_dfree(h, *B);
+    *A = *B = nullptr;
+    return rc;
+  }
+  *k = o.k;
+  if (discarded) *discarded = o.discarded;
+  return QT_OK;
+}
 
 // ---------------------------------------------------------------------------
 // the update
@@ -744,6 +948,7 @@ static int update_impl(qt_handle* h, qt_mps* mps, int site, const double* G, dou
       else rc = svd_split_jacobi<double2, TO>(h, th, m, n, cutoff, chi_max, false, &An, &Bn, &o);
     }
   }
+  if (rc == QT_OK) rc = qt_check_status(h);
   if (rc != QT_OK) {
     qt_dfree(h, An);
     qt_dfree(h, Bn);
@@ -901,6 +1106,40 @@ int contract_pair_t(qt_handle* h, int ndA, const int64_t* dA, const C* A, int nd
 
 }  // namespace
 
+extern "C" int qt_gemm(qt_handle* h, int dtype, int opA, int opB, int64_t M, int64_t N, int64_t K,
+                       const double* alpha, const void* A, int64_t lda, const void* B, int64_t ldb,
+                       const double* beta, void* C, int64_t ldc) {
+  if (!h || !alpha || !beta || !A || !B || !C) return qt_fail(h, QT_EINVAL, "gemm: null argument");
+  if (M < 1 || N < 1 || K < 1) return qt_fail(h, QT_EINVAL, "gemm: empty operand");
+  if ((opA != QT_OP_N && opA != QT_OP_C) || (opB != QT_OP_N && opB != QT_OP_C))
+    return qt_fail(h, QT_EINVAL, "gemm: op must be N or C");
+  if (dtype != QT_C64 && dtype != QT_C128) return qt_fail(h, QT_EINVAL, "gemm: bad dtype");
+  const int64_t ar = opA == QT_OP_N ? M : K, ac = opA == QT_OP_N ? K : M;
+  const int64_t br = opB == QT_OP_N ? K : N, bc = opB == QT_OP_N ? N : K;
+  if (lda < ar || ldb < br || ldc < M) return qt_fail(h, QT_EINVAL, "gemm: leading dimension too small");
+  cudaSetDevice(h->device);
+  const size_t es = dtype == QT_C64 ? sizeof(float2) : sizeof(double2);
+  qt_scratch s(h);
+  unsigned char *dA, *dB, *dC;
+  QT_TRY(s.get(&dA, es * lda * ac));
+  QT_TRY(s.get(&dB, es * ldb * bc));
+  QT_TRY(s.get(&dC, es * ldc * N));
+  QT_CHECK_CUDA(h, cudaMemcpyAsync(dA, A, es * lda * ac, cudaMemcpyHostToDevice, h->stream));
+  QT_CHECK_CUDA(h, cudaMemcpyAsync(dB, B, es * ldb * bc, cudaMemcpyHostToDevice, h->stream));
+  QT_CHECK_CUDA(h, cudaMemcpyAsync(dC, C, es * ldc * N, cudaMemcpyHostToDevice, h->stream));
+  if (dtype == QT_C64) {
+    QT_TRY(qt_cgemm_c64(h, opA, opB, M, N, K, make_float2((float)alpha[0], (float)alpha[1]), (const float2*)dA, lda,
+                        (const float2*)dB, ldb, make_float2((float)beta[0], (float)beta[1]), (float2*)dC, ldc));
+  } else {
+    QT_TRY(qt_cgemm<double2>(h, opA, opB, M, N, K, make_double2(alpha[0], alpha[1]), (const double2*)dA, lda,
+                             (const double2*)dB, ldb, make_double2(beta[0], beta[1]), (double2*)dC, ldc));
+  }
+  QT_TRY(qt_check_status(h));
+  QT_CHECK_CUDA(h, cudaMemcpyAsync(C, dC, es * ldc * N, cudaMemcpyDeviceToHost, h->stream));
+  QT_CHECK_CUDA(h, cudaStreamSynchronize(h->stream));
+  return QT_OK;
+}
+
 extern "C" int qt_contract_pair(qt_handle* h, int dtype, int ndA, const int64_t* dimsA, const void* A, int ndB,
                                 const int64_t* dimsB, const void* B, int ncontract, const int* axesA, const int* axesB,
                                 void* C) {
@@ -919,17 +1158,37 @@ extern "C" int qt_contract_pair(qt_handle* h, int dtype, int ndA, const int64_t*
 namespace {
 
 // Exact truncated SVD of a host matrix in FP64 (any dtype), results in FP64.
-int host_truncated_svd64(qt_handle* h, const double2* M, int64_t m, int64_t n, double cutoff, int chi_max, int mode,
-                         std::vector<double2>* U, std::vector<double>* S, std::vector<double2>* Vh, int* k,
-                         double* disc) {
+// Host-facing truncated SVD.  M64 (FP64 copy of the input) feeds the exact
+// paths; M32 (the complex64 input itself, chosen mode) feeds the FP32-storage
+// QR-preconditioned Jacobi, whose cutoff is floored at the FP32 noise level
+// 4 sqrt(max(m, n)) u_fp32 ||M||_F (the chosen-mode precision contract).
+int host_truncated_svd64(qt_handle* h, const double2* M64, const float2* M32, int64_t m, int64_t n, double cutoff,
+                         int chi_max, int mode, std::vector<double2>* U, std::vector<double>* S,
+                         std::vector<double2>* Vh, int* k, double* disc) {
   qt_scratch s(h);
-  double2* dM;
-  QT_TRY(s.get(&dM, (size_t)m * n));
-  QT_CHECK_CUDA(h, cudaMemcpyAsync(dM, M, sizeof(double2) * m * n, cudaMemcpyHostToDevice, h->stream));
   SvdOut o;
   double2 *A = nullptr, *B = nullptr;
-  int rc = (mode == QT_MODE_CUSOLVER) ? svd_split_cusolver<double2>(h, dM, m, n, cutoff, chi_max, &A, &B, &o)
-                                      : svd_split_jacobi<double2, double2>(h, dM, m, n, cutoff, chi_max, false, &A, &B, &o);
+  int rc;
+  if (M32) {
+    float2* dM;
+    QT_TRY(s.get(&dM, (size_t)m * n));
+    QT_CHECK_CUDA(h, cudaMemcpyAsync(dM, M32, sizeof(float2) * m * n, cudaMemcpyHostToDevice, h->stream));
+    double* dn;
+    QT_TRY(s.get(&dn, 1));
+    QT_TRY(qt_norm2<float2>(h, dM, m * n, dn));
+    double n2 = 0;
+    QT_CHECK_CUDA(h, cudaMemcpyAsync(&n2, dn, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    QT_CHECK_CUDA(h, cudaStreamSynchronize(h->stream));
+    rc = svd_split_direct32<double2>(h, dM, m, n, std::max(cutoff, fp32_floor_rel(h, m, n) * std::sqrt(n2)), chi_max,
+                                     &A, &B, &o);
+  } else {
+    double2* dM;
+    QT_TRY(s.get(&dM, (size_t)m * n));
+    QT_CHECK_CUDA(h, cudaMemcpyAsync(dM, M64, sizeof(double2) * m * n, cudaMemcpyHostToDevice, h->stream));
+    rc = (mode == QT_MODE_CUSOLVER) ? svd_split_cusolver<double2>(h, dM, m, n, cutoff, chi_max, &A, &B, &o)
+                                    : svd_split_jacobi<double2, double2>(h, dM, m, n, cutoff, chi_max, false, &A, &B, &o);
+  }
+  if (rc == QT_OK) rc = qt_check_status(h);
   if (rc == QT_OK) {
     U->resize((size_t)m * o.k);
     Vh->resize((size_t)o.k * n);
@@ -972,8 +1231,9 @@ extern "C" int qt_truncated_svd(qt_handle* h, int dtype, int64_t m, int64_t n, c
     M64[i] = (dtype == QT_C64) ? make_double2(((const float2*)M)[i].x, ((const float2*)M)[i].y) : ((const double2*)M)[i];
   int kk = 0;
   double disc = 0;
-  QT_TRY(host_truncated_svd64(h, M64.data(), m, n, cutoff, chi_max, mode == QT_MODE_CUSOLVER ? mode : QT_MODE_PLAIN,
-                              &u, &s, &vh, &kk, &disc));
+  const bool fp32 = dtype == QT_C64 && mode == QT_MODE_CHOSEN;
+  QT_TRY(host_truncated_svd64(h, M64.data(), fp32 ? (const float2*)M : nullptr, m, n, cutoff, chi_max,
+                              mode == QT_MODE_CUSOLVER ? mode : QT_MODE_PLAIN, &u, &s, &vh, &kk, &disc));
   for (int j = 0; j < kk; j++) S[j] = s[j];
   for (int64_t j = 0; j < kcap; j++)
     for (int64_t i = 0; i < m; i++) {
@@ -1027,8 +1287,8 @@ extern "C" int qt_contract_svd(qt_handle* h, int dtype, int nd1, const int64_t* 
   std::vector<double> s1, s2;
   int k1 = 0, k2 = 0;
   double dd = 0;
-  QT_TRY(host_truncated_svd64(h, a.data(), m1, D1, er, 0, QT_MODE_PLAIN, &u1, &s1, &v1, &k1, &dd));
-  QT_TRY(host_truncated_svd64(h, b.data(), D1, m2, er, 0, QT_MODE_PLAIN, &u2, &s2, &v2, &k2, &dd));
+  QT_TRY(host_truncated_svd64(h, a.data(), nullptr, m1, D1, er, 0, QT_MODE_PLAIN, &u1, &s1, &v1, &k1, &dd));
+  QT_TRY(host_truncated_svd64(h, b.data(), nullptr, D1, m2, er, 0, QT_MODE_PLAIN, &u2, &s2, &v2, &k2, &dd));
   // L = U1 diag(S1) V1h (m1 x D1) ; R = U2 diag(S2) V2h (D1 x m2) ; out = L R
   std::vector<double2> us1((size_t)m1 * k1), us2((size_t)D1 * k2), L((size_t)m1 * D1), R((size_t)D1 * m2);
   for (int j = 0; j < k1; j++)

@@ -31,8 +31,14 @@ struct qt_handle {
   int64_t launches = 0;           // kernel launches issued through this handle
   int* d_flags = nullptr;         // device status words (see QT_FLAG_*)
   int* h_flags = nullptr;         // pinned host mirror
+  int* d_status = nullptr;        // sticky device status of the tensor-core GEMM's bounded waits
   qt_rank_model* rank_model = nullptr;
   uint64_t sketch_counter = 0;    // advances the sketch RNG stream per update
+  // algorithmic work issued (cumulative): Jacobi rounds and the bytes of X and
+  // V they must move (every pair's columns read once per round, rotated pairs
+  // written back and their V rows read and written); tensor-core GEMM TF32
+  // flops (24 M N K per complex product) and launches
+  double work_jacobi_bytes = 0, work_jacobi_rounds = 0, work_tc_flops = 0, work_tc_launches = 0;
   bool prof = false;
   std::vector<qt_profile_rec> prof_recs;
   std::vector<cudaEvent_t> event_pool;
@@ -69,6 +75,9 @@ struct qt_mps {
 // ---------------------------------------------------------------------------
 
 int qt_fail(qt_handle* h, int code, const std::string& msg);
+// Reads and clears the sticky device status (after the work queued so far):
+// QT_ETIMEOUT when a tensor-core GEMM's pipeline wait gave up.
+int qt_check_status(qt_handle* h);
 
 #define QT_CHECK_CUDA(h, call)                                                    \
   do {                                                                            \
@@ -204,7 +213,8 @@ int qt_norm2(qt_handle* h, const C* x, int64_t n, double* d_out);
 
 // k_jacobi.cu ----------------------------------------------------------------
 // One-sided block Jacobi SVD of X (mm x nn, mm >= nn) in place: X <- X V with
-// orthogonal columns, V (nn x nn) accumulated.  TS = storage type.
+// orthogonal columns, V (nn x nn) accumulated (V = nullptr: not accumulated).
+// TS = storage type.
 template <typename TS>
 int qt_jacobi_svd(qt_handle* h, TS* X, int64_t mm, int64_t nn, int64_t ldx, TS* V, int64_t ldv,
                   double tol, int max_sweeps, int* sweeps_out);

@@ -26,7 +26,7 @@ const MESSAGES = Dict(Cint(-1) => "Error must be positive",
 struct QtConfig
     device::Cint; mode::Cint; cutoff::Cdouble; chi_max::Cint; oversample::Cint; power_iters::Cint
     renormalize::Cint; use_rank_model::Cint; max_sweeps::Cint; jacobi_tol::Cdouble; noise_floor::Cdouble
-    seed::UInt64; tc_gemm::Cint
+    seed::UInt64; tc_gemm::Cint; jacobi_kernel::Cint
 end
 
 struct QtUpdateStats
@@ -50,7 +50,8 @@ function Engine(; mode::Symbol=:plain, cutoff=0.0, chi_max=0, device=0, tc_gemm=
     ccall((:qt_config_default, lib), Cint, (Ref{QtConfig},), cfg)
     c = cfg[]
     cfg[] = QtConfig(device, MODES[mode], cutoff, chi_max, c.oversample, c.power_iters, c.renormalize,
-                     c.use_rank_model, c.max_sweeps, c.jacobi_tol, c.noise_floor, c.seed, Cint(tc_gemm))
+                     c.use_rank_model, c.max_sweeps, c.jacobi_tol, c.noise_floor, c.seed, Cint(tc_gemm),
+                     c.jacobi_kernel)
     h = Ref{Ptr{Cvoid}}(C_NULL)
     rc = ccall((:qt_create, lib), Cint, (Ref{Ptr{Cvoid}}, Ref{QtConfig}), h, cfg)
     rc == QT_OK || error("qt_create failed ($rc)")

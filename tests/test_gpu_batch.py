@@ -40,7 +40,8 @@ def test_batch_matches_oracle(engine, use_graph):
     assert ranks.min() >= 1 and sweeps.max() > 0
     for ci, (n, depth, chi, gates) in enumerate(circuits):
         sites, stats = O.run_brickwork(n, gates, cutoff, chi)
-        assert abs(z[ci] - O.expect_z(sites, 1)) <= 1e-5, (ci, z[ci], O.expect_z(sites, 1))
+        # complex64 storage: |<Z>| error <= 2 ||psi - ref|| (the state bound below)
+        assert abs(z[ci] - O.expect_z(sites, 1)) <= 5e-5, (ci, z[ci], O.expect_z(sites, 1))
         dims = b.bond_dims(ci)
         assert list(dims) == [1] + [s.shape[2] for s in sites], (ci, dims)
         psi = O.mps_to_state([b.site(ci, i).astype(np.complex128) for i in range(1, n + 1)])

@@ -19,7 +19,7 @@ def exact_theta(a, b, g):
     return O.apply_gate_to_theta(O.theta_of(a, b), g, chil, chir)
 
 
-@pytest.mark.parametrize("chi", [64, 128])
+@pytest.mark.parametrize("chi", [128, 256])
 def test_randomized_path_matches_exact_truncation(engine, chi):
     # decaying spectrum; cutoff far above the FP32-level noise floor: the
     # sketched split keeps the exact rank and its truncation error is within

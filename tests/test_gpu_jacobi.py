@@ -1,0 +1,120 @@
+"""One-sided block Jacobi SVD: the one-launch cluster round (pair rows held in
+the shared memory of 1, 2, 4 or 8 CTAs) and the three-kernel round, in FP64
+and FP32 storage, against LAPACK on graded spectra."""
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def crandn(rng, *shape):
+    return (rng.standard_normal(shape) + 1j * rng.standard_normal(shape)) / np.sqrt(2)
+
+
+def graded(rng, m, n, decay):
+    k = min(m, n)
+    q1, _ = np.linalg.qr(crandn(rng, m, k))
+    q2, _ = np.linalg.qr(crandn(rng, n, k))
+    s = decay ** np.arange(k, dtype=np.float64)
+    return (q1 * s) @ q2.conj().T, s
+
+
+# shapes covering cluster sizes 1..8 of the FP64 round (rows per CTA <= ~390)
+# and 1..4 of the FP32 round, column counts not a multiple of the 8-column
+# block, tall and wide
+SHAPES = [(40, 24), (24, 40), (300, 201), (701, 513), (1100, 1003), (1536, 1536)]
+
+
+@pytest.mark.parametrize("kernel", [0, 1])
+@pytest.mark.parametrize("shape", SHAPES)
+def test_fp64_jacobi_matches_lapack(engine, shape, kernel):
+    rng = np.random.default_rng(sum(shape) + kernel)
+    m, n = shape
+    M, _ = graded(rng, m, n, 0.985)
+    eng = engine.Engine(mode="plain", jacobi_kernel=kernel)
+    U, S, Vh, k, _ = eng.truncated_svd(M, 0.0)
+    ref = np.linalg.svd(M, compute_uv=False)
+    assert k == min(m, n)
+    # M itself is known to ~u ||M|| (it is a rounded product), so the values
+    # agree with LAPACK's to a multiple of that, not relatively
+    assert np.abs(S - ref).max() <= 1e-12 * ref[0], np.abs(S - ref).max()
+    assert np.linalg.norm((U * S) @ Vh - M) <= 1e-12 * np.sqrt(max(m, n)) * np.linalg.norm(M)
+    assert np.abs(U.conj().T @ U - np.eye(k)).max() <= 1e-11
+    eng.close()
+
+
+@pytest.mark.parametrize("kernel", [0, 1])
+@pytest.mark.parametrize("shape", SHAPES)
+def test_fp32_jacobi_matches_lapack(engine, shape, kernel):
+    rng = np.random.default_rng(7 * sum(shape) + kernel)
+    m, n = shape
+    M, _ = graded(rng, m, n, 0.97)
+    M32 = M.astype(np.complex64)
+    ref = np.linalg.svd(M32.astype(np.complex128), compute_uv=False)
+    nrm = np.linalg.norm(ref)
+    floor = 4 * np.sqrt(max(m, n)) * 5.96e-8 * nrm  # the chosen-mode noise floor
+    tail = np.sqrt(np.cumsum(ref[::-1] ** 2))[::-1]
+
+    def rank_at(cut):
+        return int(np.argmax(np.append(tail[1:], 0.0) <= cut)) + 1
+
+    eng = engine.Engine(mode="chosen", jacobi_kernel=kernel)
+    # a cutoff well above the floor: the exact rank (+-1 at a tie)
+    cut = 50 * floor
+    U, S, Vh, k, _ = eng.truncated_svd(M32, cut, mode="chosen")
+    assert abs(k - rank_at(cut)) <= 1, (k, rank_at(cut))
+    err = np.linalg.norm((U * S) @ Vh - M32)
+    assert err <= 1.1 * np.sqrt(np.sum(ref[k:] ** 2)) + floor, (err, floor)
+    # cutoff 0: truncation at the floor, where the tail is FP32 rounding noise
+    # of the products and the rank is known to a few percent only
+    U, S, Vh, k, _ = eng.truncated_svd(M32, 0.0, mode="chosen")
+    k_ref = rank_at(floor)
+    assert k_ref - 1 <= k <= k_ref + max(2, int(0.03 * k_ref)), (k, k_ref)
+    kk = min(k, k_ref)
+    # FP32 storage: values to ~sqrt(rows) u_fp32 of ||M|| absolutely
+    assert np.abs(S[:kk] - ref[:kk]).max() <= 2 * floor, (np.abs(S[:kk] - ref[:kk]).max(), floor)
+    err = np.linalg.norm((U * S) @ Vh - M32)
+    assert err <= np.sqrt(np.sum(ref[k:] ** 2)) + 4 * floor, (err, floor)
+    # one Newton-Schulz step leaves the left factor orthonormal to FP32 rounding
+    assert np.abs(U.conj().T @ U - np.eye(k)).max() <= 2e-6 * np.sqrt(m)
+    eng.close()
+
+
+def test_one_launch_round_equals_three_kernel_round_fp64(engine):
+    """The two round implementations reach the same factorisation to FP64
+    accuracy on one matrix (different summation orders, same fixed point)."""
+    rng = np.random.default_rng(11)
+    M, _ = graded(rng, 512, 384, 0.98)
+    out = []
+    for kernel in (0, 1):
+        eng = engine.Engine(mode="plain", jacobi_kernel=kernel)
+        out.append(eng.truncated_svd(M, 1e-9))
+        eng.close()
+    (U0, S0, V0, k0, d0), (U1, S1, V1, k1, d1) = out
+    assert k0 == k1
+    assert np.abs(S0 - S1).max() <= 1e-13 * S0[0] * 384
+    assert np.linalg.norm((U0 * S0) @ V0 - (U1 * S1) @ V1) <= 1e-11 * np.linalg.norm(M)
+
+
+@pytest.mark.parametrize("chi", [256, 1024])
+def test_fp32_split_of_rank_deficient_theta(engine, chi):
+    """theta' = G (A.B) with a 0.97^k spectrum: half of its values at chi = 1024
+    lie below FP32 resolution.  The FP32 split must still reproduce the exact
+    truncation to chi (error within 1.1x, unit left factor to FP32 level)."""
+    import oracle as O
+    rng = np.random.default_rng(chi)
+    a, b, _ = O.decay_theta_factors(chi, rng, 0.97)
+    g = O.haar_unitary(rng)
+    th = O.apply_gate_to_theta(O.theta_of(a.astype(np.complex64).astype(complex), b.astype(np.complex64).astype(complex)),
+                               g, chi, chi).astype(np.complex64)
+    ref = np.linalg.svd(th.astype(complex), compute_uv=False)
+    exact = np.sqrt(np.sum(ref[chi:] ** 2))
+    eng = engine.Engine(mode="chosen", tc_gemm=1)
+    U, S, Vh, k, _ = eng.truncated_svd(th, 1e-6, chi_max=chi, mode="chosen")
+    assert k == chi
+    err = np.linalg.norm((U * S) @ Vh - th.astype(complex))
+    assert err <= 1.1 * exact, (err, exact)
+    assert np.abs(U.conj().T @ U - np.eye(k)).max() <= 1e-4
+    assert np.abs(S[:k] - ref[:k]).max() <= 1e-4 * ref[0]
+    eng.close()

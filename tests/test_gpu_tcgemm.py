@@ -51,3 +51,38 @@ def test_tc_chosen_update_matches_exact_truncation(engine):
     assert err <= 1.1 * np.sqrt(ex.discarded_weight)
     m.free()
     eng.close()
+
+
+@pytest.mark.parametrize("ops", [("N", "N"), ("C", "N"), ("N", "C"), ("C", "C")])
+@pytest.mark.parametrize("mnk", [(64, 32, 32), (2048, 32, 2048), (300, 257, 129), (1024, 1040, 2048),
+                                 (2048, 2048, 64), (2048, 2048, 2048)])
+def test_tc_gemm_ops_and_beta(tc, ops, mnk):
+    """Every operand orientation the SVD path uses, with beta = 1 accumulation
+    (the Gram-Schmidt projection update), up to 2048 in each dimension."""
+    M, N, K = mnk
+    rng = np.random.default_rng(M * 7 + N * 3 + K)
+    A = rand_c64(rng, *((M, K) if ops[0] == "N" else (K, M)))
+    B = rand_c64(rng, *((K, N) if ops[1] == "N" else (N, K)))
+    C0 = rand_c64(rng, M, N)
+    got = tc.gemm(A, B, ops[0], ops[1], alpha=-1.0, beta=1.0, out=C0)
+    opa = A.astype(np.complex128) if ops[0] == "N" else A.astype(np.complex128).conj().T
+    opb = B.astype(np.complex128) if ops[1] == "N" else B.astype(np.complex128).conj().T
+    ref = C0.astype(np.complex128) - opa @ opb
+    # split-TF32x3 with FP32 accumulation: a few 2^-21 relative per product,
+    # growing like sqrt(K) over the sum (measured ~4e-6 sqrt(K) at unit entries)
+    err = np.abs(got - ref).max() / np.sqrt(K)
+    assert err <= 2e-5, err
+
+
+@pytest.mark.parametrize("ops", [("N", "N"), ("C", "N"), ("N", "C")])
+def test_fp64_gemm_ops(engine, ops):
+    eng = engine.Engine(mode="plain")
+    rng = np.random.default_rng(3)
+    M, N, K = 130, 70, 90
+    A = rng.standard_normal((M, K) if ops[0] == "N" else (K, M)) + 1j * rng.standard_normal((M, K) if ops[0] == "N" else (K, M))
+    B = rng.standard_normal((K, N) if ops[1] == "N" else (N, K)) + 1j * rng.standard_normal((K, N) if ops[1] == "N" else (N, K))
+    got = eng.gemm(A, B, ops[0], ops[1])
+    opa = A if ops[0] == "N" else A.conj().T
+    opb = B if ops[1] == "N" else B.conj().T
+    assert np.abs(got - opa @ opb).max() <= 1e-13 * np.sqrt(K) * 4
+    eng.close()
