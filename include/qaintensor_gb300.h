@@ -156,6 +156,23 @@ int qt_truncated_svd(qt_handle* h, int dtype, int64_t m, int64_t n, const void* 
                      double cutoff, int chi_max, int mode,
                      void* U, double* S, void* Vh, int* k, double* discarded);
 
+/* Truncated SVD of a device matrix for callers that cannot allocate device
+ * memory (no counterpart in the reference).  Embedding frameworks that own
+ * every device byte through their own arena or budget, and code that must
+ * not trigger a cudaMalloc, pass only their input and output buffers; the
+ * scratch lives in a fixed file-scope device array (about 2.6 MB, resident
+ * on every device that loads the library until exit), so this call makes no
+ * cudaMalloc, cudaFree or allocating library call.
+ *   dM: m x n complex128, column-major (ld m), not modified;
+ *   dU: m x min(m,n), dS: min(m,n) doubles, dVh: min(m,n) x n (ld k on return),
+ *   *k: kept rank (tail rule of src/svd.jl:29-33 with `cutoff`, then chi_max).
+ * m, n <= 256, otherwise QT_ENOTSUP.  The first call on a device looks up the
+ * array's address (cudaGetSymbolAddress) -- make it before any stream
+ * capture.  All calls share the one array: calls that overlap on the GPU race
+ * and must be serialised by the caller.  Runs on `stream` and synchronises it. */
+int qt_truncated_svd_noalloc(int64_t m, int64_t n, const void* dM, double cutoff, int chi_max, void* dU, double* dS,
+                             void* dVh, int* k, void* stream);
+
 /* contract_svd(T1, T2, (i1, i2); er) of src/svd.jl:7-38 (i1, i2 are 1-based,
  * as in Julia).  out holds the free legs of T1 then of T2, column-major. */
 int qt_contract_svd(qt_handle* h, int dtype,

@@ -143,6 +143,7 @@ def library() -> C.CDLL:
         "qt_batch_bond_dims": (I, [P, P, I, P]),
         "qt_batch_download_site": (I, [P, P, I, I, P]),
         "qt_batch_expect_z": (I, [P, P, I, P]),
+        "qt_truncated_svd_noalloc": (I, [L, L, P, D, I, P, P, P, C.POINTER(I), P]),
         "qt_mps_apply_mpo": (I, [P, P, C.POINTER(P), C.POINTER(L)]),
         "qt_mps_compress": (I, [P, P, D, I, I, I, P, P]),
         "qt_mps_expect_mpo": (I, [P, P, C.POINTER(P), C.POINTER(L), C.POINTER(D)]),
@@ -644,6 +645,23 @@ class Batch:
                 self.free()
         except Exception:
             pass
+
+
+def truncated_svd_noalloc(m: int, n: int, dM: int, cutoff: float, chi_max: int, dU: int, dS: int, dVh: int,
+                          stream: int = 0) -> int:
+    """Truncated SVD of a complex128 device matrix for callers that cannot
+    allocate device memory: every pointer (integers, device addresses) is the
+    caller's; the scratch is the library's fixed device array.  Returns k.
+    m, n <= 256; calls must not overlap on the GPU."""
+    k = C.c_int()
+    rc = library().qt_truncated_svd_noalloc(int(m), int(n), C.c_void_p(dM), float(cutoff), int(chi_max),
+                                             C.c_void_p(dU), C.c_void_p(dS), C.c_void_p(dVh), C.byref(k),
+                                             C.c_void_p(stream))
+    if rc != QT_OK:
+        if rc in REFERENCE_MESSAGES:
+            raise QaintensorError(REFERENCE_MESSAGES[rc], rc)
+        raise EngineError(f"qt_truncated_svd_noalloc failed with status {rc}", rc)
+    return k.value
 
 
 # ---------------------------------------------------------------------------
