@@ -104,7 +104,8 @@ int64_t qt_launch_count(const qt_handle* h);
  * must move (every pair's columns read once per round; rotated pairs written
  * back, their V rows read and written), out[1] Jacobi rounds, out[2] TF32
  * flops of the tensor-core GEMMs (24 M N K per complex product), out[3] their
- * launches. */
+ * launches, out[4] Jacobi pair rotations, out[5] inner sweeps of the 16x16
+ * pair solvers (out holds 6 doubles). */
 int qt_work_counters(const qt_handle* h, double* out);
 
 /* ---- measurement helpers ------------------------------------------------ */

@@ -243,9 +243,10 @@ class Engine:
 
     def work_counters(self) -> dict:
         """Cumulative algorithmic work: Jacobi bytes/rounds, tensor-core TF32 flops/launches."""
-        out = (C.c_double * 4)()
+        out = (C.c_double * 6)()
         self._check(self._lib.qt_work_counters(self._h, out))
-        return {"jacobi_bytes": out[0], "jacobi_rounds": out[1], "tc_flops": out[2], "tc_launches": out[3]}
+        return {"jacobi_bytes": out[0], "jacobi_rounds": out[1], "tc_flops": out[2], "tc_launches": out[3],
+                "jacobi_pairs": out[4], "jacobi_inner_sweeps": out[5]}
 
     def sync(self):
         self._check(self._lib.qt_sync(self._h))
@@ -504,6 +505,43 @@ class DeviceMPS:
     def switch(self, i: int):
         """``switch!(mps, i)`` (src/switch.jl): swap the physical legs of sites i, i+1."""
         self.eng._check(self.eng._lib.qt_switch(self.eng._h, self._p, i - 1))
+
+    def switch_wires(self, i: int, j: int):
+        """``switch!(mps, i, j)`` (src/switch.jl, file lines 101-124): wire
+        numbers count from the far end (i -> L - i + 1) and the swap runs as a
+        ladder of adjacent swaps up, then down."""
+        if not (i > 0 and j > 0):
+            raise QaintensorError("Wire indices `i` and `j` must be positive")
+        L = self.nsites
+        if not (i <= L and j <= L):
+            raise QaintensorError("Indices to swap `i` and `j` must be less than or equal to the number of open "
+                                  "wires in MPS")
+        if i == j:
+            return
+        i, j = L - i + 1, L - j + 1
+        lo, hi = min(i, j), max(i, j)
+        for s in range(lo, hi):
+            self.switch(s)
+        for s in range(hi - 2, lo - 1, -1):
+            self.switch(s)
+
+    def permute(self, order):
+        """``Base.permute!(mps, order)`` (src/switch.jl, file lines 132-144)."""
+        order = list(order)
+        n = self.nsites
+        if len(order) != n:
+            raise QaintensorError("Given permutation must be same length as number of Tensors in MPS")
+        if len(set(order)) != len(order):
+            raise QaintensorError("Permutation order cannot contain repeat values")
+        if not all(x > 0 for x in order):
+            raise QaintensorError("Permutation order can only contain positive values")
+        if max(order) != len(order):
+            raise QaintensorError("Wire numbers in permutation order cannot exceed number of wires in MPS")
+        seq = list(range(1, n + 1))
+        for i in range(1, n + 1):
+            loc = seq.index(order[i - 1]) + 1
+            self.switch_wires(i, loc)
+            seq[loc - 1], seq[i - 1] = seq[i - 1], seq[loc - 1]
 
     def expect_z(self, i: int) -> float:
         out = C.c_double()

@@ -26,6 +26,8 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 
@@ -157,10 +159,11 @@ struct pair_eig_shared {
 // smaller root.  Columns with |x|^2 <= nu2 are at the rounding level of X and
 // are neither rotated nor tested.
 template <typename RW>
-__device__ void diagonalise_pair(pair_eig_shared<RW>& sh, const int* col, double tol_inner, double nu2) {
+__device__ int diagonalise_pair(pair_eig_shared<RW>& sh, const int* col, double tol_inner, double nu2) {
   typedef typename cplx_of<RW>::type CW;
   const int t = threadIdx.x;
-  for (int sweep = 0; sweep < MAX_INNER; sweep++) {
+  int sweep = 0;
+  for (; sweep < MAX_INNER; sweep++) {
     __syncthreads();  // every thread has read inner_rot of the previous sweep
     if (t == 0) sh.inner_rot = 0;
     __syncthreads();
@@ -238,6 +241,7 @@ __device__ void diagonalise_pair(pair_eig_shared<RW>& sh, const int* col, double
     if (!again) break;
   }
   __syncthreads();
+  return sweep + (sweep < MAX_INNER ? 1 : 0);
 }
 
 // FP32 variant for FP32 storage: the two-sided Jacobi runs on the scaled
@@ -245,24 +249,29 @@ __device__ void diagonalise_pair(pair_eig_shared<RW>& sh, const int* col, double
 // cosines between columns) with the diagonal D tracked separately.  The
 // cosines are O(1) numbers, so FP32 keeps each one accurate to ~u of its
 // own pair whatever the spread of the column norms -- the property the
-// unscaled FP32 Gram loses -- and the rotations are correct to FP32 level
-// right down to the FP32 tolerance.  A rotation J of pair (p, q) acts on
-// Ghat through Jt = D^{1/2} J D'^{-1/2}: Jt_pp = c sqrt(a/a'),
+// unscaled FP32 Gram loses.  A rotation J of pair (p, q) acts on Ghat
+// through Jt = D^{1/2} J D'^{-1/2}: Jt_pp = c sqrt(a/a'),
 // Jt_qp = -s e^{-i phi} sqrt(b/a'), Jt_pq = s e^{i phi} sqrt(a/b'),
 // Jt_qq = c sqrt(b/b'), with a' = a - t|gamma|, b' = b + t|gamma|.
+// The unitary is accumulated in the same scaled form, Wt = D0^{1/2} W D^{-1/2}
+// (D0 the initial diagonal): its entries are O(1), so their FP32 rounding is
+// relative to each output column's own norm once W = D0^{-1/2} Wt D^{1/2} is
+// formed -- small columns are not contaminated by the rounding of large ones.
 struct pair_eig_scaled {
   float d[JC];            // current diagonal of G
+  float d0[JC];           // initial diagonal
   float2 G[JC][JC + 1];   // scaled Gram (diagonal implicit 1)
-  float2 W[JC][JC + 1];   // accumulated unitary
+  float2 W[JC][JC + 1];   // scaled unitary Wt, then W
   int rp[JC / 2], rq[JC / 2], ron[JC / 2];
-  float rc[JC / 2], na[JC / 2], nb[JC / 2], kpp[JC / 2], kqq[JC / 2];
-  float2 rse[JC / 2], kqp[JC / 2], kpq[JC / 2];
+  float na[JC / 2], nb[JC / 2], kpp[JC / 2], kqq[JC / 2];
+  float2 kqp[JC / 2], kpq[JC / 2];
   int inner_rot;
 };
 
-__device__ void diagonalise_scaled(pair_eig_scaled& sh, const int* col, float tol_inner, float nu2) {
+__device__ int diagonalise_scaled(pair_eig_scaled& sh, const int* col, float tol_inner, float nu2, int max_inner) {
   const int t = threadIdx.x;
-  for (int sweep = 0; sweep < MAX_INNER; sweep++) {
+  int sweep = 0;
+  for (; sweep < max_inner; sweep++) {
     __syncthreads();  // every thread has read inner_rot of the previous sweep
     if (t == 0) sh.inner_rot = 0;
     __syncthreads();
@@ -275,17 +284,22 @@ __device__ void diagonalise_scaled(pair_eig_scaled& sh, const int* col, float to
         const float2 gs = sh.G[p][q];
         const float ags = sqrtf(gs.x * gs.x + gs.y * gs.y);
         if (col[p] >= 0 && col[q] >= 0 && a > nu2 && b > nu2 && ags > tol_inner) {
-          const float ag = ags * sqrtf(a) * sqrtf(b);  // |gamma|
-          const float zeta = (b - a) / (2.f * ag);
-          const float tt = copysignf(1.f, zeta) / (fabsf(zeta) + sqrtf(1.f + zeta * zeta));
-          const float c = 1.f / sqrtf(1.f + tt * tt), sn = c * tt;
-          const float2 e = make_float2(gs.x / ags, gs.y / ags);
-          const float a2 = fmaxf(a - tt * ag, 0.f), b2 = b + tt * ag;
-          const bool live = a2 > nu2;  // a column driven to the noise level is frozen
-          const float ra = live ? sqrtf(a / a2) : 0.f, rb = live ? sqrtf(b / a2) : 0.f;
-          const float sa = sqrtf(a / b2), sb = sqrtf(b / b2);
-          sh.ron[t] = 1; sh.rc[t] = c; sh.na[t] = a2; sh.nb[t] = b2;
-          sh.rse[t] = make_float2(sn * e.x, sn * e.y);
+          // rotation parameters with the fast reciprocal and reciprocal
+          // square root (a few ulp: the rotation only has to be unitary to
+          // FP32 level, and c, s below are consistent with each other)
+          const float ag = ags * sqrtf(a * b);  // |gamma|
+          const float zeta = __fdividef(b - a, 2.f * ag);
+          const float r1 = sqrtf(fmaf(zeta, zeta, 1.f));
+          const float tt = copysignf(__frcp_rn(fabsf(zeta) + r1), zeta);
+          const float c = rsqrtf(fmaf(tt, tt, 1.f)), sn = c * tt;
+          const float inv = __frcp_rn(ags);
+          const float2 e = make_float2(gs.x * inv, gs.y * inv);
+          // a column driven to the noise level is frozen at d = nu2
+          const float a2 = fmaxf(a - tt * ag, nu2), b2 = b + tt * ag;
+          const float ia2 = rsqrtf(a2), ib2 = rsqrtf(b2), sqa = sqrtf(a), sqb = sqrtf(b);
+          const float ra = sqa * ia2, rb = sqb * ia2;
+          const float sa = sqa * ib2, sb = sqb * ib2;
+          sh.ron[t] = 1; sh.na[t] = a2; sh.nb[t] = b2;
           sh.kpp[t] = c * ra;
           sh.kqp[t] = make_float2(-sn * e.x * rb, sn * e.y * rb);  // -s conj(e) sqrt(b/a')
           sh.kpq[t] = make_float2(sn * e.x * sa, sn * e.y * sa);   //  s e sqrt(a/b')
@@ -294,28 +308,22 @@ __device__ void diagonalise_scaled(pair_eig_scaled& sh, const int* col, float to
         }
       }
       __syncthreads();
-      // columns p, q: Ghat (rows r outside the pair) and W (all rows)
+      // columns p, q of Ghat (rows outside the pair) and of Wt (all rows): Jt from the right
       {
         const int task = t & 127, k = task >> 4, r = task & 15;
         if (sh.ron[k]) {
           const int p = sh.rp[k], q = sh.rq[k];
-          if (t < 128) {
-            if (r != p && r != q) {
-              const float2 xp = sh.G[r][p], xq = sh.G[r][q];
-              sh.G[r][p] = cadd(cscale(xp, sh.kpp[k]), cmul(sh.kqp[k], xq));
-              sh.G[r][q] = cadd(cmul(sh.kpq[k], xp), cscale(xq, sh.kqq[k]));
-            }
-          } else {
-            const float c = sh.rc[k];
-            const float2 se = sh.rse[k];
-            const float2 xp = sh.W[r][p], xq = sh.W[r][q];
-            sh.W[r][p] = csub(cscale(xp, c), cmul(cconj(se), xq));
-            sh.W[r][q] = cadd(cmul(se, xp), cscale(xq, c));
+          float2 (*M)[JC + 1] = (t < 128) ? sh.G : sh.W;
+          if (t >= 128 || (r != p && r != q)) {
+            const float2 xp = M[r][p], xq = M[r][q];
+            M[r][p] = cadd(cscale(xp, sh.kpp[k]), cmul(sh.kqp[k], xq));
+            M[r][q] = cadd(cmul(sh.kpq[k], xp), cscale(xq, sh.kqq[k]));
           }
         }
       }
       __syncthreads();
-      // rows p, q of Ghat (columns outside the pair): Jt^H from the left
+      // rows p, q of Ghat (columns outside the pair): Jt^H from the left; the
+      // 2x2 block of each pair and the new diagonal (disjoint entries)
       if (t < 128) {
         const int k = t >> 4, r = t & 15;
         if (sh.ron[k]) {
@@ -324,16 +332,13 @@ __device__ void diagonalise_scaled(pair_eig_scaled& sh, const int* col, float to
             const float2 gp = sh.G[p][r], gq = sh.G[q][r];
             sh.G[p][r] = cadd(cscale(gp, sh.kpp[k]), cmul(cconj(sh.kqp[k]), gq));
             sh.G[q][r] = cadd(cmul(cconj(sh.kpq[k]), gp), cscale(gq, sh.kqq[k]));
+          } else if (r == p) {
+            sh.G[p][q] = make_float2(0.f, 0.f);
+            sh.G[q][p] = make_float2(0.f, 0.f);
+            sh.d[p] = sh.na[k];
+            sh.d[q] = sh.nb[k];
           }
         }
-      }
-      __syncthreads();
-      if (t < JC / 2 && sh.ron[t]) {
-        const int p = sh.rp[t], q = sh.rq[t];
-        sh.G[p][q] = make_float2(0.f, 0.f);
-        sh.G[q][p] = make_float2(0.f, 0.f);
-        sh.d[p] = sh.na[t];
-        sh.d[q] = sh.nb[t];
       }
       __syncthreads();
     }
@@ -341,23 +346,15 @@ __device__ void diagonalise_scaled(pair_eig_scaled& sh, const int* col, float to
     if (!again) break;
   }
   __syncthreads();
-  // W is a product of FP32 rotations, unitary to a few u per rotation; one
-  // Newton-Schulz step W <- W (1.5 I - 0.5 W^H W) brings it back to ~u so
-  // that column norms do not drift over the sweeps (Ghat is free now)
+  // W = D0^{-1/2} Wt D^{1/2}
   {
     const int i = t >> 4, j = t & 15;
-    float2 p = make_float2(0.f, 0.f);
-#pragma unroll
-    for (int r = 0; r < JC; r++) cfma_conj(p, sh.W[r][i], sh.W[r][j]);
-    sh.G[i][j] = make_float2((i == j ? 1.5f : 0.f) - 0.5f * p.x, -0.5f * p.y);
-    __syncthreads();
-    float2 w = make_float2(0.f, 0.f);
-#pragma unroll
-    for (int k = 0; k < JC; k++) cfma(w, sh.W[i][k], sh.G[k][j]);
-    __syncthreads();
-    sh.W[i][j] = w;
-    __syncthreads();
+    const float d0 = sh.d0[i];
+    const float f = d0 > 0.f ? sqrtf(sh.d[j] / d0) : (i == j ? 1.f : 0.f);
+    sh.W[i][j] = d0 > 0.f ? cscale(sh.W[i][j], f) : make_float2(f, 0.f);
   }
+  __syncthreads();
+  return sweep + (sweep < max_inner ? 1 : 0);
 }
 
 // One CTA per block pair: sum the partial Grams, test the pair, and when it
@@ -369,13 +366,13 @@ eig_kernel(int nn, int nb, int round, int nparts, const double2* __restrict__ pa
            int* __restrict__ flags) {
   __shared__ pair_eig_shared<double> sh;
   __shared__ int col[JC];
-  __shared__ int any_rot, bad;
+  __shared__ int any_rot, bad, offmax_blk;
 
   const int t = threadIdx.x;
   const int pair = blockIdx.x;
   const double nu2 = nu_rel2 * (*xnorm2);
   pair_columns(round, pair, nb, nn, col);
-  if (t == 0) { any_rot = 0; bad = 0; }
+  if (t == 0) { any_rot = 0; bad = 0; offmax_blk = 0; }
   __syncthreads();
   // sum the partial Grams of this pair in a fixed order
   for (int e = t; e < NGRAM; e += NT) {
@@ -394,7 +391,8 @@ eig_kernel(int nn, int nb, int round, int nparts, const double2* __restrict__ pa
     return;
   }
   // is this pair already orthogonal to tol?  (the largest relative
-  // off-diagonal above tol is recorded as float bits)
+  // off-diagonal above tol is recorded as float bits, one atomic per pair)
+  float relmax = 0.f;
   for (int e = t; e < NGRAM; e += NT) {
     const int i = e / JC, j = e % JC;
     if (i < j && col[i] >= 0 && col[j] >= 0) {
@@ -402,11 +400,14 @@ eig_kernel(int nn, int nb, int round, int nparts, const double2* __restrict__ pa
       const double g = sqrt(cabs2(sh.G[i][j]));
       if (a > nu2 && b > nu2 && g > tol * sqrt(a * b)) {
         any_rot = 1;
-        const float rel = (a > 0 && b > 0) ? (float)fmin(g / sqrt(a * b), 1.0) : 1.0f;
-        atomicMax(&flags[QT_FLAG_OFFMAX], __float_as_int(rel));
+        relmax = fmaxf(relmax, (a > 0 && b > 0) ? (float)fmin(g / sqrt(a * b), 1.0) : 1.0f);
       }
     }
   }
+  for (int o = 16; o > 0; o >>= 1) relmax = fmaxf(relmax, __shfl_xor_sync(0xffffffffu, relmax, o));
+  if ((t & 31) == 0 && relmax > 0.f) atomicMax(&offmax_blk, __float_as_int(relmax));
+  __syncthreads();
+  if (t == 0 && offmax_blk > 0) atomicMax(&flags[QT_FLAG_OFFMAX], offmax_blk);
   __syncthreads();
   if (t == 0) rot[pair] = any_rot;
   if (!any_rot) return;
@@ -414,7 +415,8 @@ eig_kernel(int nn, int nb, int round, int nparts, const double2* __restrict__ pa
   // diagonalised well below the outer threshold so that the rounding of the
   // applied rotation (in the storage precision) cannot leave the pair just
   // above `tol`
-  diagonalise_pair<double>(sh, col, fmin(tol, 1e-14), nu2);
+  const int inner = diagonalise_pair<double>(sh, col, fmin(tol, 1e-14), nu2);
+  if (t == 0) atomicAdd(&flags[QT_FLAG_INNER], inner);
   for (int e = t; e < NGRAM; e += NT) wout[(size_t)pair * NGRAM + e] = sh.W[e / JC][e % JC];
 }
 
@@ -484,7 +486,7 @@ template <typename TS>
 __global__ void __launch_bounds__(NT)
 pair_round_kernel(TS* __restrict__ X, int64_t ldx, int mm, TS* __restrict__ V, int64_t ldv, int nn, int nb, int round,
                   int csize, int xrows_c, int vrows_c, int lds, double tol, double tol_inner, double nu_rel2,
-                  const double* __restrict__ xnorm2, int* __restrict__ flags) {
+                  const double* __restrict__ xnorm2, int* __restrict__ flags, int max_inner) {
   typedef typename real_of<TS>::type RE;
   extern __shared__ __align__(16) unsigned char dyn_smem[];
   TS* Xs = reinterpret_cast<TS*>(dyn_smem);
@@ -492,13 +494,13 @@ pair_round_kernel(TS* __restrict__ X, int64_t ldx, int mm, TS* __restrict__ V, i
   __shared__ typename std::conditional<F32, pair_eig_scaled, pair_eig_shared<double>>::type sh;
   __shared__ TS gpart[NGRAM];
   __shared__ int col[JC];
-  __shared__ int any_rot, bad;
+  __shared__ int any_rot, bad, offmax_blk, offbig_blk;
   cg::cluster_group cluster = cg::this_cluster();
   const int crank = (int)cluster.block_rank();
   const int pair = blockIdx.x / csize;
   const int t = threadIdx.x;
   pair_columns(round, pair, nb, nn, col);
-  if (t == 0) { any_rot = 0; bad = 0; }
+  if (t == 0) { any_rot = 0; bad = 0; offmax_blk = 0; offbig_blk = 0; }
   __syncthreads();
   const int xb = crank * xrows_c;
   const int xr = max(0, min(mm, xb + xrows_c) - xb);
@@ -533,6 +535,7 @@ pair_round_kernel(TS* __restrict__ X, int64_t ldx, int mm, TS* __restrict__ V, i
         for (int q = 0; q < csize; q++) s += (double)cluster.map_shared_rank(gpart, q)[t * JC + t].x;
         dd[t] = s;
         sh.d[t] = (float)s;
+        sh.d0[t] = (float)s;
         if (!isfinite(s)) bad = 1;
       }
       __syncthreads();
@@ -564,33 +567,50 @@ pair_round_kernel(TS* __restrict__ X, int64_t ldx, int mm, TS* __restrict__ V, i
     // is this pair already orthogonal to tol?  (the largest relative
     // off-diagonal above tol is recorded as float bits)
     if (!bad) {
+      // the largest relative off-diagonal above tol: a block maximum first,
+      // then one global atomic per pair (thousands of same-address atomics
+      // per round would serialise in L2)
+      float relmax = 0.f, relbig = 0.f;
+      const double big2 = 1e-6 * (*xnorm2);
       for (int e = t; e < NGRAM; e += NT) {
         const int i = e / JC, j = e % JC;
         if (i < j && col[i] >= 0 && col[j] >= 0) {
-          double rel = 0;
+          double rel = 0, a, b;
           bool live;
           if constexpr (F32) {
-            live = sh.d[i] > nu2 && sh.d[j] > nu2;
+            a = sh.d[i]; b = sh.d[j];
             rel = sqrt((double)cabs2(sh.G[i][j]));
           } else {
-            const double a = sh.G[i][i].x, b = sh.G[j][j].x;
-            live = a > nu2 && b > nu2;
-            if (live) rel = sqrt(cabs2(sh.G[i][j])) / sqrt(a * b);
+            a = sh.G[i][i].x; b = sh.G[j][j].x;
+            if (a > nu2 && b > nu2) rel = sqrt(cabs2(sh.G[i][j])) / sqrt(a * b);
           }
+          live = a > nu2 && b > nu2;
           if (live && rel > tol) {
             any_rot = 1;
-            atomicMax(&flags[QT_FLAG_OFFMAX], __float_as_int((float)fmin(rel, 1.0)));
+            relmax = fmaxf(relmax, (float)fmin(rel, 1.0));
+            if (a > big2 && b > big2) relbig = fmaxf(relbig, (float)fmin(rel, 1.0));
           }
         }
       }
+      for (int o = 16; o > 0; o >>= 1) {
+        relmax = fmaxf(relmax, __shfl_xor_sync(0xffffffffu, relmax, o));
+        relbig = fmaxf(relbig, __shfl_xor_sync(0xffffffffu, relbig, o));
+      }
+      if ((t & 31) == 0 && relmax > 0.f) atomicMax(&offmax_blk, __float_as_int(relmax));
+      if ((t & 31) == 0 && relbig > 0.f) atomicMax(&offbig_blk, __float_as_int(relbig));
+      __syncthreads();
+      if (t == 0 && offmax_blk > 0) atomicMax(&flags[QT_FLAG_OFFMAX], offmax_blk);
+      if (t == 0 && offbig_blk > 0) atomicMax(&flags[QT_FLAG_OFFBIG], offbig_blk);
     } else if (t == 0) {
       atomicOr(&flags[QT_FLAG_NONFINITE], 1);
     }
     __syncthreads();
     if (any_rot) {
       if (t == 0) atomicAdd(&flags[QT_FLAG_ROTATED], 1);
-      if constexpr (F32) diagonalise_scaled(sh, col, (float)tol_inner, (float)nu2);
-      else diagonalise_pair<RE>(sh, col, tol_inner, nu2);
+      int inner;
+      if constexpr (F32) inner = diagonalise_scaled(sh, col, (float)tol_inner, (float)nu2, max_inner);
+      else inner = diagonalise_pair<RE>(sh, col, tol_inner, nu2);
+      if (t == 0) atomicAdd(&flags[QT_FLAG_INNER], inner);
     }
   }
   cluster.sync();  // CTA 0's decision and unitary are ready
@@ -675,6 +695,13 @@ static int fused_shape(int64_t mm, int pairs, size_t elem, int* rows_c, int* lds
   }
   if (csize == 0) return 0;
   while (csize < 8 && (int64_t)pairs * csize < 152 && (mm + 2 * csize - 1) / (2 * csize) >= 64) csize *= 2;
+  // QT_JACOBI_CLUSTER=c (1, 2, 4 or 8) overrides the cluster size when the slice still fits
+  if (const char* env = std::getenv("QT_JACOBI_CLUSTER")) {
+    const int c = std::atoi(env);
+    const int64_t rc = (mm + c - 1) / c;
+    if ((c == 1 || c == 2 || c == 4 || c == 8) && (size_t)(((rc + 15) / 16) * 16 + 1) * JC * elem <= 200 * 1024)
+      csize = c;
+  }
   const int64_t rc = (mm + csize - 1) / csize;
   *rows_c = (int)rc;
   *lds = (int)(((rc + 15) / 16) * 16 + 1);  // odd multiple-of-16-plus-one stride: conflict-free Gram reads
@@ -685,7 +712,7 @@ static int fused_shape(int64_t mm, int pairs, size_t elem, int* rows_c, int* lds
 template <typename TS>
 static int launch_pair_round(qt_handle* h, int csize, int pairs, size_t smem, TS* X, int64_t ldx, int mm, TS* V,
                              int64_t ldv, int nn, int nb, int round, int xrows_c, int vrows_c, int lds, double tol,
-                             double tol_inner, double nu_rel2, const double* xnorm2) {
+                             double tol_inner, double nu_rel2, const double* xnorm2, int max_inner) {
   cudaLaunchConfig_t lc = {};
   lc.gridDim = dim3((unsigned)(pairs * csize));
   lc.blockDim = dim3(NT);
@@ -700,7 +727,7 @@ static int launch_pair_round(qt_handle* h, int csize, int pairs, size_t smem, TS
   lc.numAttrs = 1;
   if (h->prof) qt_prof_before(h, "pair_round_kernel<TS>");
   const cudaError_t e = cudaLaunchKernelEx(&lc, pair_round_kernel<TS>, X, ldx, mm, V, ldv, nn, nb, round, csize,
-                                           xrows_c, vrows_c, lds, tol, tol_inner, nu_rel2, xnorm2, h->d_flags);
+                                           xrows_c, vrows_c, lds, tol, tol_inner, nu_rel2, xnorm2, h->d_flags, max_inner);
   if (h->prof) qt_prof_after(h);
   h->launches++;
   if (e != cudaSuccess) return qt_fail(h, QT_ECUDA, std::string("launch pair_round_kernel: ") + cudaGetErrorString(e));
@@ -709,7 +736,7 @@ static int launch_pair_round(qt_handle* h, int csize, int pairs, size_t smem, TS
 
 template <typename TS>
 int qt_jacobi_svd_ws(qt_handle* h, TS* X, int64_t mm, int64_t nn, int64_t ldx, TS* V, int64_t ldv, double tol,
-                     int max_sweeps, int* sweeps_out, double2* parts) {
+                     int max_sweeps, int* sweeps_out, double2* parts, double nu_rel_in) {
   typedef typename gram_of<TS>::type TG;
   if (mm < nn) return qt_fail(h, QT_EINVAL, "jacobi: needs rows >= columns");
   if (V) QT_TRY(qt_set_identity<TS>(h, V, nn, ldv));
@@ -733,10 +760,15 @@ int qt_jacobi_svd_ws(qt_handle* h, TS* X, int64_t mm, int64_t nn, int64_t ldx, T
   }
   const bool fp32 = sizeof(typename real_of<TS>::type) == 4;
   const double u = fp32 ? 5.96e-8 : 1.11e-16;
-  // FP32 storage: only columns at the storage resolution of the whole matrix
-  // are frozen -- a chi_max-bound truncation keeps values within a few
-  // sqrt(rows) u of the norm, and those columns must still be orthogonalised
-  const double nu_rel = fp32 ? 4.0 * u : 4.0 * std::sqrt((double)std::max<int64_t>(mm, 16)) * u;
+  // Frozen-column threshold nu (relative to ||X||_F).  FP64: 4 sqrt(rows) u.
+  // FP32 default: 4 u, so that the weight of the frozen columns stays below
+  // the chosen mode's noise floor and the tail rule can resolve values near
+  // it.  Columns between 4 u and sqrt(rows) u are rounding noise of FP32
+  // products that keep rotating with O(1) cosines for tens of sweeps; callers
+  // whose rank is decided far above them (a chi_max cap, a cutoff well above
+  // the floor) pass nu_rel = sqrt(rows) u and save those sweeps.
+  const double nu_rel = nu_rel_in > 0 ? nu_rel_in
+                        : (fp32 ? 4.0 * u : 4.0 * std::sqrt((double)std::max<int64_t>(mm, 16)) * u);
   const double nu_rel2 = nu_rel * nu_rel;
   // one-launch rounds when the pair's rows fit a cluster's shared memory
   int xrows_c = 0, lds = 0;
@@ -749,13 +781,20 @@ int qt_jacobi_svd_ws(qt_handle* h, TS* X, int64_t mm, int64_t nn, int64_t ldx, T
   if (csize)
     QT_CHECK_CUDA(h, cudaFuncSetAttribute(pair_round_kernel<TS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           (int)smem));
+  // QT_JACOBI_TRACE=1 in the environment prints one line per sweep to stderr
+  static const bool trace = std::getenv("QT_JACOBI_TRACE") != nullptr;
   int sweep = 0;
   for (; sweep < max_sweeps; sweep++) {
+    // the pair solver diagonalises fully in the first sweeps; once the
+    // pairs are close to orthogonal one inner sweep of rotations reduces
+    // them quadratically and the outer test decides convergence
+    static const int inner_cap = std::getenv("QT_JACOBI_INNER") ? std::atoi(std::getenv("QT_JACOBI_INNER")) : 1;
+    const int max_inner = sweep < 2 ? MAX_INNER : std::max(1, std::min(inner_cap, MAX_INNER));
     QT_CHECK_CUDA(h, cudaMemsetAsync(h->d_flags, 0, sizeof(int) * QT_FLAG_COUNT, h->stream));
     for (int r = 0; r < rounds; r++) {
       if (csize) {
         QT_TRY(launch_pair_round<TS>(h, csize, pairs, smem, X, ldx, (int)mm, V, ldv, (int)nn, nb, r, xrows_c, vrows_c,
-                                     lds, tol, tol_inner, nu_rel2, xnorm2));
+                                     lds, tol, tol_inner, nu_rel2, xnorm2, max_inner));
         continue;
       }
       QT_LAUNCH(h, (gram_kernel<TS, TG>), grid, NT, 0, X, ldx, (int)mm, (int)nn, nb, r, xrows, parts);
@@ -770,8 +809,21 @@ int qt_jacobi_svd_ws(qt_handle* h, TS* X, int64_t mm, int64_t nn, int64_t ldx, T
     {
       const double es = (double)sizeof(TS);
       h->work_jacobi_rounds += rounds;
+      h->work_jacobi_pairs += h->h_flags[QT_FLAG_ROTATED];
+      h->work_jacobi_inner += h->h_flags[QT_FLAG_INNER];
       h->work_jacobi_bytes += (double)rounds * (double)mm * (double)nn * es +
                               (double)h->h_flags[QT_FLAG_ROTATED] * JC * es * ((double)mm + (V ? 2.0 * (double)nn : 0.0));
+    }
+    if (trace) {
+      float off;
+      std::memcpy(&off, &h->h_flags[QT_FLAG_OFFMAX], sizeof(float));
+      float offbig;
+      std::memcpy(&offbig, &h->h_flags[QT_FLAG_OFFBIG], sizeof(float));
+      std::fprintf(stderr,
+                   "jacobi %lldx%lld sweep %d: rotated pairs %d, inner sweeps %d, max rel off-diagonal %.3e "
+                   "(columns above 1e-3 ||X||: %.3e)\n",
+                   (long long)mm, (long long)nn, sweep, h->h_flags[QT_FLAG_ROTATED], h->h_flags[QT_FLAG_INNER], off,
+                   offbig);
     }
     if (h->h_flags[QT_FLAG_NONFINITE]) return qt_fail(h, QT_ENUMERIC, "jacobi: non-finite value in the matrix");
     if (h->h_flags[QT_FLAG_ROTATED] == 0) break;
@@ -788,21 +840,21 @@ int qt_jacobi_svd_ws(qt_handle* h, TS* X, int64_t mm, int64_t nn, int64_t ldx, T
   return QT_OK;
 }
 template int qt_jacobi_svd_ws<double2>(qt_handle*, double2*, int64_t, int64_t, int64_t, double2*, int64_t, double,
-                                       int, int*, double2*);
+                                       int, int*, double2*, double);
 template int qt_jacobi_svd_ws<float2>(qt_handle*, float2*, int64_t, int64_t, int64_t, float2*, int64_t, double, int,
-                                      int*, double2*);
+                                      int*, double2*, double);
 
 template <typename TS>
 int qt_jacobi_svd(qt_handle* h, TS* X, int64_t mm, int64_t nn, int64_t ldx, TS* V, int64_t ldv, double tol,
-                  int max_sweeps, int* sweeps_out) {
+                  int max_sweeps, int* sweeps_out, double nu_rel) {
   int nb = 0, chunks = 0;
   const int nparts = qt_jacobi_layout(mm, nn, &nb, &chunks);
   qt_scratch s(h);
   double2* parts;
   QT_TRY(s.get(&parts, (size_t)nparts));
-  return qt_jacobi_svd_ws<TS>(h, X, mm, nn, ldx, V, ldv, tol, max_sweeps, sweeps_out, parts);
+  return qt_jacobi_svd_ws<TS>(h, X, mm, nn, ldx, V, ldv, tol, max_sweeps, sweeps_out, parts, nu_rel);
 }
 template int qt_jacobi_svd<double2>(qt_handle*, double2*, int64_t, int64_t, int64_t, double2*, int64_t, double, int,
-                                    int*);
+                                    int*, double);
 template int qt_jacobi_svd<float2>(qt_handle*, float2*, int64_t, int64_t, int64_t, float2*, int64_t, double, int,
-                                   int*);
+                                   int*, double);

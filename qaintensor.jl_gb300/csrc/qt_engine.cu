@@ -55,6 +55,8 @@ extern "C" int qt_work_counters(const qt_handle* h, double* out) {
   out[1] = h->work_jacobi_rounds;
   out[2] = h->work_tc_flops;
   out[3] = h->work_tc_launches;
+  out[4] = h->work_jacobi_pairs;
+  out[5] = h->work_jacobi_inner;
   return QT_OK;
 }
 
@@ -578,6 +580,13 @@ double fp32_floor_rel(const qt_handle* h, int64_t m, int64_t n) {
   return h->cfg.noise_floor > 0 ? h->cfg.noise_floor : 4.0 * std::sqrt((double)std::max(m, n)) * 5.96e-8;
 }
 
+// Columns frozen at sqrt(rows) u ||theta|| hold up to ~0.35 min(m,n) u
+// ||theta|| of weight in total; a cutoff above 1.2 min(m,n) u ||theta||
+// leaves them inside the tail with room to spare.
+bool fast_freeze_ok(int64_t m, int64_t n, double eff_cut, double theta_norm) {
+  return eff_cut >= 1.2 * (double)std::min(m, n) * 5.96e-8 * theta_norm;
+}
+
 // FP32-storage truncated split of theta (m x n, ld m, not modified): the
 // one-sided block Jacobi runs on theta itself (tall or square) or on
 // theta^H (wide), with no QR preconditioning -- theta' may be numerically
@@ -592,9 +601,13 @@ double fp32_floor_rel(const qt_handle* h, int64_t m, int64_t n) {
 // tensor-core GEMMs), so A' B' carries no error beyond the truncation.
 // `extra_tail` (>= 0) is a weight outside this factorisation (a sketch's
 // residual), counted as the smallest tail value of the rank rule.
+// `fast_freeze`: the rank is decided far above the FP32 rounding level (a
+// chi_max cap, or a cutoff well above the noise floor), so the Jacobi may
+// freeze columns below sqrt(rows) u ||theta||_F and skip the sweeps that only
+// rotate rounding noise.
 template <typename TO>
 int svd_split_direct32(qt_handle* h, const float2* theta, int64_t m, int64_t n, double cutoff, int chi_max,
-                       TO** Aout, TO** Bout, SvdOut* o, double extra_tail = -1.0) {
+                       TO** Aout, TO** Bout, SvdOut* o, double extra_tail = -1.0, bool fast_freeze = false) {
   qt_scratch s(h);
   const bool wide = m < n;
   const int64_t rows = wide ? n : m, cols = wide ? m : n;
@@ -607,7 +620,7 @@ int svd_split_direct32(qt_handle* h, const float2* theta, int64_t m, int64_t n, 
     QT_CHECK_CUDA(h, cudaMemcpyAsync(X, theta, sizeof(float2) * m * n, cudaMemcpyDeviceToDevice, h->stream));
   }
   QT_TRY(qt_jacobi_svd<float2>(h, X, rows, cols, rows, V, cols, auto_tol(h, rows, true), h->cfg.max_sweeps,
-                               &o->sweeps));
+                               &o->sweeps, fast_freeze ? std::sqrt((double)rows) * 5.96e-8 : -1.0));
   double* sig;
   int* perm;
   QT_TRY(s.get(&sig, (size_t)cols));
@@ -759,9 +772,10 @@ int svd_split_chosen(qt_handle* h, float2* theta, int64_t m, int64_t n, double c
   // A sketch of three quarters of the matrix or more saves less in the small
   // SVD than its range finder and orthogonalisation cost: factor theta'
   // directly.
+  const bool fast = cap_bound || fast_freeze_ok(m, n, eff_cut, std::sqrt(tn2));
   if (4 * l >= 3 * kmin || kmin <= 32) {
     *sketch = 0;
-    const int rc = svd_split_direct32<TO>(h, theta, m, n, eff_cut, chi_max, Aout, Bout, o);
+    const int rc = svd_split_direct32<TO>(h, theta, m, n, eff_cut, chi_max, Aout, Bout, o, -1.0, fast);
     if (rc == QT_ENUMERIC) {  // the FP32-storage Jacobi did not settle: exact FP64 path
       qt_dfree(h, *Aout);
       qt_dfree(h, *Bout);
@@ -815,7 +829,7 @@ int svd_split_chosen(qt_handle* h, float2* theta, int64_t m, int64_t n, double c
   QT_TRY(qt_adjoint_copy<float2>(h, BH, n, l, n, Bm, l));
   float2 *Ab = nullptr, *Bb = nullptr;
   {
-    const int rc = svd_split_direct32<float2>(h, Bm, l, n, eff_cut, chi_max, &Ab, &Bb, o, *residual);
+    const int rc = svd_split_direct32<float2>(h, Bm, l, n, eff_cut, chi_max, &Ab, &Bb, o, *residual, fast);
     if (rc == QT_ENUMERIC) {  // the small SVD did not settle: exact FP64 path
       qt_dfree(h, Ab);
       qt_dfree(h, Bb);
@@ -870,8 +884,9 @@ int qt_split_device(qt_handle* h, int dtype, const void* M, int64_t m, int64_t n
     double n2 = 0;
     QT_CHECK_CUDA(h, cudaMemcpyAsync(&n2, dn, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     QT_CHECK_CUDA(h, cudaStreamSynchronize(h->stream));
-    rc = svd_split_direct32<float2>(h, (const float2*)M, m, n, std::max(cutoff, fp32_floor_rel(h, m, n) * std::sqrt(n2)),
-                                    chi_max, (float2**)A, (float2**)B, &o);
+    const double cut = std::max(cutoff, fp32_floor_rel(h, m, n) * std::sqrt(n2));
+    rc = svd_split_direct32<float2>(h, (const float2*)M, m, n, cut, chi_max, (float2**)A, (float2**)B, &o, -1.0,
+                                    fast_freeze_ok(m, n, cut, std::sqrt(n2)));
   } else {
     qt_scratch s(h);
     double2* Mc;
@@ -1179,8 +1194,9 @@ int host_truncated_svd64(qt_handle* h, const double2* M64, const float2* M32, in
     double n2 = 0;
     QT_CHECK_CUDA(h, cudaMemcpyAsync(&n2, dn, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     QT_CHECK_CUDA(h, cudaStreamSynchronize(h->stream));
-    rc = svd_split_direct32<double2>(h, dM, m, n, std::max(cutoff, fp32_floor_rel(h, m, n) * std::sqrt(n2)), chi_max,
-                                     &A, &B, &o);
+    const double cut = std::max(cutoff, fp32_floor_rel(h, m, n) * std::sqrt(n2));
+    rc = svd_split_direct32<double2>(h, dM, m, n, cut, chi_max, &A, &B, &o, -1.0,
+                                     fast_freeze_ok(m, n, cut, std::sqrt(n2)));
   } else {
     double2* dM;
     QT_TRY(s.get(&dM, (size_t)m * n));

@@ -39,6 +39,7 @@ struct qt_handle {
   // written back and their V rows read and written); tensor-core GEMM TF32
   // flops (24 M N K per complex product) and launches
   double work_jacobi_bytes = 0, work_jacobi_rounds = 0, work_tc_flops = 0, work_tc_launches = 0;
+  double work_jacobi_pairs = 0, work_jacobi_inner = 0;  // rotated pairs, pair-solver inner sweeps
   bool prof = false;
   std::vector<qt_profile_rec> prof_recs;
   std::vector<cudaEvent_t> event_pool;
@@ -55,6 +56,8 @@ enum {
   QT_FLAG_NONFINITE = 1, // a kernel met a non-finite value
   QT_FLAG_CHOL = 2,      // a Cholesky factorisation lost positive definiteness
   QT_FLAG_OFFMAX = 3,    // Jacobi: largest relative off-diagonal above tol this sweep (float bits)
+  QT_FLAG_INNER = 4,     // Jacobi: inner sweeps of the pair solvers this sweep
+  QT_FLAG_OFFBIG = 5,    // Jacobi: OFFMAX over pairs of columns above 1e-3 ||X||_F (float bits)
   QT_FLAG_COUNT = 8
 };
 
@@ -217,11 +220,13 @@ int qt_norm2(qt_handle* h, const C* x, int64_t n, double* d_out);
 // TS = storage type.
 template <typename TS>
 int qt_jacobi_svd(qt_handle* h, TS* X, int64_t mm, int64_t nn, int64_t ldx, TS* V, int64_t ldv,
-                  double tol, int max_sweeps, int* sweeps_out);
+                  double tol, int max_sweeps, int* sweeps_out, double nu_rel = -1.0);
 // The same with a caller-supplied partial-Gram workspace of qt_jacobi_layout() double2 entries.
+// nu_rel > 0: columns with norm <= nu_rel ||X||_F are frozen (not rotated,
+// not tested); <= 0: the default for the storage precision.
 template <typename TS>
 int qt_jacobi_svd_ws(qt_handle* h, TS* X, int64_t mm, int64_t nn, int64_t ldx, TS* V, int64_t ldv, double tol,
-                     int max_sweeps, int* sweeps_out, double2* parts);
+                     int max_sweeps, int* sweeps_out, double2* parts, double nu_rel = -1.0);
 int qt_jacobi_layout(int64_t mm, int64_t nn, int* nb_out, int* chunks_out);
 
 // k_trunc.cu -----------------------------------------------------------------

@@ -62,3 +62,30 @@ def test_contract_svd_mps_matches_oracle(engine):
         assert got.shape == ref.shape
         assert np.abs(got - ref).max() <= 1e-10 * np.abs(ref).max()
     eng.close()
+
+
+def test_switch_wires_and_permute_match_oracle(engine):
+    """switch!(mps, i, j) and permute!(mps, order) (src/switch.jl) as ladders
+    of GPU switches, against the oracle's restatement."""
+    rng = np.random.default_rng(9)
+    n = 6
+    psi = crandn(rng, 2 ** n)
+    psi /= np.linalg.norm(psi)
+    eng = engine.Engine(mode="plain")
+    for op, arg in (("wires", (2, 5)), ("wires", (6, 1)), ("perm", [3, 1, 6, 2, 5, 4])):
+        ref = O.mps_from_state(psi)
+        mps = eng.mps(ref.tensors)
+        if op == "wires":
+            O.switch_wires(ref, *arg)
+            mps.switch_wires(*arg)
+        else:
+            O.permute_mps(ref, arg)
+            mps.permute(arg)
+        got = O.mps_to_state(mps.sites())
+        want = O.mps_to_state(O.sites_from_reference_mps(ref.tensors))
+        assert np.abs(got - want).max() <= 1e-11, (op, arg)
+        mps.free()
+    with pytest.raises(engine.QaintensorError, match="repeat values"):
+        m = eng.product_state(3)
+        m.permute([1, 1, 2])
+    eng.close()
