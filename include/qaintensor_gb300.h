@@ -71,8 +71,10 @@ typedef struct {
                               below the FP32-level arithmetic and are not resolved */
   uint64_t seed;           /* sketch RNG seed */
   int tc_gemm;             /* chosen mode: 1 = tcgen05 split-TF32x3 products, 0 = FP32 SIMT */
-  int jacobi_kernel;       /* 0 = one launch per Jacobi round (cluster-resident pair rows) where
-                              the rows fit shared memory, 1 = always the three-kernel round */
+  int jacobi_kernel;       /* Jacobi round: 0 = automatic (FP32 storage: Gram + pair solver, then
+                              rotation, two launches; FP64: one launch with cluster-resident pair
+                              rows where they fit shared memory), 1 = three kernels (Gram
+                              partials, pair solver, rotation), 2 = the one-launch cluster round */
 } qt_config;
 
 typedef struct {

@@ -47,6 +47,7 @@ constexpr int JR = 64;       // rows per shared-memory slab
 constexpr int NT = 256;      // threads per CTA
 constexpr int MAX_INNER = 12;
 constexpr int NGRAM = JC * JC;
+static_assert(NT == NGRAM, "the round kernel maps one Gram entry to each thread");
 
 __device__ inline void tournament(int r, int q, int n, int& a, int& b) {
   // circle method over n (even) players, round r, table q
@@ -357,6 +358,192 @@ __device__ int diagonalise_scaled(pair_eig_scaled& sh, const int* col, float tol
   return sweep + (sweep < max_inner ? 1 : 0);
 }
 
+// The scaled iteration with one update phase per round: the 16 indices form
+// 8 disjoint pairs, so every entry of Jt^H Ghat Jt is a 2x2 combination of
+// old entries -- G'[x][y] = sum_{a in {x,x'}} sum_{b in {y,y'}} conj(Jt[a][x])
+// Ghat[a][b] Jt[b][y] (x' the partner of x, Jt = I on a pair that does not
+// rotate) -- and every entry of Wt Jt a combination of two.  Thread t owns
+// entry (t / 16, t % 16) of both; the new values go to the other buffer, so
+// a round costs two barriers (parameters, update).  Requires NT == 256.
+struct pair_eig_scaled2 {
+  float d[2][JC];
+  float d0[JC];
+  float2 G[2][JC][JC + 1];
+  float2 W[2][JC][JC + 1];
+  int partner[JC];          // partner index of each index in this round
+  float2 jt[JC][2];         // Jt[x][x] (real in .x) and Jt[x'][x] for column x
+  int inner_rot;
+};
+
+__device__ int diagonalise_scaled2(pair_eig_scaled2& sh, const int* col, float tol_inner, float nu2, int max_inner,
+                                   int* buf_out) {
+  const int t = threadIdx.x, x = t >> 4, y = t & 15;
+  int cur = 0, sweep = 0;
+  // inner_rot holds the number (1-based) of the last sweep that rotated; the
+  // caller zeroes it before the first call
+  for (; sweep < max_inner; sweep++) {
+    for (int ir = 0; ir < JC - 1; ir++) {
+      if (t < JC / 2) {
+        int p, q;
+        tournament(ir, t, JC, p, q);
+        sh.partner[p] = q; sh.partner[q] = p;
+        const float a = sh.d[cur][p], b = sh.d[cur][q];
+        const float2 gs = sh.G[cur][p][q];
+        const float ags = sqrtf(gs.x * gs.x + gs.y * gs.y);
+        float2 jpp = make_float2(1.f, 0.f), jqp = make_float2(0.f, 0.f), jpq = jqp, jqq = jpp;
+        float a2 = a, b2 = b;
+        if (col[p] >= 0 && col[q] >= 0 && a > nu2 && b > nu2 && ags > tol_inner) {
+          const float ag = ags * sqrtf(a * b);  // |gamma|
+          const float zeta = __fdividef(b - a, 2.f * ag);
+          const float r1 = sqrtf(fmaf(zeta, zeta, 1.f));
+          const float tt = copysignf(__frcp_rn(fabsf(zeta) + r1), zeta);
+          const float c = rsqrtf(fmaf(tt, tt, 1.f)), sn = c * tt;
+          const float inv = __frcp_rn(ags);
+          const float2 e = make_float2(gs.x * inv, gs.y * inv);
+          a2 = fmaxf(a - tt * ag, nu2);  // a column driven to the noise level is frozen
+          b2 = b + tt * ag;
+          const float ia2 = rsqrtf(a2), ib2 = rsqrtf(b2), sqa = sqrtf(a), sqb = sqrtf(b);
+          jpp = make_float2(c * sqa * ia2, 0.f);
+          jqp = make_float2(-sn * e.x * sqb * ia2, sn * e.y * sqb * ia2);  // -s conj(e) sqrt(b/a')
+          jpq = make_float2(sn * e.x * sqa * ib2, sn * e.y * sqa * ib2);   //  s e sqrt(a/b')
+          jqq = make_float2(c * sqb * ib2, 0.f);
+          sh.inner_rot = sweep + 1;
+        }
+        // column p of Jt: rows p (jpp) and q (jqp); column q: rows q (jqq) and p (jpq)
+        sh.jt[p][0] = jpp; sh.jt[p][1] = jqp;
+        sh.jt[q][0] = jqq; sh.jt[q][1] = jpq;
+        sh.d[cur ^ 1][p] = a2; sh.d[cur ^ 1][q] = b2;
+      }
+      __syncthreads();
+      {
+        const int xp = sh.partner[x], yp = sh.partner[y];
+        const float2 jxx = sh.jt[x][0], jpx = sh.jt[x][1];  // Jt[x][x], Jt[x'][x]
+        const float2 jyy = sh.jt[y][0], jpy = sh.jt[y][1];  // Jt[y][y], Jt[y'][y]
+        // Ghat: diagonal implicit 1; the off-diagonal of a rotated pair is
+        // zero, that of a pair left alone keeps its (sub-tolerance) value
+        float2 gnew = make_float2(0.f, 0.f);
+        if (xp == y && x != y) {
+          const bool rotated = jxx.x != 1.f || jxx.y != 0.f || jpx.x != 0.f || jpx.y != 0.f;
+          if (!rotated) gnew = sh.G[cur][x][y];
+        } else if (x != y) {
+          const float2 g_xy = sh.G[cur][x][y], g_xq = sh.G[cur][x][yp];
+          const float2 g_py = sh.G[cur][xp][y], g_pq = sh.G[cur][xp][yp];
+          // column step: h_a = G[a][y] Jt[y][y] + G[a][y'] Jt[y'][y] for a in {x, x'}
+          const float2 hx = cadd(cmul(g_xy, jyy), cmul(g_xq, jpy));
+          const float2 hp = cadd(cmul(g_py, jyy), cmul(g_pq, jpy));
+          // row step: conj(Jt[x][x]) h_x + conj(Jt[x'][x]) h_x'
+          gnew = cadd(cmul(cconj(jxx), hx), cmul(cconj(jpx), hp));
+        }
+        sh.G[cur ^ 1][x][y] = gnew;
+        // Wt Jt: column y
+        const float2 w_xy = sh.W[cur][x][y], w_xq = sh.W[cur][x][yp];
+        sh.W[cur ^ 1][x][y] = cadd(cmul(w_xy, jyy), cmul(w_xq, jpy));
+      }
+      cur ^= 1;
+      __syncthreads();
+    }
+    const int again = sh.inner_rot == sweep + 1;  // written before the round's closing barrier
+    __syncthreads();  // every thread has read it before the next sweep may write it again
+    if (!again) break;
+  }
+  // W = D0^{-1/2} Wt D^{1/2}
+  {
+    const float d0 = sh.d0[x];
+    sh.W[cur][x][y] = d0 > 0.f ? cscale(sh.W[cur][x][y], sqrtf(sh.d[cur][y] / d0))
+                               : make_float2(x == y ? 1.f : 0.f, 0.f);
+  }
+  __syncthreads();
+  *buf_out = cur;
+  return sweep + (sweep < max_inner ? 1 : 0);
+}
+
+// The same iteration run by one warp (lanes 0-31 of the calling CTA; the
+// other warps skip it and wait at the caller's barrier): the per-round
+// barriers become __syncwarp, and the idle warps leave the SM's issue slots
+// to the other CTAs resident on it.  Rotation parameters are computed by
+// lanes 0-7 (one pair each) and kept in shared memory; the column updates
+// (256 row tasks over G and Wt) and row updates (128) are spread over the
+// 32 lanes.
+__device__ int diagonalise_scaled_warp(pair_eig_scaled& sh, const int* col, float tol_inner, float nu2,
+                                       int max_inner) {
+  const int lane = threadIdx.x & 31;
+  int sweep = 0;
+  for (; sweep < max_inner; sweep++) {
+    int rotated = 0;
+    for (int ir = 0; ir < JC - 1; ir++) {
+      int on = 0;
+      if (lane < JC / 2) {
+        int p, q;
+        tournament(ir, lane, JC, p, q);
+        sh.rp[lane] = p; sh.rq[lane] = q;
+        const float a = sh.d[p], b = sh.d[q];
+        const float2 gs = sh.G[p][q];
+        const float ags = sqrtf(gs.x * gs.x + gs.y * gs.y);
+        if (col[p] >= 0 && col[q] >= 0 && a > nu2 && b > nu2 && ags > tol_inner) {
+          const float ag = ags * sqrtf(a * b);  // |gamma|
+          const float zeta = __fdividef(b - a, 2.f * ag);
+          const float r1 = sqrtf(fmaf(zeta, zeta, 1.f));
+          const float tt = copysignf(__frcp_rn(fabsf(zeta) + r1), zeta);
+          const float c = rsqrtf(fmaf(tt, tt, 1.f)), sn = c * tt;
+          const float inv = __frcp_rn(ags);
+          const float2 e = make_float2(gs.x * inv, gs.y * inv);
+          const float a2 = fmaxf(a - tt * ag, nu2), b2 = b + tt * ag;
+          const float ia2 = rsqrtf(a2), ib2 = rsqrtf(b2), sqa = sqrtf(a), sqb = sqrtf(b);
+          sh.na[lane] = a2; sh.nb[lane] = b2;
+          sh.kpp[lane] = c * sqa * ia2;
+          sh.kqp[lane] = make_float2(-sn * e.x * sqb * ia2, sn * e.y * sqb * ia2);
+          sh.kpq[lane] = make_float2(sn * e.x * sqa * ib2, sn * e.y * sqa * ib2);
+          sh.kqq[lane] = c * sqb * ib2;
+          on = 1;
+        }
+        sh.ron[lane] = on;
+      }
+      rotated |= __any_sync(0xffffffffu, on);
+      __syncwarp();
+      // columns p, q: tasks (matrix, pair k, row r) = lane + 32 i
+#pragma unroll
+      for (int i = 0; i < 8; i++) {
+        const int task = lane + 32 * i, mat = task >> 7, k = (task >> 4) & 7, r = task & 15;
+        if (!sh.ron[k]) continue;
+        const int p = sh.rp[k], q = sh.rq[k];
+        if (mat == 0 && (r == p || r == q)) continue;
+        float2 (*M)[JC + 1] = mat == 0 ? sh.G : sh.W;
+        const float2 xp = M[r][p], xq = M[r][q];
+        M[r][p] = cadd(cscale(xp, sh.kpp[k]), cmul(sh.kqp[k], xq));
+        M[r][q] = cadd(cmul(sh.kpq[k], xp), cscale(xq, sh.kqq[k]));
+      }
+      __syncwarp();
+      // rows p, q of Ghat; the pair's own 2x2 block and diagonal
+#pragma unroll
+      for (int i = 0; i < 4; i++) {
+        const int task = lane + 32 * i, k = task >> 4, r = task & 15;
+        if (!sh.ron[k]) continue;
+        const int p = sh.rp[k], q = sh.rq[k];
+        if (r != p && r != q) {
+          const float2 gp = sh.G[p][r], gq = sh.G[q][r];
+          sh.G[p][r] = cadd(cscale(gp, sh.kpp[k]), cmul(cconj(sh.kqp[k]), gq));
+          sh.G[q][r] = cadd(cmul(cconj(sh.kpq[k]), gp), cscale(gq, sh.kqq[k]));
+        } else if (r == p) {
+          sh.G[p][q] = make_float2(0.f, 0.f);
+          sh.G[q][p] = make_float2(0.f, 0.f);
+          sh.d[p] = sh.na[k];
+          sh.d[q] = sh.nb[k];
+        }
+      }
+      __syncwarp();
+    }
+    if (!rotated) break;
+  }
+  // W = D0^{-1/2} Wt D^{1/2}
+  for (int e = lane; e < NGRAM; e += 32) {
+    const int i = e >> 4, j = e & 15;
+    const float d0 = sh.d0[i];
+    sh.W[i][j] = d0 > 0.f ? cscale(sh.W[i][j], sqrtf(sh.d[j] / d0)) : make_float2(i == j ? 1.f : 0.f, 0.f);
+  }
+  __syncwarp();
+  return sweep + (sweep < max_inner ? 1 : 0);
+}
+
 // One CTA per block pair: sum the partial Grams, test the pair, and when it
 // needs rotating diagonalise its 16x16 Gram; the unitary goes to wout[pair]
 // and the decision to rot[pair] (the apply kernel reads both).
@@ -366,13 +553,13 @@ eig_kernel(int nn, int nb, int round, int nparts, const double2* __restrict__ pa
            int* __restrict__ flags) {
   __shared__ pair_eig_shared<double> sh;
   __shared__ int col[JC];
-  __shared__ int any_rot, bad, offmax_blk;
+  __shared__ int any_rot, bad, offmax_blk, offbig_blk;
 
   const int t = threadIdx.x;
   const int pair = blockIdx.x;
   const double nu2 = nu_rel2 * (*xnorm2);
   pair_columns(round, pair, nb, nn, col);
-  if (t == 0) { any_rot = 0; bad = 0; offmax_blk = 0; }
+  if (t == 0) { any_rot = 0; bad = 0; offmax_blk = 0; offbig_blk = 0; }
   __syncthreads();
   // sum the partial Grams of this pair in a fixed order
   for (int e = t; e < NGRAM; e += NT) {
@@ -392,7 +579,8 @@ eig_kernel(int nn, int nb, int round, int nparts, const double2* __restrict__ pa
   }
   // is this pair already orthogonal to tol?  (the largest relative
   // off-diagonal above tol is recorded as float bits, one atomic per pair)
-  float relmax = 0.f;
+  float relmax = 0.f, relbig = 0.f;
+  const double big2 = 1e-6 * (*xnorm2);
   for (int e = t; e < NGRAM; e += NT) {
     const int i = e / JC, j = e % JC;
     if (i < j && col[i] >= 0 && col[j] >= 0) {
@@ -400,14 +588,21 @@ eig_kernel(int nn, int nb, int round, int nparts, const double2* __restrict__ pa
       const double g = sqrt(cabs2(sh.G[i][j]));
       if (a > nu2 && b > nu2 && g > tol * sqrt(a * b)) {
         any_rot = 1;
-        relmax = fmaxf(relmax, (a > 0 && b > 0) ? (float)fmin(g / sqrt(a * b), 1.0) : 1.0f);
+        const float rel = (a > 0 && b > 0) ? (float)fmin(g / sqrt(a * b), 1.0) : 1.0f;
+        relmax = fmaxf(relmax, rel);
+        if (a > big2 && b > big2) relbig = fmaxf(relbig, rel);
       }
     }
   }
-  for (int o = 16; o > 0; o >>= 1) relmax = fmaxf(relmax, __shfl_xor_sync(0xffffffffu, relmax, o));
+  for (int o = 16; o > 0; o >>= 1) {
+    relmax = fmaxf(relmax, __shfl_xor_sync(0xffffffffu, relmax, o));
+    relbig = fmaxf(relbig, __shfl_xor_sync(0xffffffffu, relbig, o));
+  }
   if ((t & 31) == 0 && relmax > 0.f) atomicMax(&offmax_blk, __float_as_int(relmax));
+  if ((t & 31) == 0 && relbig > 0.f) atomicMax(&offbig_blk, __float_as_int(relbig));
   __syncthreads();
   if (t == 0 && offmax_blk > 0) atomicMax(&flags[QT_FLAG_OFFMAX], offmax_blk);
+  if (t == 0 && offbig_blk > 0) atomicMax(&flags[QT_FLAG_OFFBIG], offbig_blk);
   __syncthreads();
   if (t == 0) rot[pair] = any_rot;
   if (!any_rot) return;
@@ -461,15 +656,18 @@ __device__ void rotate_rows(const TS* __restrict__ Xs, int lds, int nrows, TS* _
   }
 }
 
-// rows [0, nrows) of the pair's columns of M -> Xs (column c at Xs + c*lds)
+// rows [0, nrows) of the pair's columns of M -> Xs (column c at Xs + c*lds).
+// Thread t copies rows t, t + NT, ...: for each row it issues the 16 column
+// loads back to back (independent, coalesced across the warp) before storing.
 template <typename TS>
 __device__ void stage_rows(const TS* __restrict__ M, int64_t ld, int nrows, int rows_alloc, const int* col,
                            TS* __restrict__ Xs, int lds) {
-  for (int idx = threadIdx.x; idx < JC * rows_alloc; idx += NT) {
-    const int c = idx / rows_alloc, rr = idx - c * rows_alloc;
-    TS v = czero<TS>();
-    if (rr < nrows && col[c] >= 0) v = M[rr + ld * col[c]];
-    Xs[c * lds + rr] = v;
+  for (int rr = threadIdx.x; rr < rows_alloc; rr += NT) {
+    TS v[JC];
+#pragma unroll
+    for (int c = 0; c < JC; c++) v[c] = (rr < nrows && col[c] >= 0) ? M[rr + ld * col[c]] : czero<TS>();
+#pragma unroll
+    for (int c = 0; c < JC; c++) Xs[c * lds + rr] = v[c];
   }
 }
 
@@ -486,7 +684,8 @@ template <typename TS>
 __global__ void __launch_bounds__(NT)
 pair_round_kernel(TS* __restrict__ X, int64_t ldx, int mm, TS* __restrict__ V, int64_t ldv, int nn, int nb, int round,
                   int csize, int xrows_c, int vrows_c, int lds, double tol, double tol_inner, double nu_rel2,
-                  const double* __restrict__ xnorm2, int* __restrict__ flags, int max_inner) {
+                  const double* __restrict__ xnorm2, int* __restrict__ flags, int max_inner,
+                  unsigned long long* __restrict__ phase_ns) {
   typedef typename real_of<TS>::type RE;
   extern __shared__ __align__(16) unsigned char dyn_smem[];
   TS* Xs = reinterpret_cast<TS*>(dyn_smem);
@@ -499,6 +698,18 @@ pair_round_kernel(TS* __restrict__ X, int64_t ldx, int mm, TS* __restrict__ V, i
   const int crank = (int)cluster.block_rank();
   const int pair = blockIdx.x / csize;
   const int t = threadIdx.x;
+  // optional phase timing (diagnostics): thread 0 of each CTA adds the time
+  // spent in each phase to phase_ns[8 * (crank != 0) + phase]
+  unsigned long long tp = 0;
+  auto phase = [&](int ph) {
+    if (phase_ns && t == 0) {
+      unsigned long long tn;
+      asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(tn));
+      if (ph > 0) atomicAdd(&phase_ns[8 * (crank != 0) + ph - 1], tn - tp);
+      tp = tn;
+    }
+  };
+  phase(0);
   pair_columns(round, pair, nb, nn, col);
   if (t == 0) { any_rot = 0; bad = 0; offmax_blk = 0; offbig_blk = 0; }
   __syncthreads();
@@ -506,63 +717,88 @@ pair_round_kernel(TS* __restrict__ X, int64_t ldx, int mm, TS* __restrict__ V, i
   const int xr = max(0, min(mm, xb + xrows_c) - xb);
   stage_rows<TS>(X + xb, ldx, xr, xrows_c, col, Xs, lds);
   __syncthreads();
-  // partial Gram over this CTA's rows (upper triangle, mirrored)
-  if (t < JC * (JC + 1) / 2) {
-    int r = 0, rem = t;
-    while (rem >= JC - r) { rem -= JC - r; r++; }
-    const int gi = r, gj = r + rem;
-    const TS* xi = Xs + gi * lds;
-    const TS* xj = Xs + gj * lds;
-    TS a0 = czero<TS>(), a1 = czero<TS>();
-    int rr = 0;
-    for (; rr + 1 < xr; rr += 2) {
-      cfma_conj(a0, xi[rr], xj[rr]);
-      cfma_conj(a1, xi[rr + 1], xj[rr + 1]);
+  phase(1);  // 0: stage
+  // partial Gram over this CTA's rows: the 36 upper 2x2 tiles of the 16x16
+  // Gram, four threads per tile on interleaved rows (four independent
+  // complex accumulators each), reduced with shuffles in a fixed order
+  if (t < 160) {
+    const int tile = t >> 2, g = t & 3;
+    const bool act = tile < 36;
+    int bi = 0, rem = act ? tile : 0;
+    while (rem >= 8 - bi) { rem -= 8 - bi; bi++; }
+    const int bj = bi + rem;
+    const TS* x0 = Xs + (2 * bi) * lds;
+    const TS* x1 = x0 + lds;
+    const TS* y0 = Xs + (2 * bj) * lds;
+    const TS* y1 = y0 + lds;
+    TS a00 = czero<TS>(), a01 = czero<TS>(), a10 = czero<TS>(), a11 = czero<TS>();
+    if (act) {
+      for (int rr = g; rr < xr; rr += 4) {
+        const TS p0 = x0[rr], p1 = x1[rr], q0 = y0[rr], q1 = y1[rr];
+        cfma_conj(a00, p0, q0);
+        cfma_conj(a01, p0, q1);
+        cfma_conj(a10, p1, q0);
+        cfma_conj(a11, p1, q1);
+      }
     }
-    if (rr < xr) cfma_conj(a0, xi[rr], xj[rr]);
-    const TS a = cadd(a0, a1);
-    gpart[gi * JC + gj] = a;
-    gpart[gj * JC + gi] = cconj(a);
+#pragma unroll
+    for (int o = 1; o <= 2; o <<= 1) {
+      a00.x += __shfl_xor_sync(0xffffffffu, a00.x, o); a00.y += __shfl_xor_sync(0xffffffffu, a00.y, o);
+      a01.x += __shfl_xor_sync(0xffffffffu, a01.x, o); a01.y += __shfl_xor_sync(0xffffffffu, a01.y, o);
+      a10.x += __shfl_xor_sync(0xffffffffu, a10.x, o); a10.y += __shfl_xor_sync(0xffffffffu, a10.y, o);
+      a11.x += __shfl_xor_sync(0xffffffffu, a11.x, o); a11.y += __shfl_xor_sync(0xffffffffu, a11.y, o);
+    }
+    if (act && g == 0) {
+      const int i0 = 2 * bi, j0 = 2 * bj;
+      gpart[i0 * JC + j0] = a00;             gpart[j0 * JC + i0] = cconj(a00);
+      gpart[(i0 + 1) * JC + j0 + 1] = a11;   gpart[(j0 + 1) * JC + i0 + 1] = cconj(a11);
+      gpart[i0 * JC + j0 + 1] = a01;         gpart[(j0 + 1) * JC + i0] = cconj(a01);
+      if (bi != bj) { gpart[(i0 + 1) * JC + j0] = a10; gpart[j0 * JC + i0 + 1] = cconj(a10); }
+    }
   }
+  __syncthreads();
+  phase(2);  // 1: Gram
   cluster.sync();
+  phase(3);  // 2: first cluster barrier
   const double nu2 = nu_rel2 * (*xnorm2);
   if (crank == 0) {
+    // FP64 sums of the partials in rank order; the remote loads are issued
+    // together (independent) before the sum
+    double2 sum_e;
+    {
+      const int e = t;  // NT == NGRAM: one Gram entry per thread
+      TS v[8];
+#pragma unroll
+      for (int q = 0; q < 8; q++) v[q] = q < csize ? cluster.map_shared_rank(gpart, q)[e] : czero<TS>();
+      sum_e = make_double2(0, 0);
+#pragma unroll
+      for (int q = 0; q < 8; q++)
+        if (q < csize) sum_e = cadd(sum_e, ccast<double2>(v[q]));
+      if (!isfinite(sum_e.x) || !isfinite(sum_e.y)) bad = 1;
+    }
     if constexpr (F32) {
-      // FP64 sums of the partials, then the scaled FP32 Gram
       __shared__ double dd[JC];
-      if (t < JC) {
-        double s = 0;
-        for (int q = 0; q < csize; q++) s += (double)cluster.map_shared_rank(gpart, q)[t * JC + t].x;
-        dd[t] = s;
-        sh.d[t] = (float)s;
-        sh.d0[t] = (float)s;
-        if (!isfinite(s)) bad = 1;
+      const int i = t / JC, j = t % JC;
+      if (i == j) {
+        dd[i] = sum_e.x;
+        sh.d[i] = (float)sum_e.x;
+        sh.d0[i] = (float)sum_e.x;
       }
       __syncthreads();
-      for (int e = t; e < NGRAM; e += NT) {
-        const int i = e / JC, j = e % JC;
-        double2 s = make_double2(0, 0);
-        for (int q = 0; q < csize; q++) s = cadd(s, ccast<double2>(cluster.map_shared_rank(gpart, q)[e]));
-        if (!isfinite(s.x) || !isfinite(s.y)) bad = 1;
-        float2 v = make_float2(0.f, 0.f);
-        if (i != j && dd[i] > nu2 && dd[j] > nu2) {
-          const double sc = 1.0 / sqrt(dd[i] * dd[j]);
-          v = make_float2((float)(s.x * sc), (float)(s.y * sc));
-        }
-        sh.G[i][j] = v;
-        sh.W[i][j] = make_float2(i == j ? 1.f : 0.f, 0.f);
+      float2 v = make_float2(0.f, 0.f);
+      if (i != j && dd[i] > nu2 && dd[j] > nu2) {
+        const double sc = 1.0 / sqrt(dd[i] * dd[j]);
+        v = make_float2((float)(sum_e.x * sc), (float)(sum_e.y * sc));
       }
+      sh.G[i][j] = v;
+      sh.W[i][j] = make_float2(i == j ? 1.f : 0.f, 0.f);
     } else {
-      for (int e = t; e < NGRAM; e += NT) {
-        double2 s = make_double2(0, 0);
-        for (int q = 0; q < csize; q++) s = cadd(s, ccast<double2>(cluster.map_shared_rank(gpart, q)[e]));
-        sh.G[e / JC][e % JC] = s;
-        sh.W[e / JC][e % JC] = mk((RE)((e / JC) == (e % JC) ? 1 : 0), (RE)0);
-        if (!isfinite(s.x) || !isfinite(s.y)) bad = 1;
-      }
+      sh.G[t / JC][t % JC] = sum_e;
+      sh.W[t / JC][t % JC] = mk((RE)((t / JC) == (t % JC) ? 1 : 0), (RE)0);
     }
   }
   cluster.sync();  // the partials have been read: CTAs 1.. may leave or move on
+  phase(4);  // 3: partial sums + second barrier
   if (crank == 0) {
     // is this pair already orthogonal to tol?  (the largest relative
     // off-diagonal above tol is recorded as float bits)
@@ -608,19 +844,29 @@ pair_round_kernel(TS* __restrict__ X, int64_t ldx, int mm, TS* __restrict__ V, i
     if (any_rot) {
       if (t == 0) atomicAdd(&flags[QT_FLAG_ROTATED], 1);
       int inner;
-      if constexpr (F32) inner = diagonalise_scaled(sh, col, (float)tol_inner, (float)nu2, max_inner);
-      else inner = diagonalise_pair<RE>(sh, col, tol_inner, nu2);
+      if constexpr (F32) {
+        inner = 0;
+        if (t < 32) inner = diagonalise_scaled_warp(sh, col, (float)tol_inner, (float)nu2, max_inner);
+        __syncthreads();
+      } else {
+        inner = diagonalise_pair<RE>(sh, col, tol_inner, nu2);
+      }
       if (t == 0) atomicAdd(&flags[QT_FLAG_INNER], inner);
     }
   }
+  __syncthreads();
+  phase(5);  // 4: test + pair solver (CTA 0)
   cluster.sync();  // CTA 0's decision and unitary are ready
   if (crank != 0) {
     if (t == 0) any_rot = *cluster.map_shared_rank(&any_rot, 0);
     for (int e = t; e < NGRAM; e += NT) sh.W[e / JC][e % JC] = cluster.map_shared_rank(&sh.W[0][0], 0)[(e / JC) * (JC + 1) + e % JC];
   }
   cluster.sync();  // CTA 0 stays resident until every copy is done
+  phase(6);  // 5: third/fourth barrier + unitary copy
   if (!any_rot) return;  // the same decision in every CTA of the cluster
   rotate_rows<TS>(Xs, lds, xr, X + xb, ldx, col, sh.W);
+  __syncthreads();
+  phase(7);  // 6: rotate X
   __syncthreads();  // Xs is reused for V
   if (V == nullptr) return;  // no accumulated rotations wanted
   const int vb = crank * vrows_c;
@@ -648,6 +894,193 @@ apply_kernel(TS* __restrict__ X, int64_t ldx, int mm, TS* __restrict__ V, int64_
   const int xb = chunk * x_rows_per_chunk, vb = chunk * v_rows_per_chunk;
   apply_rows<TS>(X, ldx, xb, min(mm, xb + x_rows_per_chunk), col, Wt, Xs);
   if (V) apply_rows<TS>(V, ldv, vb, min(nn, vb + v_rows_per_chunk), col, Wt, Xs);
+}
+
+// ---------------------------------------------------------------------------
+// FP32 storage, two launches per round
+// ---------------------------------------------------------------------------
+
+constexpr int SLAB = 256;  // rows per shared-memory slab of the Gram kernel (one per thread)
+
+// grid = pairs: one CTA forms the whole 16x16 Gram of its pair (rows streamed
+// through a shared-memory slab -- each thread loads one row's 16 values, the
+// next slab prefetched into registers during the current one's products;
+// the 36 upper 2x2 tiles, four threads each on interleaved rows, FP32
+// accumulation, shuffle reduction in a fixed order), tests the pair, and
+// runs the scaled pair solver.  The unitary goes to wout[pair], the decision
+// to rot[pair].
+__global__ void __launch_bounds__(NT)
+pair_eig32_kernel(const float2* __restrict__ X, int64_t ldx, int mm, int nn, int nb, int round, double tol,
+                  float tol_inner, double nu_rel2, const double* __restrict__ xnorm2, float2* __restrict__ wout,
+                  int* __restrict__ rot, int* __restrict__ flags, int max_inner) {
+  __shared__ float2 slab[SLAB][JC + 1];
+  __shared__ float2 gram[NGRAM];
+  __shared__ pair_eig_scaled2 sh;
+  __shared__ int col[JC];
+  __shared__ int any_rot, bad, offmax_blk, offbig_blk;
+  const int t = threadIdx.x, pair = blockIdx.x;
+  pair_columns(round, pair, nb, nn, col);
+  if (t == 0) { any_rot = 0; bad = 0; offmax_blk = 0; offbig_blk = 0; sh.inner_rot = 0; }
+  __syncthreads();
+  const float2* cp[JC];
+#pragma unroll
+  for (int c = 0; c < JC; c++) cp[c] = col[c] >= 0 ? X + ldx * col[c] : nullptr;
+  float2 pf[JC];
+#pragma unroll
+  for (int c = 0; c < JC; c++) pf[c] = (cp[c] && t < mm) ? cp[c][t] : make_float2(0.f, 0.f);
+  // 36 upper 2x2 tiles x 7 row groups = 252 threads; group g takes rows
+  // g, g + 7, ... of each slab
+  const int tile = t / 7, g = t - 7 * (t / 7);
+  const bool act = t < 252;
+  int bi = 0, rem = act ? tile : 0;
+  while (rem >= 8 - bi) { rem -= 8 - bi; bi++; }
+  const int bj = bi + rem;
+  float2 a00 = make_float2(0.f, 0.f), a01 = a00, a10 = a00, a11 = a00;
+  for (int r0 = 0; r0 < mm; r0 += SLAB) {
+#pragma unroll
+    for (int c = 0; c < JC; c++) slab[t][c] = pf[c];
+    __syncthreads();
+    const int rn = r0 + SLAB + t;
+#pragma unroll
+    for (int c = 0; c < JC; c++) pf[c] = (cp[c] && rn < mm) ? cp[c][rn] : make_float2(0.f, 0.f);
+    if (act) {
+#pragma unroll 4
+      for (int rr = g; rr < SLAB; rr += 7) {
+        const float2 p0 = slab[rr][2 * bi], p1 = slab[rr][2 * bi + 1], q0 = slab[rr][2 * bj], q1 = slab[rr][2 * bj + 1];
+        cfma_conj(a00, p0, q0);
+        cfma_conj(a01, p0, q1);
+        cfma_conj(a10, p1, q0);
+        cfma_conj(a11, p1, q1);
+      }
+    }
+    __syncthreads();
+  }
+  // reduce the 7 row groups in a fixed order (partials in the slab buffer)
+  float2* red = &slab[0][0];
+  if (act) {
+    red[(g * 36 + tile) * 4 + 0] = a00;
+    red[(g * 36 + tile) * 4 + 1] = a01;
+    red[(g * 36 + tile) * 4 + 2] = a10;
+    red[(g * 36 + tile) * 4 + 3] = a11;
+  }
+  __syncthreads();
+  if (t < 144) {
+    const int tl = t >> 2, q = t & 3;
+    float2 v = red[tl * 4 + q];
+    for (int gg = 1; gg < 7; gg++) v = cadd(v, red[(gg * 36 + tl) * 4 + q]);
+    int ti = 0, tr = tl;
+    while (tr >= 8 - ti) { tr -= 8 - ti; ti++; }
+    const int tj = ti + tr;
+    const int r = 2 * ti + (q >> 1), c = 2 * tj + (q & 1);
+    if (ti != tj || r <= c) {
+      gram[r * JC + c] = v;
+      gram[c * JC + r] = cconj(v);
+    }
+  }
+  __syncthreads();
+  // scaled Gram, diagonal, test
+  const double nu2 = nu_rel2 * (*xnorm2);
+  const int i = t / JC, j = t % JC;
+  {
+    const float2 v = gram[t];
+    if (!isfinite(v.x) || !isfinite(v.y)) bad = 1;
+    if (i == j) { sh.d[0][i] = v.x; sh.d0[i] = v.x; }
+  }
+  __syncthreads();
+  {
+    const float di = sh.d[0][i], dj = sh.d[0][j];
+    float2 v = make_float2(0.f, 0.f);
+    if (i != j && di > nu2 && dj > nu2) v = cscale(gram[t], (float)(1.0 / sqrt((double)di * (double)dj)));
+    sh.G[0][i][j] = v;
+    sh.W[0][i][j] = make_float2(i == j ? 1.f : 0.f, 0.f);
+  }
+  __syncthreads();
+  if (bad) {
+    if (t == 0) { atomicOr(&flags[QT_FLAG_NONFINITE], 1); rot[pair] = 0; }
+    return;
+  }
+  {
+    float relmax = 0.f, relbig = 0.f;
+    const double big2 = 1e-6 * (*xnorm2);
+    if (i < j && col[i] >= 0 && col[j] >= 0 && sh.d[0][i] > nu2 && sh.d[0][j] > nu2) {
+      const float rel = fminf(sqrtf(cabs2(sh.G[0][i][j])), 1.f);
+      if (rel > tol) {
+        any_rot = 1;
+        relmax = rel;
+        if (sh.d[0][i] > big2 && sh.d[0][j] > big2) relbig = rel;
+      }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      relmax = fmaxf(relmax, __shfl_xor_sync(0xffffffffu, relmax, o));
+      relbig = fmaxf(relbig, __shfl_xor_sync(0xffffffffu, relbig, o));
+    }
+    if ((t & 31) == 0 && relmax > 0.f) atomicMax(&offmax_blk, __float_as_int(relmax));
+    if ((t & 31) == 0 && relbig > 0.f) atomicMax(&offbig_blk, __float_as_int(relbig));
+  }
+  __syncthreads();
+  if (t == 0) {
+    rot[pair] = any_rot;
+    if (offmax_blk > 0) atomicMax(&flags[QT_FLAG_OFFMAX], offmax_blk);
+    if (offbig_blk > 0) atomicMax(&flags[QT_FLAG_OFFBIG], offbig_blk);
+    if (any_rot) atomicAdd(&flags[QT_FLAG_ROTATED], 1);
+  }
+  if (!any_rot) return;
+  int buf = 0;
+  const int inner = diagonalise_scaled2(sh, col, tol_inner, (float)nu2, max_inner, &buf);
+  if (t == 0) atomicAdd(&flags[QT_FLAG_INNER], inner);
+  wout[(size_t)pair * NGRAM + t] = sh.W[buf][i][j];
+}
+
+// grid (pair, row chunk): rotate this chunk's rows of X (and of V) by the
+// pair's unitary.  One row per thread: its 16 values are loaded together
+// (independent, coalesced across the warp), multiplied by W from shared
+// memory (two entries per 16-byte broadcast load) and stored; no staging,
+// no barriers after W is loaded.
+__global__ void __launch_bounds__(NT, 3)
+pair_apply32_kernel(float2* __restrict__ X, int64_t ldx, int mm, float2* __restrict__ V, int64_t ldv, int nn, int nb,
+                    int round, int x_rows_per_chunk, int v_rows_per_chunk, const float2* __restrict__ win,
+                    const int* __restrict__ rot) {
+  __shared__ __align__(16) float2 Wt[JC][JC];
+  __shared__ int col[JC];
+  const int pair = blockIdx.x, chunk = blockIdx.y;
+  if (!rot[pair]) return;
+  pair_columns(round, pair, nb, nn, col);
+  Wt[threadIdx.x / JC][threadIdx.x % JC] = win[(size_t)pair * NGRAM + threadIdx.x];
+  __syncthreads();
+  int cidx[JC];
+#pragma unroll
+  for (int c = 0; c < JC; c++) cidx[c] = col[c];
+  for (int pass = 0; pass < 2; pass++) {
+    float2* M = pass == 0 ? X : V;
+    if (M == nullptr) break;
+    const int64_t ld = pass == 0 ? ldx : ldv;
+    const int per = pass == 0 ? x_rows_per_chunk : v_rows_per_chunk;
+    const int lim = pass == 0 ? mm : nn;
+    const int e = min(lim, chunk * per + per);
+    for (int r = chunk * per + threadIdx.x; r < e; r += NT) {
+      float2 x[JC];
+#pragma unroll
+      for (int k = 0; k < JC; k++) x[k] = cidx[k] >= 0 ? M[r + ld * cidx[k]] : make_float2(0.f, 0.f);
+      float2 acc[JC];
+#pragma unroll
+      for (int c = 0; c < JC; c++) acc[c] = make_float2(0.f, 0.f);
+      // keep the 256 W entries in shared memory (re-read per row) rather than
+      // letting them be hoisted into registers across the row loop
+      asm volatile("" ::: "memory");
+#pragma unroll
+      for (int k = 0; k < JC; k++) {
+#pragma unroll
+        for (int c = 0; c < JC; c += 2) {
+          const float4 w = *reinterpret_cast<const float4*>(&Wt[k][c]);
+          cfma(acc[c], x[k], make_float2(w.x, w.y));
+          cfma(acc[c + 1], x[k], make_float2(w.z, w.w));
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < JC; c++)
+        if (cidx[c] >= 0) M[r + ld * cidx[c]] = acc[c];
+    }
+  }
 }
 
 // ||X||_F^2 in FP64, one CTA per column, added into *out.
@@ -712,7 +1145,8 @@ static int fused_shape(int64_t mm, int pairs, size_t elem, int* rows_c, int* lds
 template <typename TS>
 static int launch_pair_round(qt_handle* h, int csize, int pairs, size_t smem, TS* X, int64_t ldx, int mm, TS* V,
                              int64_t ldv, int nn, int nb, int round, int xrows_c, int vrows_c, int lds, double tol,
-                             double tol_inner, double nu_rel2, const double* xnorm2, int max_inner) {
+                             double tol_inner, double nu_rel2, const double* xnorm2, int max_inner,
+                             unsigned long long* phase_ns) {
   cudaLaunchConfig_t lc = {};
   lc.gridDim = dim3((unsigned)(pairs * csize));
   lc.blockDim = dim3(NT);
@@ -727,7 +1161,8 @@ static int launch_pair_round(qt_handle* h, int csize, int pairs, size_t smem, TS
   lc.numAttrs = 1;
   if (h->prof) qt_prof_before(h, "pair_round_kernel<TS>");
   const cudaError_t e = cudaLaunchKernelEx(&lc, pair_round_kernel<TS>, X, ldx, mm, V, ldv, nn, nb, round, csize,
-                                           xrows_c, vrows_c, lds, tol, tol_inner, nu_rel2, xnorm2, h->d_flags, max_inner);
+                                           xrows_c, vrows_c, lds, tol, tol_inner, nu_rel2, xnorm2, h->d_flags, max_inner,
+                                           phase_ns);
   if (h->prof) qt_prof_after(h);
   h->launches++;
   if (e != cudaSuccess) return qt_fail(h, QT_ECUDA, std::string("launch pair_round_kernel: ") + cudaGetErrorString(e));
@@ -770,10 +1205,21 @@ int qt_jacobi_svd_ws(qt_handle* h, TS* X, int64_t mm, int64_t nn, int64_t ldx, T
   const double nu_rel = nu_rel_in > 0 ? nu_rel_in
                         : (fp32 ? 4.0 * u : 4.0 * std::sqrt((double)std::max<int64_t>(mm, 16)) * u);
   const double nu_rel2 = nu_rel * nu_rel;
-  // one-launch rounds when the pair's rows fit a cluster's shared memory
+  // Round implementation (cfg.jacobi_kernel): FP32 storage by default runs
+  // two launches per round (Gram + pair solver, then the rotation); 2 asks
+  // for the one-launch cluster round, 1 for the three-kernel round.  FP64
+  // storage uses the one-launch round where a pair's rows fit a cluster's
+  // shared memory.
+  const int jk = h->cfg.jacobi_kernel;
+  const bool two_launch = fp32 && jk == 0;
   int xrows_c = 0, lds = 0;
   size_t smem = 0;
-  const int csize = (h->cfg.jacobi_kernel == 1) ? 0 : fused_shape(mm, pairs, sizeof(TS), &xrows_c, &lds, &smem);
+  const int csize = (jk == 1 || two_launch) ? 0 : fused_shape(mm, pairs, sizeof(TS), &xrows_c, &lds, &smem);
+  // two-launch shape: the rotation grid fills the 152 SMs once at three
+  // resident CTAs each (80 registers a thread), rows looped per thread
+  int achunks = std::max(1, std::min<int>((3 * 152) / pairs, (int)((mm + NT - 1) / NT)));
+  const int axrows = (int)(((mm + achunks - 1) / achunks + 31) / 32 * 32);
+  const int avrows = (int)(((nn + achunks - 1) / achunks + 31) / 32 * 32);
   const int vrows_c = csize ? (int)((nn + csize - 1) / csize) : 0;
   // the inner eigen-solve is driven well below the outer threshold so that the
   // rounding of the applied rotation cannot leave the pair just above `tol`
@@ -781,8 +1227,17 @@ int qt_jacobi_svd_ws(qt_handle* h, TS* X, int64_t mm, int64_t nn, int64_t ldx, T
   if (csize)
     QT_CHECK_CUDA(h, cudaFuncSetAttribute(pair_round_kernel<TS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           (int)smem));
-  // QT_JACOBI_TRACE=1 in the environment prints one line per sweep to stderr
+  // QT_JACOBI_TRACE=1 in the environment prints one line per sweep to stderr;
+  // QT_JACOBI_PHASES=1 adds the average time per phase of the one-launch
+  // rounds at the end (CTA 0 of each cluster / the others)
   static const bool trace = std::getenv("QT_JACOBI_TRACE") != nullptr;
+  static const bool phases = std::getenv("QT_JACOBI_PHASES") != nullptr;
+  unsigned long long* phase_ns = nullptr;
+  qt_scratch pscratch(h);
+  if (phases && csize) {
+    QT_TRY(pscratch.get(&phase_ns, 16));
+    QT_CHECK_CUDA(h, cudaMemsetAsync(phase_ns, 0, 16 * sizeof(unsigned long long), h->stream));
+  }
   int sweep = 0;
   for (; sweep < max_sweeps; sweep++) {
     // the pair solver diagonalises fully in the first sweeps; once the
@@ -792,9 +1247,18 @@ int qt_jacobi_svd_ws(qt_handle* h, TS* X, int64_t mm, int64_t nn, int64_t ldx, T
     const int max_inner = sweep < 2 ? MAX_INNER : std::max(1, std::min(inner_cap, MAX_INNER));
     QT_CHECK_CUDA(h, cudaMemsetAsync(h->d_flags, 0, sizeof(int) * QT_FLAG_COUNT, h->stream));
     for (int r = 0; r < rounds; r++) {
+      if (two_launch) {
+        if constexpr (sizeof(typename real_of<TS>::type) == 4) {
+          QT_LAUNCH(h, pair_eig32_kernel, pairs, NT, 0, (const float2*)X, ldx, (int)mm, (int)nn, nb, r, tol,
+                    (float)tol_inner, nu_rel2, (const double*)xnorm2, (float2*)wbuf, rotf, h->d_flags, max_inner);
+          QT_LAUNCH(h, pair_apply32_kernel, dim3(pairs, achunks), NT, 0, (float2*)X, ldx, (int)mm, (float2*)V, ldv,
+                    (int)nn, nb, r, axrows, avrows, (const float2*)wbuf, (const int*)rotf);
+        }
+        continue;
+      }
       if (csize) {
         QT_TRY(launch_pair_round<TS>(h, csize, pairs, smem, X, ldx, (int)mm, V, ldv, (int)nn, nb, r, xrows_c, vrows_c,
-                                     lds, tol, tol_inner, nu_rel2, xnorm2, max_inner));
+                                     lds, tol, tol_inner, nu_rel2, xnorm2, max_inner, phase_ns));
         continue;
       }
       QT_LAUNCH(h, (gram_kernel<TS, TG>), grid, NT, 0, X, ldx, (int)mm, (int)nn, nb, r, xrows, parts);
@@ -829,12 +1293,29 @@ int qt_jacobi_svd_ws(qt_handle* h, TS* X, int64_t mm, int64_t nn, int64_t ldx, T
     if (h->h_flags[QT_FLAG_ROTATED] == 0) break;
   }
   *sweeps_out = sweep + (sweep < max_sweeps ? 1 : 0);
+  if (phase_ns) {
+    unsigned long long hp[16];
+    QT_CHECK_CUDA(h, cudaMemcpy(hp, phase_ns, sizeof(hp), cudaMemcpyDeviceToHost));
+    const double launches = (double)(*sweeps_out) * rounds;
+    const char* nm[7] = {"stage", "gram", "barrier1", "sums+barrier2", "test+solver", "barriers+copy", "rotate"};
+    for (int g = 0; g < 2; g++) {
+      const double ctas = launches * pairs * (g == 0 ? 1 : csize - 1);
+      std::fprintf(stderr, "jacobi phases (%s), us per CTA per round:", g == 0 ? "CTA 0" : "other CTAs");
+      for (int i = 0; i < 7; i++) std::fprintf(stderr, " %s %.2f", nm[i], ctas > 0 ? hp[8 * g + i] / ctas * 1e-3 : 0.0);
+      std::fprintf(stderr, "\n");
+    }
+  }
   if (sweep >= max_sweeps) {
     // Out of sweeps: accept when the worst remaining pair is orthogonal to
-    // 1e-6 relative (its effect on the singular values is below 1e-12).
-    float off;
+    // 1e-6 relative (its effect on the singular values is below 1e-12), or --
+    // FP32 storage -- when every column above 1e-3 ||X||_F has converged and
+    // only columns near the rounding level still rotate (their total weight,
+    // all the tail rule needs of them, is rotation-invariant).
+    float off, offbig;
     std::memcpy(&off, &h->h_flags[QT_FLAG_OFFMAX], sizeof(float));
+    std::memcpy(&offbig, &h->h_flags[QT_FLAG_OFFBIG], sizeof(float));
     if (off < 1e-6f) return QT_OK;
+    if (fp32 && offbig <= tol) return QT_OK;
     return qt_fail(h, QT_ENUMERIC, "jacobi: no convergence within the sweep limit (off " + std::to_string(off) + ")");
   }
   return QT_OK;

@@ -26,7 +26,7 @@ def graded(rng, m, n, decay):
 SHAPES = [(40, 24), (24, 40), (300, 201), (701, 513), (1100, 1003), (1536, 1536)]
 
 
-@pytest.mark.parametrize("kernel", [0, 1])
+@pytest.mark.parametrize("kernel", [0, 1, 2])
 @pytest.mark.parametrize("shape", SHAPES)
 def test_fp64_jacobi_matches_lapack(engine, shape, kernel):
     rng = np.random.default_rng(sum(shape) + kernel)
@@ -44,7 +44,7 @@ def test_fp64_jacobi_matches_lapack(engine, shape, kernel):
     eng.close()
 
 
-@pytest.mark.parametrize("kernel", [0, 1])
+@pytest.mark.parametrize("kernel", [0, 1, 2])
 @pytest.mark.parametrize("shape", SHAPES)
 def test_fp32_jacobi_matches_lapack(engine, shape, kernel):
     rng = np.random.default_rng(7 * sum(shape) + kernel)
