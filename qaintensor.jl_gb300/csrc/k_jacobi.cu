@@ -362,9 +362,10 @@ __device__ int diagonalise_scaled(pair_eig_scaled& sh, const int* col, float tol
 // 8 disjoint pairs, so every entry of Jt^H Ghat Jt is a 2x2 combination of
 // old entries -- G'[x][y] = sum_{a in {x,x'}} sum_{b in {y,y'}} conj(Jt[a][x])
 // Ghat[a][b] Jt[b][y] (x' the partner of x, Jt = I on a pair that does not
-// rotate) -- and every entry of Wt Jt a combination of two.  Thread t owns
-// entry (t / 16, t % 16) of both; the new values go to the other buffer, so
-// a round costs two barriers (parameters, update).  Requires NT == 256.
+// rotate) -- and every entry of Wt Jt a combination of two.  Thread t < 256
+// owns entry (t / 16, t % 16) of both; the new values go to the other
+// buffer, so a round costs two barriers (parameters, update).  Every thread
+// of the block calls it (the barriers are block-wide).
 struct pair_eig_scaled2 {
   float d[2][JC];
   float d0[JC];
@@ -377,7 +378,8 @@ struct pair_eig_scaled2 {
 
 __device__ int diagonalise_scaled2(pair_eig_scaled2& sh, const int* col, float tol_inner, float nu2, int max_inner,
                                    int* buf_out) {
-  const int t = threadIdx.x, x = t >> 4, y = t & 15;
+  const int t = threadIdx.x, x = (t >> 4) & 15, y = t & 15;
+  const bool owner = t < NGRAM;
   int cur = 0, sweep = 0;
   // inner_rot holds the number (1-based) of the last sweep that rotated; the
   // caller zeroes it before the first call
@@ -415,7 +417,7 @@ __device__ int diagonalise_scaled2(pair_eig_scaled2& sh, const int* col, float t
         sh.d[cur ^ 1][p] = a2; sh.d[cur ^ 1][q] = b2;
       }
       __syncthreads();
-      {
+      if (owner) {
         const int xp = sh.partner[x], yp = sh.partner[y];
         const float2 jxx = sh.jt[x][0], jpx = sh.jt[x][1];  // Jt[x][x], Jt[x'][x]
         const float2 jyy = sh.jt[y][0], jpy = sh.jt[y][1];  // Jt[y][y], Jt[y'][y]
@@ -447,7 +449,7 @@ __device__ int diagonalise_scaled2(pair_eig_scaled2& sh, const int* col, float t
     if (!again) break;
   }
   // W = D0^{-1/2} Wt D^{1/2}
-  {
+  if (owner) {
     const float d0 = sh.d0[x];
     sh.W[cur][x][y] = d0 > 0.f ? cscale(sh.W[cur][x][y], sqrtf(sh.d[cur][y] / d0))
                                : make_float2(x == y ? 1.f : 0.f, 0.f);
@@ -900,52 +902,66 @@ apply_kernel(TS* __restrict__ X, int64_t ldx, int mm, TS* __restrict__ V, int64_
 // FP32 storage, two launches per round
 // ---------------------------------------------------------------------------
 
-constexpr int SLAB = 256;  // rows per shared-memory slab of the Gram kernel (one per thread)
+constexpr int SLAB = 256;  // rows per shared-memory slab of the Gram kernel
+constexpr int NTG = 512;   // threads of the Gram kernel
 
-// grid = pairs: one CTA forms the whole 16x16 Gram of its pair (rows streamed
-// through a shared-memory slab -- each thread loads one row's 16 values, the
-// next slab prefetched into registers during the current one's products;
-// the 36 upper 2x2 tiles, four threads each on interleaved rows, FP32
-// accumulation, shuffle reduction in a fixed order), tests the pair, and
+// grid = pairs: one CTA of 512 threads forms the whole 16x16 Gram of its pair
+// (rows streamed through a 256-row shared-memory slab -- each thread loads
+// half a row, the next slab prefetched into registers during the current
+// one's products; the 36 upper 2x2 tiles, 14 threads each on interleaved
+// rows, FP32 accumulation, reduction in a fixed order), tests the pair, and
 // runs the scaled pair solver.  The unitary goes to wout[pair], the decision
 // to rot[pair].
-__global__ void __launch_bounds__(NT)
+__global__ void __launch_bounds__(NTG, 1)
 pair_eig32_kernel(const float2* __restrict__ X, int64_t ldx, int mm, int nn, int nb, int round, double tol,
                   float tol_inner, double nu_rel2, const double* __restrict__ xnorm2, float2* __restrict__ wout,
-                  int* __restrict__ rot, int* __restrict__ flags, int max_inner) {
+                  int* __restrict__ rot, int* __restrict__ flags, int max_inner, unsigned long long* phase_ns) {
   __shared__ float2 slab[SLAB][JC + 1];
   __shared__ float2 gram[NGRAM];
   __shared__ pair_eig_scaled2 sh;
   __shared__ int col[JC];
   __shared__ int any_rot, bad, offmax_blk, offbig_blk;
   const int t = threadIdx.x, pair = blockIdx.x;
+  unsigned long long tp = 0;
+  auto phase = [&](int ph) {  // optional diagnostics: time per phase into phase_ns[ph - 1]
+    if (phase_ns && t == 0) {
+      unsigned long long tn;
+      asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(tn));
+      if (ph > 0) atomicAdd(&phase_ns[ph - 1], tn - tp);
+      tp = tn;
+    }
+  };
+  phase(0);
   pair_columns(round, pair, nb, nn, col);
   if (t == 0) { any_rot = 0; bad = 0; offmax_blk = 0; offbig_blk = 0; sh.inner_rot = 0; }
   __syncthreads();
-  const float2* cp[JC];
+  // slab loads: thread t covers row (t & 255) of columns 8 (t >> 8) .. + 7
+  const int lr = t & (SLAB - 1), ch = 8 * (t >> 8);
+  const float2* cp[8];
 #pragma unroll
-  for (int c = 0; c < JC; c++) cp[c] = col[c] >= 0 ? X + ldx * col[c] : nullptr;
-  float2 pf[JC];
+  for (int c = 0; c < 8; c++) cp[c] = col[ch + c] >= 0 ? X + ldx * col[ch + c] : nullptr;
+  float2 pf[8];
 #pragma unroll
-  for (int c = 0; c < JC; c++) pf[c] = (cp[c] && t < mm) ? cp[c][t] : make_float2(0.f, 0.f);
-  // 36 upper 2x2 tiles x 7 row groups = 252 threads; group g takes rows
-  // g, g + 7, ... of each slab
-  const int tile = t / 7, g = t - 7 * (t / 7);
-  const bool act = t < 252;
+  for (int c = 0; c < 8; c++) pf[c] = (cp[c] && lr < mm) ? cp[c][lr] : make_float2(0.f, 0.f);
+  // 36 upper 2x2 tiles x 14 row groups = 504 threads; group g takes rows
+  // g, g + 14, ... of each slab
+  constexpr int NGRP = 14;
+  const int tile = t / NGRP, g = t - NGRP * (t / NGRP);
+  const bool act = t < 36 * NGRP;
   int bi = 0, rem = act ? tile : 0;
   while (rem >= 8 - bi) { rem -= 8 - bi; bi++; }
   const int bj = bi + rem;
   float2 a00 = make_float2(0.f, 0.f), a01 = a00, a10 = a00, a11 = a00;
   for (int r0 = 0; r0 < mm; r0 += SLAB) {
 #pragma unroll
-    for (int c = 0; c < JC; c++) slab[t][c] = pf[c];
+    for (int c = 0; c < 8; c++) slab[lr][ch + c] = pf[c];
     __syncthreads();
-    const int rn = r0 + SLAB + t;
+    const int rn = r0 + SLAB + lr;
 #pragma unroll
-    for (int c = 0; c < JC; c++) pf[c] = (cp[c] && rn < mm) ? cp[c][rn] : make_float2(0.f, 0.f);
+    for (int c = 0; c < 8; c++) pf[c] = (cp[c] && rn < mm) ? cp[c][rn] : make_float2(0.f, 0.f);
     if (act) {
 #pragma unroll 4
-      for (int rr = g; rr < SLAB; rr += 7) {
+      for (int rr = g; rr < SLAB; rr += NGRP) {
         const float2 p0 = slab[rr][2 * bi], p1 = slab[rr][2 * bi + 1], q0 = slab[rr][2 * bj], q1 = slab[rr][2 * bj + 1];
         cfma_conj(a00, p0, q0);
         cfma_conj(a01, p0, q1);
@@ -955,7 +971,8 @@ pair_eig32_kernel(const float2* __restrict__ X, int64_t ldx, int mm, int nn, int
     }
     __syncthreads();
   }
-  // reduce the 7 row groups in a fixed order (partials in the slab buffer)
+  phase(1);  // 0: Gram products
+  // reduce the row groups in a fixed order (partials in the slab buffer)
   float2* red = &slab[0][0];
   if (act) {
     red[(g * 36 + tile) * 4 + 0] = a00;
@@ -967,7 +984,7 @@ pair_eig32_kernel(const float2* __restrict__ X, int64_t ldx, int mm, int nn, int
   if (t < 144) {
     const int tl = t >> 2, q = t & 3;
     float2 v = red[tl * 4 + q];
-    for (int gg = 1; gg < 7; gg++) v = cadd(v, red[(gg * 36 + tl) * 4 + q]);
+    for (int gg = 1; gg < NGRP; gg++) v = cadd(v, red[(gg * 36 + tl) * 4 + q]);
     int ti = 0, tr = tl;
     while (tr >= 8 - ti) { tr -= 8 - ti; ti++; }
     const int tj = ti + tr;
@@ -980,14 +997,15 @@ pair_eig32_kernel(const float2* __restrict__ X, int64_t ldx, int mm, int nn, int
   __syncthreads();
   // scaled Gram, diagonal, test
   const double nu2 = nu_rel2 * (*xnorm2);
-  const int i = t / JC, j = t % JC;
-  {
+  const bool owner = t < NGRAM;
+  const int i = (t / JC) & 15, j = t % JC;
+  if (owner) {
     const float2 v = gram[t];
     if (!isfinite(v.x) || !isfinite(v.y)) bad = 1;
     if (i == j) { sh.d[0][i] = v.x; sh.d0[i] = v.x; }
   }
   __syncthreads();
-  {
+  if (owner) {
     const float di = sh.d[0][i], dj = sh.d[0][j];
     float2 v = make_float2(0.f, 0.f);
     if (i != j && di > nu2 && dj > nu2) v = cscale(gram[t], (float)(1.0 / sqrt((double)di * (double)dj)));
@@ -1002,7 +1020,7 @@ pair_eig32_kernel(const float2* __restrict__ X, int64_t ldx, int mm, int nn, int
   {
     float relmax = 0.f, relbig = 0.f;
     const double big2 = 1e-6 * (*xnorm2);
-    if (i < j && col[i] >= 0 && col[j] >= 0 && sh.d[0][i] > nu2 && sh.d[0][j] > nu2) {
+    if (owner && i < j && col[i] >= 0 && col[j] >= 0 && sh.d[0][i] > nu2 && sh.d[0][j] > nu2) {
       const float rel = fminf(sqrtf(cabs2(sh.G[0][i][j])), 1.f);
       if (rel > tol) {
         any_rot = 1;
@@ -1024,11 +1042,13 @@ pair_eig32_kernel(const float2* __restrict__ X, int64_t ldx, int mm, int nn, int
     if (offbig_blk > 0) atomicMax(&flags[QT_FLAG_OFFBIG], offbig_blk);
     if (any_rot) atomicAdd(&flags[QT_FLAG_ROTATED], 1);
   }
+  phase(2);  // 1: reduction, scaled Gram, test
   if (!any_rot) return;
   int buf = 0;
   const int inner = diagonalise_scaled2(sh, col, tol_inner, (float)nu2, max_inner, &buf);
   if (t == 0) atomicAdd(&flags[QT_FLAG_INNER], inner);
-  wout[(size_t)pair * NGRAM + t] = sh.W[buf][i][j];
+  if (owner) wout[(size_t)pair * NGRAM + t] = sh.W[buf][i][j];
+  phase(3);  // 2: pair solver
 }
 
 // grid (pair, row chunk): rotate this chunk's rows of X (and of V) by the
@@ -1215,9 +1235,8 @@ int qt_jacobi_svd_ws(qt_handle* h, TS* X, int64_t mm, int64_t nn, int64_t ldx, T
   int xrows_c = 0, lds = 0;
   size_t smem = 0;
   const int csize = (jk == 1 || two_launch) ? 0 : fused_shape(mm, pairs, sizeof(TS), &xrows_c, &lds, &smem);
-  // two-launch shape: the rotation grid fills the 152 SMs once at three
-  // resident CTAs each (80 registers a thread), rows looped per thread
-  int achunks = std::max(1, std::min<int>((3 * 152) / pairs, (int)((mm + NT - 1) / NT)));
+  // two-launch shape: one row per rotation thread, about eight CTAs per SM
+  int achunks = std::max(1, std::min<int>((8 * 152 + pairs - 1) / pairs, (int)((mm + NT - 1) / NT)));
   const int axrows = (int)(((mm + achunks - 1) / achunks + 31) / 32 * 32);
   const int avrows = (int)(((nn + achunks - 1) / achunks + 31) / 32 * 32);
   const int vrows_c = csize ? (int)((nn + csize - 1) / csize) : 0;
@@ -1234,7 +1253,7 @@ int qt_jacobi_svd_ws(qt_handle* h, TS* X, int64_t mm, int64_t nn, int64_t ldx, T
   static const bool phases = std::getenv("QT_JACOBI_PHASES") != nullptr;
   unsigned long long* phase_ns = nullptr;
   qt_scratch pscratch(h);
-  if (phases && csize) {
+  if (phases && (csize || two_launch)) {
     QT_TRY(pscratch.get(&phase_ns, 16));
     QT_CHECK_CUDA(h, cudaMemsetAsync(phase_ns, 0, 16 * sizeof(unsigned long long), h->stream));
   }
@@ -1249,8 +1268,9 @@ int qt_jacobi_svd_ws(qt_handle* h, TS* X, int64_t mm, int64_t nn, int64_t ldx, T
     for (int r = 0; r < rounds; r++) {
       if (two_launch) {
         if constexpr (sizeof(typename real_of<TS>::type) == 4) {
-          QT_LAUNCH(h, pair_eig32_kernel, pairs, NT, 0, (const float2*)X, ldx, (int)mm, (int)nn, nb, r, tol,
-                    (float)tol_inner, nu_rel2, (const double*)xnorm2, (float2*)wbuf, rotf, h->d_flags, max_inner);
+          QT_LAUNCH(h, pair_eig32_kernel, pairs, NTG, 0, (const float2*)X, ldx, (int)mm, (int)nn, nb, r, tol,
+                    (float)tol_inner, nu_rel2, (const double*)xnorm2, (float2*)wbuf, rotf, h->d_flags, max_inner,
+                    phase_ns);
           QT_LAUNCH(h, pair_apply32_kernel, dim3(pairs, achunks), NT, 0, (float2*)X, ldx, (int)mm, (float2*)V, ldv,
                     (int)nn, nb, r, axrows, avrows, (const float2*)wbuf, (const int*)rotf);
         }
@@ -1293,7 +1313,14 @@ int qt_jacobi_svd_ws(qt_handle* h, TS* X, int64_t mm, int64_t nn, int64_t ldx, T
     if (h->h_flags[QT_FLAG_ROTATED] == 0) break;
   }
   *sweeps_out = sweep + (sweep < max_sweeps ? 1 : 0);
-  if (phase_ns) {
+  if (phase_ns && two_launch) {
+    unsigned long long hp[3];
+    QT_CHECK_CUDA(h, cudaMemcpy(hp, phase_ns, sizeof(hp), cudaMemcpyDeviceToHost));
+    const double launches = (double)(*sweeps_out) * rounds * pairs;
+    std::fprintf(stderr, "jacobi Gram kernel, us per CTA: products %.2f, reduction+test %.2f, solver (rotating pairs "
+                 "only, averaged over all) %.2f\n", hp[0] / launches * 1e-3, hp[1] / launches * 1e-3,
+                 hp[2] / launches * 1e-3);
+  } else if (phase_ns) {
     unsigned long long hp[16];
     QT_CHECK_CUDA(h, cudaMemcpy(hp, phase_ns, sizeof(hp), cudaMemcpyDeviceToHost));
     const double launches = (double)(*sweeps_out) * rounds;
