@@ -382,9 +382,13 @@ def load_peaks():
 def roofline(prof, work, n_prof):
     """Roofline of the dominant kernel (largest total device time in the
     profiled updates), from the engine's algorithmic work counters:
-      pair_round_kernel (one-launch Jacobi round): HBM-class bound; bytes = X
-        columns read once per round + rotated pairs' X written and V rows
-        read and written;
+      Jacobi round kernels: HBM-class bound.  Algorithmic bytes of a round are
+        every column of X read once (the Gram products) plus the rotated
+        pairs' columns written once (and their V rows read and written).  Per
+        kernel: the Gram + pair-solver kernel (pair_eig32_kernel) is charged
+        the reads, the rotation kernel (pair_apply32_kernel) reads and writes
+        the rotated columns, a one-launch round (pair_round_kernel,
+        jacobi_round32_kernel) is charged the whole round;
       tc_gemm_kernel: tensor bound; 24 M N K TF32 flops per complex product,
         peak = half the measured dense bf16 rate (TF32 runs at half the bf16
         tensor rate)."""
@@ -393,11 +397,16 @@ def roofline(prof, work, n_prof):
     peaks, src = load_peaks()
     name, launches, ms = prof[0]
     per_launch_s = ms / 1e3 / launches
-    if name.startswith("pair_round_kernel") or name.startswith("(gram_kernel") or name.startswith("apply_kernel"):
+    jacobi = {"pair_round_kernel": work["jacobi_bytes"], "jacobi_round32_kernel": work["jacobi_bytes"],
+              "(gram_kernel": work["jacobi_gram_bytes"], "pair_eig32_kernel": work["jacobi_gram_bytes"],
+              "apply_kernel": 2.0 * work["jacobi_rot_bytes"], "pair_apply32_kernel": 2.0 * work["jacobi_rot_bytes"]}
+    for prefix, nbytes in jacobi.items():
+        if not name.startswith(prefix):
+            continue
         n_launch = work["jacobi_rounds"]
         if n_launch <= 0:
             return {"kernel": name, "note": "no Jacobi work recorded"}
-        bytes_per_launch = work["jacobi_bytes"] / n_launch
+        bytes_per_launch = nbytes / n_launch
         achieved = bytes_per_launch / per_launch_s / 1e9
         peak = peaks["hbm_gbs"]
         return {"kernel": name, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",

@@ -71,10 +71,13 @@ typedef struct {
                               below the FP32-level arithmetic and are not resolved */
   uint64_t seed;           /* sketch RNG seed */
   int tc_gemm;             /* chosen mode: 1 = tcgen05 split-TF32x3 products, 0 = FP32 SIMT */
-  int jacobi_kernel;       /* Jacobi round: 0 = automatic (FP32 storage: Gram + pair solver, then
-                              rotation, two launches; FP64: one launch with cluster-resident pair
-                              rows where they fit shared memory), 1 = three kernels (Gram
-                              partials, pair solver, rotation), 2 = the one-launch cluster round */
+  int jacobi_kernel;       /* Jacobi round: 0 = automatic (FP32 storage: one cooperative launch per
+                              sweep, each round rebuilding its columns from the previous round's
+                              unitaries, where one CTA per pair fits on the device, else 3; FP64:
+                              one launch with cluster-resident pair rows where they fit shared
+                              memory), 1 = three kernels (Gram partials, pair solver, rotation),
+                              2 = the one-launch cluster round, 3 = FP32 two launches per round
+                              (Gram + pair solver, then rotation) */
 } qt_config;
 
 typedef struct {
@@ -107,7 +110,9 @@ int64_t qt_launch_count(const qt_handle* h);
  * back, their V rows read and written), out[1] Jacobi rounds, out[2] TF32
  * flops of the tensor-core GEMMs (24 M N K per complex product), out[3] their
  * launches, out[4] Jacobi pair rotations, out[5] inner sweeps of the 16x16
- * pair solvers (out holds 6 doubles). */
+ * pair solvers, out[6] the part of out[0] read by the rounds' Gram products
+ * (every column of X once per round), out[7] bytes of X and V columns
+ * written by rotations (out holds 8 doubles). */
 int qt_work_counters(const qt_handle* h, double* out);
 
 /* ---- measurement helpers ------------------------------------------------ */

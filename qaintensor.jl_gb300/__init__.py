@@ -243,10 +243,11 @@ class Engine:
 
     def work_counters(self) -> dict:
         """Cumulative algorithmic work: Jacobi bytes/rounds, tensor-core TF32 flops/launches."""
-        out = (C.c_double * 6)()
+        out = (C.c_double * 8)()
         self._check(self._lib.qt_work_counters(self._h, out))
         return {"jacobi_bytes": out[0], "jacobi_rounds": out[1], "tc_flops": out[2], "tc_launches": out[3],
-                "jacobi_pairs": out[4], "jacobi_inner_sweeps": out[5]}
+                "jacobi_pairs": out[4], "jacobi_inner_sweeps": out[5], "jacobi_gram_bytes": out[6],
+                "jacobi_rot_bytes": out[7]}
 
     def sync(self):
         self._check(self._lib.qt_sync(self._h))

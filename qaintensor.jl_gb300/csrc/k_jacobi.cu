@@ -1103,6 +1103,438 @@ pair_apply32_kernel(float2* __restrict__ X, int64_t ldx, int mm, float2* __restr
   }
 }
 
+// ---------------------------------------------------------------------------
+// FP32 storage: one cooperative launch per sweep
+// ---------------------------------------------------------------------------
+//
+// CTA q owns table q of every round.  Round g (counted over the whole
+// iteration) rebuilds its two blocks from the previous round's data and
+// unitaries: a block whose round g-1 pair rotated becomes that pair's 16
+// columns times the matching 16x8 block of its unitary, otherwise it is
+// copied.  The rebuilt columns go to the other buffer of a ping-pong pair
+// (round g reads buffer (g-1)&1 and writes buffer g&1), and on their way
+// through shared memory they feed the Gram products, so a round reads and
+// writes every column once and needs no separate rotation pass.  Rounds are
+// chained per CTA through done[q] (the last round CTA q finished): round g
+// waits for the round g-1 CTAs whose output it reads (read after write) and
+// for those that read what it overwrites -- the previous contents of its
+// destination columns and of its unitary slot (write after read).  Every
+// wait is bounded; a wait that gives up sets QT_FLAG_ABORT, which ends the
+// other CTAs' waits too.  The pending unitaries of the last round are applied
+// in place by pair_apply32_kernel after the last sweep.
+
+constexpr int PS_SLAB = 256;                 // rows per slab
+constexpr int PS_LDS = JC + 2;               // slab row stride in float2 (16-byte aligned rows)
+constexpr int PS_TILES = 10;                 // upper 4x4 tiles of the 16x16 Gram
+constexpr int PS_NGRP = NTG / PS_TILES;      // 51 row groups per tile
+constexpr size_t PS_SMEM = 2 * PS_SLAB * PS_LDS * sizeof(float2);  // double-buffered slab, 73,728 bytes
+constexpr int PS_SPIN = 1 << 23;             // polls of a round wait before it gives up
+static_assert(PS_TILES * PS_NGRP * 16 <= 2 * PS_SLAB * PS_LDS, "Gram partials reuse the slab buffer");
+
+// table q and side (0: first block of the pair, 1: second) of block `blk` in
+// round `round` of the circle tournament over n players
+__device__ inline void pair_of(int round, int blk, int n, int& q, int& side) {
+  if (blk == n - 1) { q = 0; side = 1; return; }
+  const int rr = round % (n - 1);
+  if (blk == rr) { q = 0; side = 0; return; }
+  const int d = (blk - rr + (n - 1)) % (n - 1);
+  int partner;
+  if (d <= n / 2 - 1) { q = d; partner = (rr - q + (n - 1)) % (n - 1); }
+  else { q = n - 1 - d; partner = (rr + q) % (n - 1); }
+  side = blk > partner ? 1 : 0;
+}
+
+__device__ inline int ld_acquire_gpu(const int* p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ inline void st_release_gpu(int* p, int v) {
+  asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+struct sweep_solver {
+  float d[2][JC];
+  float d0[JC];
+  float2 G[2][JC][JC + 1];
+  float2 W[2][JC][JC + 1];
+  unsigned char ptab[JC - 1][JC];  // partner of each index in each inner round
+  int inner_rot;
+};
+
+// The scaled pair solver with one barrier per inner round: thread (x, y) of
+// warps 0-7 computes the rotation of y's pair itself (the two half-warps
+// compute the same 16, bit-identically) and takes x's from lane x by shuffle,
+// then updates Ghat[x][y] and Wt[x][y] into the other buffer.  Same
+// iteration as diagonalise_scaled2.
+__device__ int diagonalise_lanes(sweep_solver& sh, const int* col, float tol_inner, float nu2, int max_inner,
+                                 int* buf_out) {
+  const int t = threadIdx.x, x = (t >> 4) & 15, y = t & 15;
+  const bool owner = t < NGRAM;  // warps 0-7, whole warps
+  int cur = 0, sweep = 0;
+  for (; sweep < max_inner; sweep++) {
+    for (int ir = 0; ir < JC - 1; ir++) {
+      if (owner) {
+        const int yp = sh.ptab[ir][y], xp = sh.ptab[ir][x];
+        const int p = min(y, yp), q = max(y, yp);
+        const float a = sh.d[cur][p], b = sh.d[cur][q];
+        const float2 gs = sh.G[cur][p][q];
+        const float ags = sqrtf(gs.x * gs.x + gs.y * gs.y);
+        float2 jpp = make_float2(1.f, 0.f), jqp = make_float2(0.f, 0.f), jpq = jqp, jqq = jpp;
+        float a2 = a, b2 = b;
+        const bool rotp = col[p] >= 0 && col[q] >= 0 && a > nu2 && b > nu2 && ags > tol_inner;
+        if (rotp) {
+          const float ag = ags * sqrtf(a * b);  // |gamma|
+          const float zeta = __fdividef(b - a, 2.f * ag);
+          const float r1 = sqrtf(fmaf(zeta, zeta, 1.f));
+          const float tt = copysignf(__frcp_rn(fabsf(zeta) + r1), zeta);
+          const float c = rsqrtf(fmaf(tt, tt, 1.f)), sn = c * tt;
+          const float inv = __frcp_rn(ags);
+          const float2 e = make_float2(gs.x * inv, gs.y * inv);
+          a2 = fmaxf(a - tt * ag, nu2);  // a column driven to the noise level is frozen
+          b2 = b + tt * ag;
+          const float ia2 = rsqrtf(a2), ib2 = rsqrtf(b2), sqa = sqrtf(a), sqb = sqrtf(b);
+          jpp = make_float2(c * sqa * ia2, 0.f);
+          jqp = make_float2(-sn * e.x * sqb * ia2, sn * e.y * sqb * ia2);  // -s conj(e) sqrt(b/a')
+          jpq = make_float2(sn * e.x * sqa * ib2, sn * e.y * sqa * ib2);   //  s e sqrt(a/b')
+          jqq = make_float2(c * sqb * ib2, 0.f);
+        }
+        // column y of Jt: rows y and y'
+        const bool low = y == p;
+        const float2 jyy = low ? jpp : jqq, jpy = low ? jqp : jpq;
+        // column x of Jt from lane x (which holds y == x)
+        float2 jxx, jpx;
+        jxx.x = __shfl_sync(0xffffffffu, jyy.x, x);
+        jxx.y = __shfl_sync(0xffffffffu, jyy.y, x);
+        jpx.x = __shfl_sync(0xffffffffu, jpy.x, x);
+        jpx.y = __shfl_sync(0xffffffffu, jpy.y, x);
+        if (x == y) sh.d[cur ^ 1][y] = low ? a2 : b2;
+        if (rotp && x == 0) sh.inner_rot = sweep + 1;
+        float2 gnew = make_float2(0.f, 0.f);
+        if (xp == y && x != y) {
+          const bool rotated = jxx.x != 1.f || jxx.y != 0.f || jpx.x != 0.f || jpx.y != 0.f;
+          if (!rotated) gnew = sh.G[cur][x][y];
+        } else if (x != y) {
+          const float2 g_xy = sh.G[cur][x][y], g_xq = sh.G[cur][x][yp];
+          const float2 g_py = sh.G[cur][xp][y], g_pq = sh.G[cur][xp][yp];
+          const float2 hx = cadd(cmul(g_xy, jyy), cmul(g_xq, jpy));
+          const float2 hp = cadd(cmul(g_py, jyy), cmul(g_pq, jpy));
+          gnew = cadd(cmul(cconj(jxx), hx), cmul(cconj(jpx), hp));
+        }
+        sh.G[cur ^ 1][x][y] = gnew;
+        const float2 w_xy = sh.W[cur][x][y], w_xq = sh.W[cur][x][yp];
+        sh.W[cur ^ 1][x][y] = cadd(cmul(w_xy, jyy), cmul(w_xq, jpy));
+      }
+      cur ^= 1;
+      __syncthreads();
+    }
+    const int again = sh.inner_rot == sweep + 1;  // written before the round's closing barrier
+    __syncthreads();
+    if (!again) break;
+  }
+  if (owner) {
+    const float d0 = sh.d0[x];
+    sh.W[cur][x][y] = d0 > 0.f ? cscale(sh.W[cur][x][y], sqrtf(sh.d[cur][y] / d0))
+                               : make_float2(x == y ? 1.f : 0.f, 0.f);
+  }
+  __syncthreads();
+  *buf_out = cur;
+  return sweep + (sweep < max_inner ? 1 : 0);
+}
+
+// One sweep (rounds g0 .. g0 + nb - 2).  xb[0] is X itself, xb[1] a scratch
+// copy of its shape (likewise vb for V); wbuf holds 2 x pairs unitaries,
+// rotbuf 2 x pairs decisions, done[pairs] the completed round of each CTA.
+__global__ void __launch_bounds__(NTG, 1)
+jacobi_sweep32_kernel(float2* __restrict__ xb0, float2* __restrict__ xb1, int64_t ldx, int mm,
+                      float2* __restrict__ vb0, float2* __restrict__ vb1, int64_t ldv, int nn, int nb, int g0,
+                      int has_prev, double tol, float tol_inner, double nu_rel2, const double* __restrict__ xnorm2,
+                      float2* __restrict__ wbuf, int* __restrict__ rotbuf, int* __restrict__ done,
+                      int* __restrict__ flags, int max_inner, unsigned long long* phase_ns) {
+  extern __shared__ __align__(16) float2 ps_slab[];  // [2][PS_SLAB][PS_LDS]
+  __shared__ __align__(16) float2 wsub[2][JC][JW];    // 16x8 unitary blocks that rebuild the two blocks
+  __shared__ float2 psum[3][PS_TILES * 16];
+  __shared__ float2 gram[NGRAM];
+  __shared__ sweep_solver sh;
+  __shared__ int col[JC], scol[2][JC], srcq[2], sside[2], srot[2];
+  __shared__ int any_rot, bad, offmax_blk, offbig_blk;
+  const int t = threadIdx.x, q = blockIdx.x, pairs = gridDim.x, R = nb - 1;
+  unsigned long long tp = 0;
+  auto phase = [&](int ph) {  // optional diagnostics: time per phase into phase_ns[ph - 1]
+    if (phase_ns && t == 0) {
+      unsigned long long tn;
+      asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(tn));
+      if (ph > 0) atomicAdd(&phase_ns[ph - 1], tn - tp);
+      tp = tn;
+    }
+  };
+  if (t < (JC / 2) * (JC - 1)) {
+    const int ir = t / (JC / 2), tq = t % (JC / 2);
+    int a, b;
+    tournament(ir, tq, JC, a, b);
+    sh.ptab[ir][a] = (unsigned char)b;
+    sh.ptab[ir][b] = (unsigned char)a;
+  }
+  const double nu2d = nu_rel2 * (*xnorm2);
+  const float nu2 = (float)nu2d;
+  const double big2 = 1e-6 * (*xnorm2);
+  // slab rows: thread t rebuilds row (t & 255) of block (t >> 8)
+  const int lr = t & (PS_SLAB - 1), h = t >> 8;
+  // Gram products: 4x4 tile (ti, tj), ti <= tj, row group grp
+  const int tile = t / PS_NGRP, grp = t - PS_NGRP * (t / PS_NGRP);
+  const bool act = tile < PS_TILES;
+  int ti = 0, rem = act ? tile : 0;
+  while (rem >= 4 - ti) { rem -= 4 - ti; ti++; }
+  const int tj = ti + rem;
+  const int nslab = (mm + PS_SLAB - 1) / PS_SLAB;
+  for (int r = 0; r < R; r++) {
+    const int g = g0 + r;
+    const bool prev = r > 0 || has_prev;
+    const int rp = r > 0 ? r - 1 : R - 1;  // round (within its sweep) of g - 1
+    const int rpp = (r + 2 * R - 2) % R;   // ... of g - 2
+    phase(0);
+    int bi, bj;
+    tournament(r, q, nb, bi, bj);
+    // ---- wait for the round g - 1 CTAs this round depends on
+    int gave_up = 0;
+    if (prev && t < 6) {
+      int target = -1, qq, s;
+      if (t < 2) {  // read after write: the pairs that held our blocks in round g - 1
+        pair_of(rp, t == 0 ? bi : bj, nb, qq, s);
+        target = qq;
+      } else if (g >= 2 && t < 4) {  // write after read: readers of our blocks' round g - 2 columns
+        const int blk = t == 2 ? bi : bj;
+        int a2, b2;
+        pair_of(rpp, blk, nb, qq, s);
+        tournament(rpp, qq, nb, a2, b2);
+        pair_of(rp, a2 == blk ? b2 : a2, nb, qq, s);
+        target = qq;
+      } else if (g >= 2) {  // write after read: readers of unitary slot q of round g - 2
+        int a2, b2;
+        tournament(rpp, q, nb, a2, b2);
+        pair_of(rp, t == 4 ? a2 : b2, nb, qq, s);
+        target = qq;
+      }
+      if (target >= 0) {
+        int it = 0;
+        for (; it < PS_SPIN; it++) {
+          if (ld_acquire_gpu(done + target) >= g - 1) break;
+          if (*(volatile int*)(flags + QT_FLAG_ABORT)) { it = PS_SPIN; break; }
+          __nanosleep(64);
+        }
+        if (it >= PS_SPIN) { gave_up = 1; atomicExch(flags + QT_FLAG_ABORT, 1); }
+      }
+    }
+    if (__syncthreads_or(gave_up)) return;
+    phase(1);  // 0: waits
+    pair_columns(r, q, nb, nn, col);
+    if (t == 0) { any_rot = 0; bad = 0; offmax_blk = 0; offbig_blk = 0; sh.inner_rot = 0; }
+    if (prev && t < 2) {
+      int qq, s;
+      pair_of(rp, t == 0 ? bi : bj, nb, qq, s);
+      srcq[t] = qq;
+      sside[t] = s;
+      srot[t] = __ldcg(rotbuf + (size_t)((g - 1) & 1) * pairs + qq);
+    }
+    if (!prev && t < 2) srot[t] = 0;
+    __syncthreads();
+    if (t < 2 * JC) {  // source columns of each half: the round g - 1 pair, or the block itself
+      const int hh = t / JC, c = t % JC;
+      int gc;
+      if (srot[hh]) {
+        int a2, b2;
+        tournament(rp, srcq[hh], nb, a2, b2);
+        gc = c < JW ? a2 * JW + c : b2 * JW + (c - JW);
+      } else {
+        gc = c < JW ? (hh == 0 ? bi : bj) * JW + c : -1;
+      }
+      scol[hh][c] = gc < nn ? gc : -1;
+    }
+    if (t < 2 * JC * JW) {
+      const int hh = t / (JC * JW), k = (t / JW) % JC, c = t % JW;
+      if (srot[hh])
+        wsub[hh][k][c] = __ldcg(wbuf + (size_t)((g - 1) & 1) * pairs * NGRAM + (size_t)srcq[hh] * NGRAM + k * JC +
+                                sside[hh] * JW + c);
+    }
+    __syncthreads();
+    const float2* __restrict__ src = prev ? (((g - 1) & 1) ? xb1 : xb0) : ((g & 1) ? xb1 : xb0);
+    float2* __restrict__ dst = (g & 1) ? xb1 : xb0;
+    const bool hrot = srot[h] != 0;
+    // column indices stay in shared memory (warp-uniform broadcast reads)
+    const int* sc = scol[h];
+    const int* oc = col + h * JW;
+    // ---- rebuild the rows slab by slab; Gram products on the previous slab meanwhile
+    float2 xr[JC];
+    auto load_row = [&](const float2* __restrict__ M, int64_t ld, int lim, int rr) {
+      if (hrot) {
+#pragma unroll
+        for (int k = 0; k < JC; k++)
+          xr[k] = (sc[k] >= 0 && rr < lim) ? __ldcg(M + rr + ld * sc[k]) : make_float2(0.f, 0.f);
+      } else {
+#pragma unroll
+        for (int k = 0; k < JW; k++)
+          xr[k] = (sc[k] >= 0 && rr < lim) ? __ldcg(M + rr + ld * sc[k]) : make_float2(0.f, 0.f);
+      }
+    };
+    auto rebuild = [&](float2* out) {
+      if (hrot) {
+#pragma unroll
+        for (int c = 0; c < JW; c++) out[c] = make_float2(0.f, 0.f);
+        asm volatile("" ::: "memory");  // keep wsub in shared memory
+#pragma unroll
+        for (int k = 0; k < JC; k++) {
+#pragma unroll
+          for (int c = 0; c < JW; c += 2) {
+            const float4 w = *reinterpret_cast<const float4*>(&wsub[h][k][c]);
+            cfma(out[c], xr[k], make_float2(w.x, w.y));
+            cfma(out[c + 1], xr[k], make_float2(w.z, w.w));
+          }
+        }
+      } else {
+#pragma unroll
+        for (int c = 0; c < JW; c++) out[c] = xr[c];
+      }
+    };
+    auto build_slab = [&](int s) {
+      const int rr = s * PS_SLAB + lr;
+      float2 o[JW];
+      rebuild(o);
+      if (prev && rr < mm) {
+#pragma unroll
+        for (int c = 0; c < JW; c++)
+          if (oc[c] >= 0) __stcg(dst + rr + ldx * oc[c], o[c]);
+      }
+      float4* sp = reinterpret_cast<float4*>(ps_slab + ((size_t)(s & 1) * PS_SLAB + lr) * PS_LDS + h * JW);
+#pragma unroll
+      for (int c = 0; c < JW; c += 2) sp[c / 2] = make_float4(o[c].x, o[c].y, o[c + 1].x, o[c + 1].y);
+    };
+    float2 acc[16];
+#pragma unroll
+    for (int e = 0; e < 16; e++) acc[e] = make_float2(0.f, 0.f);
+    load_row(src, ldx, mm, lr);
+    build_slab(0);
+    __syncthreads();
+    for (int s = 0; s < nslab; s++) {
+      if (s + 1 < nslab) load_row(src, ldx, mm, (s + 1) * PS_SLAB + lr);
+      if (act) {
+        const float2* base = ps_slab + (size_t)(s & 1) * PS_SLAB * PS_LDS;
+        const int rows = min(PS_SLAB, mm - s * PS_SLAB);
+#pragma unroll 1
+        for (int rr = grp; rr < rows; rr += PS_NGRP) {
+          const float4* rowp = reinterpret_cast<const float4*>(base + (size_t)rr * PS_LDS);
+          const float4 p01 = rowp[2 * ti], p23 = rowp[2 * ti + 1], q01 = rowp[2 * tj], q23 = rowp[2 * tj + 1];
+          const float2 pv[4] = {make_float2(p01.x, p01.y), make_float2(p01.z, p01.w), make_float2(p23.x, p23.y),
+                                make_float2(p23.z, p23.w)};
+          const float2 qv[4] = {make_float2(q01.x, q01.y), make_float2(q01.z, q01.w), make_float2(q23.x, q23.y),
+                                make_float2(q23.z, q23.w)};
+#pragma unroll
+          for (int a = 0; a < 4; a++)
+#pragma unroll
+            for (int b = 0; b < 4; b++) cfma_conj(acc[a * 4 + b], pv[a], qv[b]);
+        }
+      }
+      if (s + 1 < nslab) build_slab(s + 1);
+      __syncthreads();
+    }
+    // ---- V rows (rotation only)
+    if (prev && vb0) {
+      const float2* __restrict__ vsrc = ((g - 1) & 1) ? vb1 : vb0;
+      float2* __restrict__ vdst = (g & 1) ? vb1 : vb0;
+      for (int rr = lr; rr < nn; rr += PS_SLAB) {
+        load_row(vsrc, ldv, nn, rr);
+        float2 o[JW];
+        rebuild(o);
+#pragma unroll
+        for (int c = 0; c < JW; c++)
+          if (oc[c] >= 0) __stcg(vdst + rr + ldv * oc[c], o[c]);
+      }
+    }
+    phase(2);  // 1: rebuild + Gram products
+    // ---- reduce the row groups in a fixed order
+    float2* red = ps_slab;
+    if (act) {
+#pragma unroll
+      for (int e = 0; e < 16; e++) red[(grp * PS_TILES + tile) * 16 + e] = acc[e];
+    }
+    __syncthreads();
+    if (t < 3 * PS_TILES * 16) {
+      const int ent = t / 3, part = t % 3;
+      constexpr int per = (PS_NGRP + 2) / 3;
+      float2 v = make_float2(0.f, 0.f);
+      for (int gg = part * per; gg < min(PS_NGRP, part * per + per); gg++) v = cadd(v, red[gg * PS_TILES * 16 + ent]);
+      psum[part][ent] = v;
+    }
+    __syncthreads();
+    if (t < PS_TILES * 16) {
+      const float2 v = cadd(cadd(psum[0][t], psum[1][t]), psum[2][t]);
+      const int tl = t / 16, e = t % 16;
+      int ai = 0, rm = tl;
+      while (rm >= 4 - ai) { rm -= 4 - ai; ai++; }
+      const int aj = ai + rm;
+      const int rw = 4 * ai + e / 4, cl = 4 * aj + e % 4;
+      if (ai != aj || rw <= cl) {
+        gram[rw * JC + cl] = v;
+        gram[cl * JC + rw] = cconj(v);
+      }
+    }
+    __syncthreads();
+    // ---- scaled Gram, test
+    const bool owner = t < NGRAM;
+    const int i = (t / JC) & 15, j = t % JC;
+    if (owner) {
+      const float2 v = gram[t];
+      if (!isfinite(v.x) || !isfinite(v.y)) bad = 1;
+      if (i == j) { sh.d[0][i] = v.x; sh.d0[i] = v.x; }
+    }
+    __syncthreads();
+    if (owner) {
+      const float di = sh.d[0][i], dj = sh.d[0][j];
+      float2 v = make_float2(0.f, 0.f);
+      if (i != j && di > nu2 && dj > nu2) v = cscale(gram[t], (float)(1.0 / sqrt((double)di * (double)dj)));
+      sh.G[0][i][j] = v;
+      sh.W[0][i][j] = make_float2(i == j ? 1.f : 0.f, 0.f);
+    }
+    __syncthreads();
+    {
+      float relmax = 0.f, relbig = 0.f;
+      if (!bad && owner && i < j && col[i] >= 0 && col[j] >= 0 && sh.d[0][i] > nu2 && sh.d[0][j] > nu2) {
+        const float rel = fminf(sqrtf(cabs2(sh.G[0][i][j])), 1.f);
+        if (rel > tol) {
+          any_rot = 1;
+          relmax = rel;
+          if (sh.d[0][i] > big2 && sh.d[0][j] > big2) relbig = rel;
+        }
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        relmax = fmaxf(relmax, __shfl_xor_sync(0xffffffffu, relmax, o));
+        relbig = fmaxf(relbig, __shfl_xor_sync(0xffffffffu, relbig, o));
+      }
+      if ((t & 31) == 0 && relmax > 0.f) atomicMax(&offmax_blk, __float_as_int(relmax));
+      if ((t & 31) == 0 && relbig > 0.f) atomicMax(&offbig_blk, __float_as_int(relbig));
+    }
+    __syncthreads();
+    if (t == 0) {
+      if (bad) atomicOr(&flags[QT_FLAG_NONFINITE], 1);
+      __stcg(rotbuf + (size_t)(g & 1) * pairs + q, any_rot);
+      if (offmax_blk > 0) atomicMax(&flags[QT_FLAG_OFFMAX], offmax_blk);
+      if (offbig_blk > 0) atomicMax(&flags[QT_FLAG_OFFBIG], offbig_blk);
+      if (any_rot) atomicAdd(&flags[QT_FLAG_ROTATED], 1);
+    }
+    phase(3);  // 2: reduction, scaled Gram, test
+    if (any_rot) {
+      int buf = 0;
+      const int inner = diagonalise_lanes(sh, col, tol_inner, nu2, max_inner, &buf);
+      if (t == 0) atomicAdd(&flags[QT_FLAG_INNER], inner);
+      if (owner) __stcg(wbuf + (size_t)(g & 1) * pairs * NGRAM + (size_t)q * NGRAM + t, sh.W[buf][i][j]);
+    }
+    phase(4);  // 3: pair solver
+    // ---- publish round g
+    __threadfence();
+    __syncthreads();
+    if (t == 0) st_release_gpu(done + q, g);
+  }
+}
+
 // ||X||_F^2 in FP64, one CTA per column, added into *out.
 template <typename TS>
 __global__ void frob_kernel(const TS* __restrict__ X, int64_t ldx, int mm, double* out) {
@@ -1189,6 +1621,51 @@ static int launch_pair_round(qt_handle* h, int csize, int pairs, size_t smem, TS
   return QT_OK;
 }
 
+// Whether one CTA per pair of jacobi_sweep32_kernel can be resident at once
+// (the cooperative launch needs it).
+static bool sweep32_fits(qt_handle* h, int pairs) {
+  static int max_ctas = -1;
+  if (max_ctas < 0) {
+    int dev = 0, coop = 0, sms = 0, per_sm = 0;
+    max_ctas = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess &&
+        cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) == cudaSuccess && coop &&
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess &&
+        cudaFuncSetAttribute(jacobi_sweep32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)PS_SMEM) ==
+            cudaSuccess &&
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, jacobi_sweep32_kernel, NTG, PS_SMEM) == cudaSuccess)
+      max_ctas = per_sm * sms;
+    cudaGetLastError();
+  }
+  (void)h;
+  return pairs <= max_ctas;
+}
+
+static int launch_sweep32(qt_handle* h, int pairs, float2* x0, float2* x1, int64_t ldx, int mm, float2* v0,
+                          float2* v1, int64_t ldv, int nn, int nb, int g0, int has_prev, double tol, float tol_inner,
+                          double nu_rel2, const double* xnorm2, float2* wbuf, int* rotbuf, int* done, int max_inner,
+                          unsigned long long* phase_ns) {
+  cudaLaunchConfig_t lc = {};
+  lc.gridDim = dim3((unsigned)pairs);
+  lc.blockDim = dim3(NTG);
+  lc.dynamicSmemBytes = PS_SMEM;
+  lc.stream = h->stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  lc.attrs = attr;
+  lc.numAttrs = 1;
+  if (h->prof) qt_prof_before(h, "jacobi_sweep32_kernel");
+  const cudaError_t e = cudaLaunchKernelEx(&lc, jacobi_sweep32_kernel, x0, x1, ldx, mm, v0, v1, ldv, nn, nb, g0,
+                                           has_prev, tol, tol_inner, nu_rel2, xnorm2, wbuf, rotbuf, done, h->d_flags,
+                                           max_inner, phase_ns);
+  if (h->prof) qt_prof_after(h);
+  h->launches++;
+  if (e != cudaSuccess)
+    return qt_fail(h, QT_ECUDA, std::string("launch jacobi_sweep32_kernel: ") + cudaGetErrorString(e));
+  return QT_OK;
+}
+
 template <typename TS>
 int qt_jacobi_svd_ws(qt_handle* h, TS* X, int64_t mm, int64_t nn, int64_t ldx, TS* V, int64_t ldv, double tol,
                      int max_sweeps, int* sweeps_out, double2* parts, double nu_rel_in) {
@@ -1231,10 +1708,11 @@ int qt_jacobi_svd_ws(qt_handle* h, TS* X, int64_t mm, int64_t nn, int64_t ldx, T
   // storage uses the one-launch round where a pair's rows fit a cluster's
   // shared memory.
   const int jk = h->cfg.jacobi_kernel;
-  const bool two_launch = fp32 && jk == 0;
+  const bool sweep_kernel = fp32 && jk == 0 && sweep32_fits(h, pairs);
+  const bool two_launch = fp32 && (jk == 3 || (jk == 0 && !sweep_kernel));
   int xrows_c = 0, lds = 0;
   size_t smem = 0;
-  const int csize = (jk == 1 || two_launch) ? 0 : fused_shape(mm, pairs, sizeof(TS), &xrows_c, &lds, &smem);
+  const int csize = (jk == 1 || two_launch || sweep_kernel) ? 0 : fused_shape(mm, pairs, sizeof(TS), &xrows_c, &lds, &smem);
   // two-launch shape: one row per rotation thread, about eight CTAs per SM
   int achunks = std::max(1, std::min<int>((8 * 152 + pairs - 1) / pairs, (int)((mm + NT - 1) / NT)));
   const int axrows = (int)(((mm + achunks - 1) / achunks + 31) / 32 * 32);
@@ -1253,9 +1731,21 @@ int qt_jacobi_svd_ws(qt_handle* h, TS* X, int64_t mm, int64_t nn, int64_t ldx, T
   static const bool phases = std::getenv("QT_JACOBI_PHASES") != nullptr;
   unsigned long long* phase_ns = nullptr;
   qt_scratch pscratch(h);
-  if (phases && (csize || two_launch)) {
+  if (phases && (csize || two_launch || sweep_kernel)) {
     QT_TRY(pscratch.get(&phase_ns, 16));
     QT_CHECK_CUDA(h, cudaMemsetAsync(phase_ns, 0, 16 * sizeof(unsigned long long), h->stream));
+  }
+  // sweep kernel: ping-pong copies of X and V, the round counter, and
+  // whether the last round's unitaries are still to be applied
+  TS* X1 = nullptr;
+  TS* V1 = nullptr;
+  int* done = reinterpret_cast<int*>(parts);
+  int gcount = 0;
+  bool pending = false;
+  if (sweep_kernel) {
+    QT_TRY(pscratch.get(&X1, (size_t)ldx * nn));
+    if (V) QT_TRY(pscratch.get(&V1, (size_t)ldv * nn));
+    QT_CHECK_CUDA(h, cudaMemsetAsync(done, 0xff, sizeof(int) * pairs, h->stream));
   }
   int sweep = 0;
   for (; sweep < max_sweeps; sweep++) {
@@ -1265,7 +1755,16 @@ int qt_jacobi_svd_ws(qt_handle* h, TS* X, int64_t mm, int64_t nn, int64_t ldx, T
     static const int inner_cap = std::getenv("QT_JACOBI_INNER") ? std::atoi(std::getenv("QT_JACOBI_INNER")) : 1;
     const int max_inner = sweep < 2 ? MAX_INNER : std::max(1, std::min(inner_cap, MAX_INNER));
     QT_CHECK_CUDA(h, cudaMemsetAsync(h->d_flags, 0, sizeof(int) * QT_FLAG_COUNT, h->stream));
-    for (int r = 0; r < rounds; r++) {
+    if (sweep_kernel) {
+      if constexpr (sizeof(typename real_of<TS>::type) == 4) {
+        QT_TRY(launch_sweep32(h, pairs, (float2*)X, (float2*)X1, ldx, (int)mm, (float2*)V, (float2*)V1, ldv, (int)nn,
+                              nb, gcount, pending ? 1 : 0, tol, (float)tol_inner, nu_rel2, (const double*)xnorm2,
+                              (float2*)wbuf, rotf, done, max_inner, phase_ns));
+      }
+      gcount += rounds;
+      pending = true;
+    }
+    for (int r = 0; r < rounds && !sweep_kernel; r++) {
       if (two_launch) {
         if constexpr (sizeof(typename real_of<TS>::type) == 4) {
           QT_LAUNCH(h, pair_eig32_kernel, pairs, NTG, 0, (const float2*)X, ldx, (int)mm, (int)nn, nb, r, tol,
@@ -1297,6 +1796,8 @@ int qt_jacobi_svd_ws(qt_handle* h, TS* X, int64_t mm, int64_t nn, int64_t ldx, T
       h->work_jacobi_inner += h->h_flags[QT_FLAG_INNER];
       h->work_jacobi_bytes += (double)rounds * (double)mm * (double)nn * es +
                               (double)h->h_flags[QT_FLAG_ROTATED] * JC * es * ((double)mm + (V ? 2.0 * (double)nn : 0.0));
+      h->work_jacobi_gram_bytes += (double)rounds * (double)mm * (double)nn * es;
+      h->work_jacobi_rot_bytes += (double)h->h_flags[QT_FLAG_ROTATED] * JC * es * ((double)mm + (V ? (double)nn : 0.0));
     }
     if (trace) {
       float off;
@@ -1309,11 +1810,36 @@ int qt_jacobi_svd_ws(qt_handle* h, TS* X, int64_t mm, int64_t nn, int64_t ldx, T
                    (long long)mm, (long long)nn, sweep, h->h_flags[QT_FLAG_ROTATED], h->h_flags[QT_FLAG_INNER], off,
                    offbig);
     }
+    if (h->h_flags[QT_FLAG_ABORT]) return qt_fail(h, QT_ETIMEOUT, "jacobi: a round of the sweep kernel gave up waiting");
     if (h->h_flags[QT_FLAG_NONFINITE]) return qt_fail(h, QT_ENUMERIC, "jacobi: non-finite value in the matrix");
     if (h->h_flags[QT_FLAG_ROTATED] == 0) break;
   }
   *sweeps_out = sweep + (sweep < max_sweeps ? 1 : 0);
-  if (phase_ns && two_launch) {
+  if (sweep_kernel && pending) {
+    // the last round's unitaries, in place, then the data back into X and V
+    if constexpr (sizeof(typename real_of<TS>::type) == 4) {
+      const int b = (gcount - 1) & 1;
+      float2* xf = (float2*)(b ? X1 : X);
+      float2* vf = V ? (float2*)(b ? V1 : V) : nullptr;
+      QT_LAUNCH(h, pair_apply32_kernel, dim3(pairs, achunks), NT, 0, xf, ldx, (int)mm, vf, ldv, (int)nn, nb,
+                rounds - 1, axrows, avrows, (const float2*)wbuf + (size_t)b * pairs * NGRAM, (const int*)rotf + b * pairs);
+      if (b) {
+        QT_CHECK_CUDA(h, cudaMemcpy2DAsync(X, ldx * sizeof(TS), X1, ldx * sizeof(TS), mm * sizeof(TS), nn,
+                                           cudaMemcpyDeviceToDevice, h->stream));
+        if (V)
+          QT_CHECK_CUDA(h, cudaMemcpy2DAsync(V, ldv * sizeof(TS), V1, ldv * sizeof(TS), nn * sizeof(TS), nn,
+                                             cudaMemcpyDeviceToDevice, h->stream));
+      }
+    }
+  }
+  if (phase_ns && sweep_kernel) {
+    unsigned long long hp[4];
+    QT_CHECK_CUDA(h, cudaMemcpy(hp, phase_ns, sizeof(hp), cudaMemcpyDeviceToHost));
+    const double ctas = (double)gcount * pairs;
+    std::fprintf(stderr, "jacobi sweep kernel, us per CTA per round: waits %.2f, rebuild+products %.2f, "
+                 "reduction+test %.2f, solver %.2f\n", hp[0] / ctas * 1e-3, hp[1] / ctas * 1e-3, hp[2] / ctas * 1e-3,
+                 hp[3] / ctas * 1e-3);
+  } else if (phase_ns && two_launch) {
     unsigned long long hp[3];
     QT_CHECK_CUDA(h, cudaMemcpy(hp, phase_ns, sizeof(hp), cudaMemcpyDeviceToHost));
     const double launches = (double)(*sweeps_out) * rounds * pairs;

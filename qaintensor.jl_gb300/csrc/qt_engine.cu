@@ -57,6 +57,8 @@ extern "C" int qt_work_counters(const qt_handle* h, double* out) {
   out[3] = h->work_tc_launches;
   out[4] = h->work_jacobi_pairs;
   out[5] = h->work_jacobi_inner;
+  out[6] = h->work_jacobi_gram_bytes;
+  out[7] = h->work_jacobi_rot_bytes;
   return QT_OK;
 }
 

@@ -40,6 +40,7 @@ struct qt_handle {
   // flops (24 M N K per complex product) and launches
   double work_jacobi_bytes = 0, work_jacobi_rounds = 0, work_tc_flops = 0, work_tc_launches = 0;
   double work_jacobi_pairs = 0, work_jacobi_inner = 0;  // rotated pairs, pair-solver inner sweeps
+  double work_jacobi_gram_bytes = 0, work_jacobi_rot_bytes = 0;  // X read by the Gram products; X, V rewritten
   bool prof = false;
   std::vector<qt_profile_rec> prof_recs;
   std::vector<cudaEvent_t> event_pool;
@@ -58,6 +59,7 @@ enum {
   QT_FLAG_OFFMAX = 3,    // Jacobi: largest relative off-diagonal above tol this sweep (float bits)
   QT_FLAG_INNER = 4,     // Jacobi: inner sweeps of the pair solvers this sweep
   QT_FLAG_OFFBIG = 5,    // Jacobi: OFFMAX over pairs of columns above 1e-3 ||X||_F (float bits)
+  QT_FLAG_ABORT = 6,     // Jacobi sweep kernel: a bounded round wait gave up
   QT_FLAG_COUNT = 8
 };
 

@@ -1,6 +1,8 @@
-"""One-sided block Jacobi SVD: the one-launch cluster round (pair rows held in
-the shared memory of 1, 2, 4 or 8 CTAs) and the three-kernel round, in FP64
-and FP32 storage, against LAPACK on graded spectra."""
+"""One-sided block Jacobi SVD against LAPACK on graded spectra, in FP64 and
+FP32 storage, for every round implementation: the one-launch cluster round
+(pair rows held in the shared memory of 1, 2, 4 or 8 CTAs), the three-kernel
+round, and for FP32 the cooperative sweep kernel (jacobi_kernel 0, one launch
+per sweep) and the two-launch round (3)."""
 
 import numpy as np
 import pytest
@@ -44,7 +46,7 @@ def test_fp64_jacobi_matches_lapack(engine, shape, kernel):
     eng.close()
 
 
-@pytest.mark.parametrize("kernel", [0, 1, 2])
+@pytest.mark.parametrize("kernel", [0, 1, 2, 3])
 @pytest.mark.parametrize("shape", SHAPES)
 def test_fp32_jacobi_matches_lapack(engine, shape, kernel):
     rng = np.random.default_rng(7 * sum(shape) + kernel)
@@ -118,3 +120,28 @@ def test_fp32_split_of_rank_deficient_theta(engine, chi):
     assert np.abs(U.conj().T @ U - np.eye(k)).max() <= 1e-4
     assert np.abs(S[:k] - ref[:k]).max() <= 1e-4 * ref[0]
     eng.close()
+
+
+@pytest.mark.parametrize("shape", [(1100, 1003), (333, 517)])
+def test_sweep_kernel_equals_two_launch_round_fp32(engine, shape):
+    """The cooperative sweep kernel (rotation folded into the next round's
+    Gram, ping-pong buffers, per-pair round flags) and the two-launch round
+    reach the same truncation: same rank, values within the FP32 floor."""
+    rng = np.random.default_rng(sum(shape))
+    m, n = shape
+    M, _ = graded(rng, m, n, 0.97)
+    M32 = M.astype(np.complex64)
+    floor = 4 * np.sqrt(max(m, n)) * 5.96e-8 * np.linalg.norm(M32)
+    out = []
+    for kernel in (0, 3):
+        eng = engine.Engine(mode="chosen", jacobi_kernel=kernel)
+        out.append(eng.truncated_svd(M32, 50 * floor, mode="chosen"))
+        eng.close()
+    (U0, S0, V0, k0, _), (U1, S1, V1, k1, _) = out
+    assert abs(k0 - k1) <= 1
+    k = min(k0, k1)
+    assert np.abs(S0[:k] - S1[:k]).max() <= 2 * floor
+    ref = np.linalg.svd(M32.astype(np.complex128), compute_uv=False)
+    for U, S, Vh, kk in ((U0, S0, V0, k0), (U1, S1, V1, k1)):
+        err = np.linalg.norm((U * S) @ Vh - M32)
+        assert err <= 1.1 * np.sqrt(np.sum(ref[kk:] ** 2)) + floor, (err, floor)
