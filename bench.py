@@ -379,7 +379,22 @@ def load_peaks():
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
 
 
-def roofline(prof, work, n_prof):
+def profiled_traffic(kernel):
+    """DRAM bytes per launch of `kernel` from its committed ncu summary
+    (profiles/<kernel>_chi1024.md, line `traffic_per_launch_bytes: N`), or None."""
+    base = kernel.split("<")[0].split("(")[-1].strip()
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "profiles", f"{base}_chi1024.md")
+    try:
+        with open(path) as f:
+            for line in f:
+                if line.startswith("traffic_per_launch_bytes:"):
+                    return float(line.split(":", 1)[1])
+    except OSError:
+        pass
+    return None
+
+
+def roofline(prof, work, n_prof, sm_mhz=2070.0):
     """Roofline of the dominant kernel (largest total device time in the
     profiled updates), from the engine's algorithmic work counters:
       Jacobi round kernels: HBM-class bound.  Algorithmic bytes of a round are
@@ -387,8 +402,8 @@ def roofline(prof, work, n_prof):
         pairs' columns written once (and their V rows read and written).  Per
         kernel: the Gram + pair-solver kernel (pair_eig32_kernel) is charged
         the reads, the rotation kernel (pair_apply32_kernel) reads and writes
-        the rotated columns, a one-launch round (pair_round_kernel,
-        jacobi_round32_kernel) is charged the whole round;
+        the rotated columns, a one-launch round (pair_round_kernel) or sweep
+        (jacobi_sweep32_kernel) is charged all its rounds;
       tc_gemm_kernel: tensor bound; 24 M N K TF32 flops per complex product,
         peak = half the measured dense bf16 rate (TF32 runs at half the bf16
         tensor rate)."""
@@ -397,21 +412,37 @@ def roofline(prof, work, n_prof):
     peaks, src = load_peaks()
     name, launches, ms = prof[0]
     per_launch_s = ms / 1e3 / launches
-    jacobi = {"pair_round_kernel": work["jacobi_bytes"], "jacobi_round32_kernel": work["jacobi_bytes"],
+    jacobi = {"pair_round_kernel": work["jacobi_bytes"], "jacobi_sweep32_kernel": work["jacobi_bytes"],
               "(gram_kernel": work["jacobi_gram_bytes"], "pair_eig32_kernel": work["jacobi_gram_bytes"],
               "apply_kernel": 2.0 * work["jacobi_rot_bytes"], "pair_apply32_kernel": 2.0 * work["jacobi_rot_bytes"]}
     for prefix, nbytes in jacobi.items():
         if not name.startswith(prefix):
             continue
-        n_launch = work["jacobi_rounds"]
-        if n_launch <= 0:
+        if work["jacobi_rounds"] <= 0:
             return {"kernel": name, "note": "no Jacobi work recorded"}
-        bytes_per_launch = nbytes / n_launch
+        # work counters are per update; the profile covers n_prof updates
+        bytes_per_launch = nbytes * n_prof / launches
         achieved = bytes_per_launch / per_launch_s / 1e9
         peak = peaks["hbm_gbs"]
-        return {"kernel": name, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "traffic": None, "bytes_per_launch": bytes_per_launch,
-                "peak_source": f"{src} hbm_gbs", "note": "X and V of the round are L2-resident (<= 67 MB at 2048^2)"}
+        out = {"kernel": name, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+               "frac": achieved / peak, "traffic": profiled_traffic(name), "bytes_per_launch": bytes_per_launch,
+               "peak_source": f"{src} hbm_gbs",
+               "note": "X and V of the round are L2-resident (<= 67 MB at 2048^2); traffic = DRAM bytes per launch "
+                       "of the committed ncu capture (cold L2)"}
+        # the FP32 pipe: the rebuild/rotation costs 1024 FMA per row per
+        # rotated pair (rot_bytes / 128 rows of 16 columns), the Gram 544 per
+        # row per pair (gram_bytes / 128); peak = 152 SMs x 128 FMA/clock at
+        # the SM clock sampled during the run
+        fma = 8.0 * work["jacobi_rot_bytes"] + 4.25 * work["jacobi_gram_bytes"]
+        if name.startswith("pair_eig32_kernel") or name.startswith("(gram_kernel"):
+            fma = 4.25 * work["jacobi_gram_bytes"]
+        elif name.startswith("pair_apply32_kernel") or name.startswith("apply_kernel"):
+            fma = 8.0 * work["jacobi_rot_bytes"]
+        tflops = 2.0 * fma * n_prof / (ms / 1e3) / 1e12
+        out["fp32_pipe"] = {"achieved_tflops": tflops, "sm_mhz": sm_mhz,
+                            "peak_tflops": 2.0 * 152 * 128 * sm_mhz * 1e6 / 1e12,
+                            "frac": tflops / (2.0 * 152 * 128 * sm_mhz * 1e6 / 1e12)}
+        return out
     if name.startswith("tc_gemm_kernel"):
         n_launch = work["tc_launches"]
         flops_per_launch = work["tc_flops"] / max(n_launch, 1)
@@ -481,7 +512,8 @@ def main():
             "accuracy": res.get("accuracy"),
             "kernels": [{"name": n, "launches": c, "ms": round(t, 3)} for n, c, t in prof[:8]],
         }
-        line["roofline"] = roofline(prof, res["work"], res["n_prof"])
+        line["roofline"] = roofline(prof, res["work"], res["n_prof"],
+                                    (res["clocks"] or {}).get("sm_mhz") or 2070.0)
         if "plain" in res:
             line["plain_fp64_gpu"] = res["plain"]
             line["cusolver_fp64_gpu"] = res["cusolver"]

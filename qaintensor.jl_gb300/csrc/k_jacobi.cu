@@ -6,26 +6,29 @@
 // the input equals U diag(s) V^H.
 //
 // Columns are split into blocks of JW = 8.  One sweep is a round-robin
-// tournament over the blocks; a round processes every block pair (16
-// columns) at once in three kernels:
-//   gram   -- grid (pair, row chunk): the 16x16 Gram of the pair over one row
-//             chunk, written as a partial (no atomics: the reduction below
-//             runs in a fixed order, so results are reproducible);
-//   eig    -- grid (pair): sums the partials, tests the pair against `tol`
-//             (relative), and diagonalises the Gram with a cyclic two-sided
-//             Jacobi in FP64 whose 2x2 rotations use the relative-accuracy
-//             formula (tan from zeta = (beta-alpha)/(2|gamma|), the smaller
-//             root); the 16x16 unitary goes to global memory;
-//   apply  -- grid (pair, row chunk): applies that unitary to its row chunk
-//             of X and of V.
-// A sweep in which no pair rotates ends the iteration.
-//
-// Storage / Gram accumulation: double2 / FP64 for the exact path; float2 /
-// FP32 for the FP32-storage path (whose achievable orthogonality is FP32
-// anyway); the 16x16 eigen-solve and the rotation angles are FP64 in both.
+// tournament over the blocks (circle method); a round processes every block
+// pair (16 columns) at once: the pair's 16x16 Gram is formed, tested against
+// `tol` (relative off-diagonals), diagonalised by a cyclic two-sided Jacobi
+// (the pair solver) and the resulting unitary applied to the pair's columns
+// of X (and rows of V).  A sweep in which no pair rotates ends the iteration.
+// Round implementations:
+//   FP32 storage, default: jacobi_sweep32_kernel -- one cooperative launch
+//     per sweep, each round rebuilding its columns from the previous round's
+//     unitaries (see the comment above that kernel);
+//   FP32 storage, two launches per round: pair_eig32_kernel (Gram + test +
+//     pair solver) and pair_apply32_kernel (rotation);
+//   FP64 storage, default: pair_round_kernel -- one launch per round, a
+//     thread-block cluster holding the pair's rows in shared memory;
+//   any storage: gram_kernel + eig_kernel + apply_kernel (partial Grams
+//     over row chunks, FP64 pair solver, rotation).
+// The FP64-storage solvers work on the FP64 Gram; the FP32-storage solvers
+// on the scaled FP32 Gram (cosines), see pair_eig_scaled below.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
+#include <functional>
+#include <vector>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -268,95 +271,6 @@ struct pair_eig_scaled {
   float2 kqp[JC / 2], kpq[JC / 2];
   int inner_rot;
 };
-
-__device__ int diagonalise_scaled(pair_eig_scaled& sh, const int* col, float tol_inner, float nu2, int max_inner) {
-  const int t = threadIdx.x;
-  int sweep = 0;
-  for (; sweep < max_inner; sweep++) {
-    __syncthreads();  // every thread has read inner_rot of the previous sweep
-    if (t == 0) sh.inner_rot = 0;
-    __syncthreads();
-    for (int ir = 0; ir < JC - 1; ir++) {
-      if (t < JC / 2) {
-        int p, q;
-        tournament(ir, t, JC, p, q);
-        sh.rp[t] = p; sh.rq[t] = q; sh.ron[t] = 0;
-        const float a = sh.d[p], b = sh.d[q];
-        const float2 gs = sh.G[p][q];
-        const float ags = sqrtf(gs.x * gs.x + gs.y * gs.y);
-        if (col[p] >= 0 && col[q] >= 0 && a > nu2 && b > nu2 && ags > tol_inner) {
-          // rotation parameters with the fast reciprocal and reciprocal
-          // square root (a few ulp: the rotation only has to be unitary to
-          // FP32 level, and c, s below are consistent with each other)
-          const float ag = ags * sqrtf(a * b);  // |gamma|
-          const float zeta = __fdividef(b - a, 2.f * ag);
-          const float r1 = sqrtf(fmaf(zeta, zeta, 1.f));
-          const float tt = copysignf(__frcp_rn(fabsf(zeta) + r1), zeta);
-          const float c = rsqrtf(fmaf(tt, tt, 1.f)), sn = c * tt;
-          const float inv = __frcp_rn(ags);
-          const float2 e = make_float2(gs.x * inv, gs.y * inv);
-          // a column driven to the noise level is frozen at d = nu2
-          const float a2 = fmaxf(a - tt * ag, nu2), b2 = b + tt * ag;
-          const float ia2 = rsqrtf(a2), ib2 = rsqrtf(b2), sqa = sqrtf(a), sqb = sqrtf(b);
-          const float ra = sqa * ia2, rb = sqb * ia2;
-          const float sa = sqa * ib2, sb = sqb * ib2;
-          sh.ron[t] = 1; sh.na[t] = a2; sh.nb[t] = b2;
-          sh.kpp[t] = c * ra;
-          sh.kqp[t] = make_float2(-sn * e.x * rb, sn * e.y * rb);  // -s conj(e) sqrt(b/a')
-          sh.kpq[t] = make_float2(sn * e.x * sa, sn * e.y * sa);   //  s e sqrt(a/b')
-          sh.kqq[t] = c * sb;
-          sh.inner_rot = 1;
-        }
-      }
-      __syncthreads();
-      // columns p, q of Ghat (rows outside the pair) and of Wt (all rows): Jt from the right
-      {
-        const int task = t & 127, k = task >> 4, r = task & 15;
-        if (sh.ron[k]) {
-          const int p = sh.rp[k], q = sh.rq[k];
-          float2 (*M)[JC + 1] = (t < 128) ? sh.G : sh.W;
-          if (t >= 128 || (r != p && r != q)) {
-            const float2 xp = M[r][p], xq = M[r][q];
-            M[r][p] = cadd(cscale(xp, sh.kpp[k]), cmul(sh.kqp[k], xq));
-            M[r][q] = cadd(cmul(sh.kpq[k], xp), cscale(xq, sh.kqq[k]));
-          }
-        }
-      }
-      __syncthreads();
-      // rows p, q of Ghat (columns outside the pair): Jt^H from the left; the
-      // 2x2 block of each pair and the new diagonal (disjoint entries)
-      if (t < 128) {
-        const int k = t >> 4, r = t & 15;
-        if (sh.ron[k]) {
-          const int p = sh.rp[k], q = sh.rq[k];
-          if (r != p && r != q) {
-            const float2 gp = sh.G[p][r], gq = sh.G[q][r];
-            sh.G[p][r] = cadd(cscale(gp, sh.kpp[k]), cmul(cconj(sh.kqp[k]), gq));
-            sh.G[q][r] = cadd(cmul(cconj(sh.kpq[k]), gp), cscale(gq, sh.kqq[k]));
-          } else if (r == p) {
-            sh.G[p][q] = make_float2(0.f, 0.f);
-            sh.G[q][p] = make_float2(0.f, 0.f);
-            sh.d[p] = sh.na[k];
-            sh.d[q] = sh.nb[k];
-          }
-        }
-      }
-      __syncthreads();
-    }
-    const int again = sh.inner_rot;  // read after the round's closing barrier
-    if (!again) break;
-  }
-  __syncthreads();
-  // W = D0^{-1/2} Wt D^{1/2}
-  {
-    const int i = t >> 4, j = t & 15;
-    const float d0 = sh.d0[i];
-    const float f = d0 > 0.f ? sqrtf(sh.d[j] / d0) : (i == j ? 1.f : 0.f);
-    sh.W[i][j] = d0 > 0.f ? cscale(sh.W[i][j], f) : make_float2(f, 0.f);
-  }
-  __syncthreads();
-  return sweep + (sweep < max_inner ? 1 : 0);
-}
 
 // The scaled iteration with one update phase per round: the 16 indices form
 // 8 disjoint pairs, so every entry of Jt^H Ghat Jt is a 2x2 combination of
@@ -1158,46 +1072,61 @@ struct sweep_solver {
   float d0[JC];
   float2 G[2][JC][JC + 1];
   float2 W[2][JC][JC + 1];
-  unsigned char ptab[JC - 1][JC];  // partner of each index in each inner round
   int inner_rot;
 };
+
+// partner of index y in inner round ir of the circle tournament over the 16
+// columns of a pair (the pairing of tournament(ir, ., 16)): 15 meets ir, the
+// others meet 2 ir - y (mod 15)
+__device__ inline int inner_partner(int ir, int y) {
+  if (y == JC - 1) return ir;
+  if (y == ir) return JC - 1;
+  return (2 * ir - y + (JC - 1)) % (JC - 1);
+}
 
 // The scaled pair solver with one barrier per inner round: thread (x, y) of
 // warps 0-7 computes the rotation of y's pair itself (the two half-warps
 // compute the same 16, bit-identically) and takes x's from lane x by shuffle,
 // then updates Ghat[x][y] and Wt[x][y] into the other buffer.  Same
-// iteration as diagonalise_scaled2.
+// iteration as diagonalise_scaled2; the rotation is evaluated with the
+// special-function unit's square roots and reciprocals (a few ulps: the
+// rotation stays unitary to FP32 rounding, and the one-sided iteration
+// re-measures every pair from the data in the next round anyway).
 __device__ int diagonalise_lanes(sweep_solver& sh, const int* col, float tol_inner, float nu2, int max_inner,
                                  int* buf_out) {
   const int t = threadIdx.x, x = (t >> 4) & 15, y = t & 15;
   const bool owner = t < NGRAM;  // warps 0-7, whole warps
+  const float tol2 = tol_inner * tol_inner;
   int cur = 0, sweep = 0;
   for (; sweep < max_inner; sweep++) {
     for (int ir = 0; ir < JC - 1; ir++) {
       if (owner) {
-        const int yp = sh.ptab[ir][y], xp = sh.ptab[ir][x];
+        const int yp = inner_partner(ir, y), xp = inner_partner(ir, x);
         const int p = min(y, yp), q = max(y, yp);
         const float a = sh.d[cur][p], b = sh.d[cur][q];
         const float2 gs = sh.G[cur][p][q];
-        const float ags = sqrtf(gs.x * gs.x + gs.y * gs.y);
+        const float ags2 = gs.x * gs.x + gs.y * gs.y;
         float2 jpp = make_float2(1.f, 0.f), jqp = make_float2(0.f, 0.f), jpq = jqp, jqq = jpp;
         float a2 = a, b2 = b;
-        const bool rotp = col[p] >= 0 && col[q] >= 0 && a > nu2 && b > nu2 && ags > tol_inner;
+        const bool rotp = col[p] >= 0 && col[q] >= 0 && a > nu2 && b > nu2 && ags2 > tol2;
         if (rotp) {
-          const float ag = ags * sqrtf(a * b);  // |gamma|
+          const float ria = rsqrtf(a), rib = rsqrtf(b), rags = rsqrtf(ags2);
+          const float sqa = a * ria, sqb = b * rib;
+          const float ag = ags2 * rags * sqa * sqb;  // |gamma|
           const float zeta = __fdividef(b - a, 2.f * ag);
-          const float r1 = sqrtf(fmaf(zeta, zeta, 1.f));
-          const float tt = copysignf(__frcp_rn(fabsf(zeta) + r1), zeta);
+          const float z2 = fmaf(zeta, zeta, 1.f);
+          const float r1 = z2 * rsqrtf(z2);
+          const float tt = copysignf(__fdividef(1.f, fabsf(zeta) + r1), zeta);
           const float c = rsqrtf(fmaf(tt, tt, 1.f)), sn = c * tt;
-          const float inv = __frcp_rn(ags);
-          const float2 e = make_float2(gs.x * inv, gs.y * inv);
-          a2 = fmaxf(a - tt * ag, nu2);  // a column driven to the noise level is frozen
-          b2 = b + tt * ag;
-          const float ia2 = rsqrtf(a2), ib2 = rsqrtf(b2), sqa = sqrtf(a), sqb = sqrtf(b);
-          jpp = make_float2(c * sqa * ia2, 0.f);
-          jqp = make_float2(-sn * e.x * sqb * ia2, sn * e.y * sqb * ia2);  // -s conj(e) sqrt(b/a')
-          jpq = make_float2(sn * e.x * sqa * ib2, sn * e.y * sqa * ib2);   //  s e sqrt(a/b')
-          jqq = make_float2(c * sqb * ib2, 0.f);
+          const float2 e = make_float2(gs.x * rags, gs.y * rags);
+          a2 = fmaxf(fmaf(-tt, ag, a), nu2);  // a column driven to the noise level is frozen
+          b2 = fmaf(tt, ag, b);
+          const float ia2 = rsqrtf(a2), ib2 = rsqrtf(b2);
+          const float fa = sqa * ia2, fb = sqb * ib2, fab = sqb * ia2, fba = sqa * ib2;
+          jpp = make_float2(c * fa, 0.f);
+          jqp = make_float2(-sn * e.x * fab, sn * e.y * fab);  // -s conj(e) sqrt(b/a')
+          jpq = make_float2(sn * e.x * fba, sn * e.y * fba);   //  s e sqrt(a/b')
+          jqq = make_float2(c * fb, 0.f);
         }
         // column y of Jt: rows y and y'
         const bool low = y == p;
@@ -1234,7 +1163,7 @@ __device__ int diagonalise_lanes(sweep_solver& sh, const int* col, float tol_inn
   }
   if (owner) {
     const float d0 = sh.d0[x];
-    sh.W[cur][x][y] = d0 > 0.f ? cscale(sh.W[cur][x][y], sqrtf(sh.d[cur][y] / d0))
+    sh.W[cur][x][y] = d0 > 0.f ? cscale(sh.W[cur][x][y], sqrtf(sh.d[cur][y]) * rsqrtf(d0))
                                : make_float2(x == y ? 1.f : 0.f, 0.f);
   }
   __syncthreads();
@@ -1250,16 +1179,17 @@ jacobi_sweep32_kernel(float2* __restrict__ xb0, float2* __restrict__ xb1, int64_
                       float2* __restrict__ vb0, float2* __restrict__ vb1, int64_t ldv, int nn, int nb, int g0,
                       int has_prev, double tol, float tol_inner, double nu_rel2, const double* __restrict__ xnorm2,
                       float2* __restrict__ wbuf, int* __restrict__ rotbuf, int* __restrict__ done,
-                      int* __restrict__ flags, int max_inner, unsigned long long* phase_ns) {
+                      int* __restrict__ flags, int max_inner, float keep2, float* __restrict__ dnorm,
+                      unsigned long long* phase_ns) {
   extern __shared__ __align__(16) float2 ps_slab[];  // [2][PS_SLAB][PS_LDS]
   __shared__ __align__(16) float2 wsub[2][JC][JW];    // 16x8 unitary blocks that rebuild the two blocks
   __shared__ float2 psum[3][PS_TILES * 16];
   __shared__ float2 gram[NGRAM];
   __shared__ sweep_solver sh;
   __shared__ int col[JC], scol[2][JC], srcq[2], sside[2], srot[2];
-  __shared__ int any_rot, bad, offmax_blk, offbig_blk;
+  __shared__ int any_rot, bad, offmax_blk, offbig_blk, offkept_blk;
   const int t = threadIdx.x, q = blockIdx.x, pairs = gridDim.x, R = nb - 1;
-  unsigned long long tp = 0;
+  __shared__ unsigned long long tp;
   auto phase = [&](int ph) {  // optional diagnostics: time per phase into phase_ns[ph - 1]
     if (phase_ns && t == 0) {
       unsigned long long tn;
@@ -1268,16 +1198,9 @@ jacobi_sweep32_kernel(float2* __restrict__ xb0, float2* __restrict__ xb1, int64_
       tp = tn;
     }
   };
-  if (t < (JC / 2) * (JC - 1)) {
-    const int ir = t / (JC / 2), tq = t % (JC / 2);
-    int a, b;
-    tournament(ir, tq, JC, a, b);
-    sh.ptab[ir][a] = (unsigned char)b;
-    sh.ptab[ir][b] = (unsigned char)a;
-  }
-  const double nu2d = nu_rel2 * (*xnorm2);
-  const float nu2 = (float)nu2d;
-  const double big2 = 1e-6 * (*xnorm2);
+  const float nu2 = (float)(nu_rel2 * (*xnorm2));
+  const float big2 = (float)(1e-6 * (*xnorm2));
+  const float tolf = (float)tol;
   // slab rows: thread t rebuilds row (t & 255) of block (t >> 8)
   const int lr = t & (PS_SLAB - 1), h = t >> 8;
   // Gram products: 4x4 tile (ti, tj), ti <= tj, row group grp
@@ -1328,7 +1251,7 @@ jacobi_sweep32_kernel(float2* __restrict__ xb0, float2* __restrict__ xb1, int64_
     if (__syncthreads_or(gave_up)) return;
     phase(1);  // 0: waits
     pair_columns(r, q, nb, nn, col);
-    if (t == 0) { any_rot = 0; bad = 0; offmax_blk = 0; offbig_blk = 0; sh.inner_rot = 0; }
+    if (t == 0) { any_rot = 0; bad = 0; offmax_blk = 0; offbig_blk = 0; offkept_blk = 0; sh.inner_rot = 0; }
     if (prev && t < 2) {
       int qq, s;
       pair_of(rp, t == 0 ? bi : bj, nb, qq, s);
@@ -1450,18 +1373,21 @@ jacobi_sweep32_kernel(float2* __restrict__ xb0, float2* __restrict__ xb1, int64_
       }
     }
     phase(2);  // 1: rebuild + Gram products
-    // ---- reduce the row groups in a fixed order
+    // ---- reduce the row groups in a fixed order: three partial sums of 17
+    // groups each, then their sum; the diagonal goes to the solver's D
     float2* red = ps_slab;
     if (act) {
 #pragma unroll
       for (int e = 0; e < 16; e++) red[(grp * PS_TILES + tile) * 16 + e] = acc[e];
     }
     __syncthreads();
+    static_assert(PS_NGRP == 3 * 17, "three partial sums of 17 row groups");
     if (t < 3 * PS_TILES * 16) {
       const int ent = t / 3, part = t % 3;
-      constexpr int per = (PS_NGRP + 2) / 3;
-      float2 v = make_float2(0.f, 0.f);
-      for (int gg = part * per; gg < min(PS_NGRP, part * per + per); gg++) v = cadd(v, red[gg * PS_TILES * 16 + ent]);
+      const float2* rp0 = red + (size_t)(part * 17) * PS_TILES * 16 + ent;
+      float2 v = rp0[0];
+#pragma unroll
+      for (int gg = 1; gg < 17; gg++) v = cadd(v, rp0[(size_t)gg * PS_TILES * 16]);
       psum[part][ent] = v;
     }
     __syncthreads();
@@ -1473,44 +1399,47 @@ jacobi_sweep32_kernel(float2* __restrict__ xb0, float2* __restrict__ xb1, int64_
       const int aj = ai + rm;
       const int rw = 4 * ai + e / 4, cl = 4 * aj + e % 4;
       if (ai != aj || rw <= cl) {
+        if (!isfinite(v.x) || !isfinite(v.y)) bad = 1;
         gram[rw * JC + cl] = v;
         gram[cl * JC + rw] = cconj(v);
+        if (rw == cl) {
+          sh.d[0][rw] = v.x;
+          sh.d0[rw] = v.x;
+          // the last round of the sweep reports every column's squared norm
+          if (dnorm && r == R - 1 && col[rw] >= 0) dnorm[col[rw]] = v.x;
+        }
       }
     }
     __syncthreads();
     // ---- scaled Gram, test
     const bool owner = t < NGRAM;
     const int i = (t / JC) & 15, j = t % JC;
-    if (owner) {
-      const float2 v = gram[t];
-      if (!isfinite(v.x) || !isfinite(v.y)) bad = 1;
-      if (i == j) { sh.d[0][i] = v.x; sh.d0[i] = v.x; }
-    }
-    __syncthreads();
-    if (owner) {
-      const float di = sh.d[0][i], dj = sh.d[0][j];
-      float2 v = make_float2(0.f, 0.f);
-      if (i != j && di > nu2 && dj > nu2) v = cscale(gram[t], (float)(1.0 / sqrt((double)di * (double)dj)));
-      sh.G[0][i][j] = v;
-      sh.W[0][i][j] = make_float2(i == j ? 1.f : 0.f, 0.f);
-    }
-    __syncthreads();
     {
-      float relmax = 0.f, relbig = 0.f;
-      if (!bad && owner && i < j && col[i] >= 0 && col[j] >= 0 && sh.d[0][i] > nu2 && sh.d[0][j] > nu2) {
-        const float rel = fminf(sqrtf(cabs2(sh.G[0][i][j])), 1.f);
-        if (rel > tol) {
-          any_rot = 1;
-          relmax = rel;
-          if (sh.d[0][i] > big2 && sh.d[0][j] > big2) relbig = rel;
+      float relmax = 0.f, relbig = 0.f, relkept = 0.f;
+      if (owner) {
+        const float di = sh.d[0][i], dj = sh.d[0][j];
+        const bool live = i != j && di > nu2 && dj > nu2;
+        const float2 v = live ? cscale(gram[t], rsqrtf(di) * rsqrtf(dj)) : make_float2(0.f, 0.f);
+        sh.G[0][i][j] = v;
+        sh.W[0][i][j] = make_float2(i == j ? 1.f : 0.f, 0.f);
+        if (!bad && live && i < j && col[i] >= 0 && col[j] >= 0) {
+          const float rel = fminf(sqrtf(cabs2(v)), 1.f);
+          if (rel > tolf) {
+            any_rot = 1;
+            relmax = rel;
+            if (di > big2 && dj > big2) relbig = rel;
+            if (fmaxf(di, dj) > keep2) relkept = rel;
+          }
         }
       }
       for (int o = 16; o > 0; o >>= 1) {
         relmax = fmaxf(relmax, __shfl_xor_sync(0xffffffffu, relmax, o));
         relbig = fmaxf(relbig, __shfl_xor_sync(0xffffffffu, relbig, o));
+        relkept = fmaxf(relkept, __shfl_xor_sync(0xffffffffu, relkept, o));
       }
       if ((t & 31) == 0 && relmax > 0.f) atomicMax(&offmax_blk, __float_as_int(relmax));
       if ((t & 31) == 0 && relbig > 0.f) atomicMax(&offbig_blk, __float_as_int(relbig));
+      if ((t & 31) == 0 && relkept > 0.f) atomicMax(&offkept_blk, __float_as_int(relkept));
     }
     __syncthreads();
     if (t == 0) {
@@ -1518,6 +1447,7 @@ jacobi_sweep32_kernel(float2* __restrict__ xb0, float2* __restrict__ xb1, int64_
       __stcg(rotbuf + (size_t)(g & 1) * pairs + q, any_rot);
       if (offmax_blk > 0) atomicMax(&flags[QT_FLAG_OFFMAX], offmax_blk);
       if (offbig_blk > 0) atomicMax(&flags[QT_FLAG_OFFBIG], offbig_blk);
+      if (offkept_blk > 0) atomicMax(&flags[QT_FLAG_OFFKEPT], offkept_blk);
       if (any_rot) atomicAdd(&flags[QT_FLAG_ROTATED], 1);
     }
     phase(3);  // 2: reduction, scaled Gram, test
@@ -1644,7 +1574,7 @@ static bool sweep32_fits(qt_handle* h, int pairs) {
 static int launch_sweep32(qt_handle* h, int pairs, float2* x0, float2* x1, int64_t ldx, int mm, float2* v0,
                           float2* v1, int64_t ldv, int nn, int nb, int g0, int has_prev, double tol, float tol_inner,
                           double nu_rel2, const double* xnorm2, float2* wbuf, int* rotbuf, int* done, int max_inner,
-                          unsigned long long* phase_ns) {
+                          float keep2, float* dnorm, unsigned long long* phase_ns) {
   cudaLaunchConfig_t lc = {};
   lc.gridDim = dim3((unsigned)pairs);
   lc.blockDim = dim3(NTG);
@@ -1658,7 +1588,7 @@ static int launch_sweep32(qt_handle* h, int pairs, float2* x0, float2* x1, int64
   if (h->prof) qt_prof_before(h, "jacobi_sweep32_kernel");
   const cudaError_t e = cudaLaunchKernelEx(&lc, jacobi_sweep32_kernel, x0, x1, ldx, mm, v0, v1, ldv, nn, nb, g0,
                                            has_prev, tol, tol_inner, nu_rel2, xnorm2, wbuf, rotbuf, done, h->d_flags,
-                                           max_inner, phase_ns);
+                                           max_inner, keep2, dnorm, phase_ns);
   if (h->prof) qt_prof_after(h);
   h->launches++;
   if (e != cudaSuccess)
@@ -1668,7 +1598,7 @@ static int launch_sweep32(qt_handle* h, int pairs, float2* x0, float2* x1, int64
 
 template <typename TS>
 int qt_jacobi_svd_ws(qt_handle* h, TS* X, int64_t mm, int64_t nn, int64_t ldx, TS* V, int64_t ldv, double tol,
-                     int max_sweeps, int* sweeps_out, double2* parts, double nu_rel_in) {
+                     int max_sweeps, int* sweeps_out, double2* parts, double nu_rel_in, int keep_count) {
   typedef typename gram_of<TS>::type TG;
   if (mm < nn) return qt_fail(h, QT_EINVAL, "jacobi: needs rows >= columns");
   if (V) QT_TRY(qt_set_identity<TS>(h, V, nn, ldv));
@@ -1742,24 +1672,45 @@ int qt_jacobi_svd_ws(qt_handle* h, TS* X, int64_t mm, int64_t nn, int64_t ldx, T
   int* done = reinterpret_cast<int*>(parts);
   int gcount = 0;
   bool pending = false;
+  // kept-set convergence (keep_count > 0, sweep kernel): the last round of
+  // each sweep reports the squared column norms; a column within a factor
+  // keep_margin of the keep_count-th largest norm counts as kept
+  static const double keep_margin =
+      std::getenv("QT_JACOBI_KEEP_MARGIN") ? std::atof(std::getenv("QT_JACOBI_KEEP_MARGIN")) : 0.25;
+  static const bool keep_stop = !std::getenv("QT_JACOBI_KEEP_STOP") || std::atoi(std::getenv("QT_JACOBI_KEEP_STOP"));
+  const bool keep_track = sweep_kernel && keep_count > 0 && keep_count < nn;
+  float* dnorm = nullptr;
+  std::vector<float> hnorm;
+  float keep2 = 0.f;
+  double prev_tail2 = -1.0, prev_change = -1.0;
+  static const double keep_tol =
+      std::getenv("QT_JACOBI_KEEP_TOL") ? std::atof(std::getenv("QT_JACOBI_KEEP_TOL")) : 1e-3;
   if (sweep_kernel) {
     QT_TRY(pscratch.get(&X1, (size_t)ldx * nn));
     if (V) QT_TRY(pscratch.get(&V1, (size_t)ldv * nn));
     QT_CHECK_CUDA(h, cudaMemsetAsync(done, 0xff, sizeof(int) * pairs, h->stream));
+    if (keep_track) {
+      QT_TRY(pscratch.get(&dnorm, (size_t)nn));
+      hnorm.resize(nn);
+    }
   }
   int sweep = 0;
   for (; sweep < max_sweeps; sweep++) {
-    // the pair solver diagonalises fully in the first sweeps; once the
+    // the pair solver runs up to 12 inner sweeps in the first two outer
+    // sweeps (FP32 storage: 2, which measured fastest overall); once the
     // pairs are close to orthogonal one inner sweep of rotations reduces
     // them quadratically and the outer test decides convergence
+    // (QT_JACOBI_INNER0 / QT_JACOBI_INNER override the two caps)
     static const int inner_cap = std::getenv("QT_JACOBI_INNER") ? std::atoi(std::getenv("QT_JACOBI_INNER")) : 1;
-    const int max_inner = sweep < 2 ? MAX_INNER : std::max(1, std::min(inner_cap, MAX_INNER));
+    static const int inner_cap0 =
+        std::getenv("QT_JACOBI_INNER0") ? std::atoi(std::getenv("QT_JACOBI_INNER0")) : (fp32 ? 2 : MAX_INNER);
+    const int max_inner = std::max(1, std::min(sweep < 2 ? inner_cap0 : inner_cap, MAX_INNER));
     QT_CHECK_CUDA(h, cudaMemsetAsync(h->d_flags, 0, sizeof(int) * QT_FLAG_COUNT, h->stream));
     if (sweep_kernel) {
       if constexpr (sizeof(typename real_of<TS>::type) == 4) {
         QT_TRY(launch_sweep32(h, pairs, (float2*)X, (float2*)X1, ldx, (int)mm, (float2*)V, (float2*)V1, ldv, (int)nn,
                               nb, gcount, pending ? 1 : 0, tol, (float)tol_inner, nu_rel2, (const double*)xnorm2,
-                              (float2*)wbuf, rotf, done, max_inner, phase_ns));
+                              (float2*)wbuf, rotf, done, max_inner, keep2, dnorm, phase_ns));
       }
       gcount += rounds;
       pending = true;
@@ -1788,6 +1739,8 @@ int qt_jacobi_svd_ws(qt_handle* h, TS* X, int64_t mm, int64_t nn, int64_t ldx, T
     }
     QT_CHECK_CUDA(h, cudaMemcpyAsync(h->h_flags, h->d_flags, sizeof(int) * QT_FLAG_COUNT, cudaMemcpyDeviceToHost,
                                      h->stream));
+    if (keep_track)
+      QT_CHECK_CUDA(h, cudaMemcpyAsync(hnorm.data(), dnorm, sizeof(float) * nn, cudaMemcpyDeviceToHost, h->stream));
     QT_CHECK_CUDA(h, cudaStreamSynchronize(h->stream));
     {
       const double es = (double)sizeof(TS);
@@ -1799,6 +1752,23 @@ int qt_jacobi_svd_ws(qt_handle* h, TS* X, int64_t mm, int64_t nn, int64_t ldx, T
       h->work_jacobi_gram_bytes += (double)rounds * (double)mm * (double)nn * es;
       h->work_jacobi_rot_bytes += (double)h->h_flags[QT_FLAG_ROTATED] * JC * es * ((double)mm + (V ? (double)nn : 0.0));
     }
+    float offkept = 0.f;
+    std::memcpy(&offkept, &h->h_flags[QT_FLAG_OFFKEPT], sizeof(float));
+    const float keep2_used = keep2;
+    double tail2 = -1.0, tail2_change = -1.0;
+    if (keep_track) {
+      // the weight left outside the keep_count largest columns bounds the
+      // truncation error of the final split from above (those columns span
+      // at least their own weight); its change over the sweep measures how
+      // much the kept set still moves
+      std::vector<float> srt(hnorm);
+      std::nth_element(srt.begin(), srt.begin() + (keep_count - 1), srt.end(), std::greater<float>());
+      keep2 = (float)(keep_margin * keep_margin) * srt[keep_count - 1];
+      tail2 = 0.0;
+      for (int64_t c = keep_count; c < nn; c++) tail2 += (double)srt[c];
+      if (prev_tail2 >= 0.0) tail2_change = prev_tail2 - tail2;
+      prev_tail2 = tail2;
+    }
     if (trace) {
       float off;
       std::memcpy(&off, &h->h_flags[QT_FLAG_OFFMAX], sizeof(float));
@@ -1806,13 +1776,25 @@ int qt_jacobi_svd_ws(qt_handle* h, TS* X, int64_t mm, int64_t nn, int64_t ldx, T
       std::memcpy(&offbig, &h->h_flags[QT_FLAG_OFFBIG], sizeof(float));
       std::fprintf(stderr,
                    "jacobi %lldx%lld sweep %d: rotated pairs %d, inner sweeps %d, max rel off-diagonal %.3e "
-                   "(columns above 1e-3 ||X||: %.3e)\n",
+                   "(columns above 1e-3 ||X||: %.3e; above the keep threshold %.3e: %.3e); tail weight %.6e, "
+                   "change %.3e\n",
                    (long long)mm, (long long)nn, sweep, h->h_flags[QT_FLAG_ROTATED], h->h_flags[QT_FLAG_INNER], off,
-                   offbig);
+                   offbig, std::sqrt((double)keep2_used), offkept, tail2, tail2_change);
     }
     if (h->h_flags[QT_FLAG_ABORT]) return qt_fail(h, QT_ETIMEOUT, "jacobi: a round of the sweep kernel gave up waiting");
     if (h->h_flags[QT_FLAG_NONFINITE]) return qt_fail(h, QT_ENUMERIC, "jacobi: non-finite value in the matrix");
     if (h->h_flags[QT_FLAG_ROTATED] == 0) break;
+    // kept set converged: no pair with a column above the threshold rotated,
+    // or the tail weight moved by at most keep_tol of itself over this sweep
+    // after at most 10 keep_tol over the previous one (the iteration is in
+    // its fast-converging phase, where the remaining sweeps would change the
+    // tail by about as much again: the truncation error is then final to
+    // ~keep_tol / 2 relative)
+    if (keep_track && keep_stop && keep2_used > 0.f && offkept == 0.f) break;
+    if (keep_track && keep_stop && tail2_change >= 0.0 && prev_change >= 0.0 && tail2_change <= keep_tol * tail2 &&
+        prev_change <= 10.0 * keep_tol * tail2)
+      break;
+    prev_change = tail2_change;
   }
   *sweeps_out = sweep + (sweep < max_sweeps ? 1 : 0);
   if (sweep_kernel && pending) {
@@ -1874,21 +1856,21 @@ int qt_jacobi_svd_ws(qt_handle* h, TS* X, int64_t mm, int64_t nn, int64_t ldx, T
   return QT_OK;
 }
 template int qt_jacobi_svd_ws<double2>(qt_handle*, double2*, int64_t, int64_t, int64_t, double2*, int64_t, double,
-                                       int, int*, double2*, double);
+                                       int, int*, double2*, double, int);
 template int qt_jacobi_svd_ws<float2>(qt_handle*, float2*, int64_t, int64_t, int64_t, float2*, int64_t, double, int,
-                                      int*, double2*, double);
+                                      int*, double2*, double, int);
 
 template <typename TS>
 int qt_jacobi_svd(qt_handle* h, TS* X, int64_t mm, int64_t nn, int64_t ldx, TS* V, int64_t ldv, double tol,
-                  int max_sweeps, int* sweeps_out, double nu_rel) {
+                  int max_sweeps, int* sweeps_out, double nu_rel, int keep_count) {
   int nb = 0, chunks = 0;
   const int nparts = qt_jacobi_layout(mm, nn, &nb, &chunks);
   qt_scratch s(h);
   double2* parts;
   QT_TRY(s.get(&parts, (size_t)nparts));
-  return qt_jacobi_svd_ws<TS>(h, X, mm, nn, ldx, V, ldv, tol, max_sweeps, sweeps_out, parts, nu_rel);
+  return qt_jacobi_svd_ws<TS>(h, X, mm, nn, ldx, V, ldv, tol, max_sweeps, sweeps_out, parts, nu_rel, keep_count);
 }
 template int qt_jacobi_svd<double2>(qt_handle*, double2*, int64_t, int64_t, int64_t, double2*, int64_t, double, int,
-                                    int*, double);
+                                    int*, double, int);
 template int qt_jacobi_svd<float2>(qt_handle*, float2*, int64_t, int64_t, int64_t, float2*, int64_t, double, int,
-                                   int*, double);
+                                   int*, double, int);

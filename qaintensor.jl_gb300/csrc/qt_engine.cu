@@ -589,6 +589,28 @@ bool fast_freeze_ok(int64_t m, int64_t n, double eff_cut, double theta_norm) {
   return eff_cut >= 1.2 * (double)std::min(m, n) * 5.96e-8 * theta_norm;
 }
 
+// In-place scaling of n complex values by a power of two (exact).
+template <typename C>
+__global__ void scale_pow2_kernel(C* x, int64_t n, double scale) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    C v = x[i];
+    v.x *= scale;
+    v.y *= scale;
+    x[i] = v;
+  }
+}
+
+// FP32 storage keeps squared column norms and Gram entries in FP32: a matrix
+// far from unit norm (an unnormalised state after repeated operator
+// applications reaches |psi|^2 ~ 1e38, the FP32 limit) is scaled by 2^-e
+// first -- exact -- and the results scaled back.  Returns e (0 when
+// ||M||_F^2 lies within 2^+-64).
+int fp32_scale_exponent(double norm2) {
+  if (!(norm2 > 0) || !std::isfinite(norm2)) return 0;
+  const int e2 = std::ilogb(norm2);
+  return (e2 > 64 || e2 < -64) ? e2 / 2 : 0;
+}
+
 // FP32-storage truncated split of theta (m x n, ld m, not modified): the
 // one-sided block Jacobi runs on theta itself (tall or square) or on
 // theta^H (wide), with no QR preconditioning -- theta' may be numerically
@@ -607,22 +629,35 @@ bool fast_freeze_ok(int64_t m, int64_t n, double eff_cut, double theta_norm) {
 // chi_max cap, or a cutoff well above the noise floor), so the Jacobi may
 // freeze columns below sqrt(rows) u ||theta||_F and skip the sweeps that only
 // rotate rounding noise.
+// `keep_hint` > 0: the rank is pinned at that cap, so the Jacobi may stop once
+// the columns at and above the cut have converged.
 template <typename TO>
 int svd_split_direct32(qt_handle* h, const float2* theta, int64_t m, int64_t n, double cutoff, int chi_max,
-                       TO** Aout, TO** Bout, SvdOut* o, double extra_tail = -1.0, bool fast_freeze = false) {
+                       TO** Aout, TO** Bout, SvdOut* o, double extra_tail = -1.0, bool fast_freeze = false,
+                       int keep_hint = 0) {
   qt_scratch s(h);
   const bool wide = m < n;
   const int64_t rows = wide ? n : m, cols = wide ? m : n;
   float2 *X, *V = nullptr;
+  double* dn;
   QT_TRY(s.get(&X, (size_t)rows * cols));
+  QT_TRY(s.get(&dn, 1));
+  QT_TRY(qt_norm2<float2>(h, theta, m * n, dn));
   if (wide) {
     QT_TRY(qt_adjoint_copy<float2>(h, theta, m, n, m, X, n));
     QT_TRY(s.get(&V, (size_t)cols * cols));
   } else {
     QT_CHECK_CUDA(h, cudaMemcpyAsync(X, theta, sizeof(float2) * m * n, cudaMemcpyDeviceToDevice, h->stream));
   }
+  double tn2 = 0;
+  QT_CHECK_CUDA(h, cudaMemcpyAsync(&tn2, dn, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  QT_CHECK_CUDA(h, cudaStreamSynchronize(h->stream));
+  // the Jacobi works on X = theta 2^-e; the unit left factor and the
+  // projection B' = A'^H theta (from theta itself) need no correction
+  const int e = fp32_scale_exponent(tn2);
+  if (e) QT_LAUNCH(h, scale_pow2_kernel<float2>, 256, 256, 0, X, rows * cols, std::ldexp(1.0, -e));
   QT_TRY(qt_jacobi_svd<float2>(h, X, rows, cols, rows, V, cols, auto_tol(h, rows, true), h->cfg.max_sweeps,
-                               &o->sweeps, fast_freeze ? std::sqrt((double)rows) * 5.96e-8 : -1.0));
+                               &o->sweeps, fast_freeze ? std::sqrt((double)rows) * 5.96e-8 : -1.0, keep_hint));
   double* sig;
   int* perm;
   QT_TRY(s.get(&sig, (size_t)cols));
@@ -631,6 +666,8 @@ int svd_split_direct32(qt_handle* h, const float2* theta, int64_t m, int64_t n, 
   o->s.resize(cols);
   QT_CHECK_CUDA(h, cudaMemcpyAsync(o->s.data(), sig, sizeof(double) * cols, cudaMemcpyDeviceToHost, h->stream));
   QT_CHECK_CUDA(h, cudaStreamSynchronize(h->stream));
+  if (e)
+    for (double& v : o->s) v = std::ldexp(v, e);
   if (extra_tail >= 0) {
     std::vector<double> sx = o->s;
     sx.push_back(extra_tail);
@@ -777,7 +814,8 @@ int svd_split_chosen(qt_handle* h, float2* theta, int64_t m, int64_t n, double c
   const bool fast = cap_bound || fast_freeze_ok(m, n, eff_cut, std::sqrt(tn2));
   if (4 * l >= 3 * kmin || kmin <= 32) {
     *sketch = 0;
-    const int rc = svd_split_direct32<TO>(h, theta, m, n, eff_cut, chi_max, Aout, Bout, o, -1.0, fast);
+    const int rc = svd_split_direct32<TO>(h, theta, m, n, eff_cut, chi_max, Aout, Bout, o, -1.0, fast,
+                                          cap_bound ? chi_max : 0);
     if (rc == QT_ENUMERIC) {  // the FP32-storage Jacobi did not settle: exact FP64 path
       qt_dfree(h, *Aout);
       qt_dfree(h, *Bout);
@@ -788,6 +826,12 @@ int svd_split_chosen(qt_handle* h, float2* theta, int64_t m, int64_t n, double c
     return rc;
   }
   *sketch = (int)l;
+  // the range finder's Gram matrices are FP32: work on theta 2^-e (theta is
+  // this function's to overwrite) and scale the results back at the end
+  const int e = fp32_scale_exponent(tn2);
+  const double up = std::ldexp(1.0, e);
+  if (e) QT_LAUNCH(h, scale_pow2_kernel<float2>, 256, 256, 0, theta, m * n, 1.0 / up);
+  const double cut_s = e ? eff_cut / up : eff_cut;
   const float2 one = make_float2(1, 0), zero = make_float2(0, 0), mone = make_float2(-1, 0);
   float2 *om, *Y, *Z, *BH;
   QT_TRY(s.get(&om, (size_t)n * l));
@@ -831,7 +875,8 @@ int svd_split_chosen(qt_handle* h, float2* theta, int64_t m, int64_t n, double c
   QT_TRY(qt_adjoint_copy<float2>(h, BH, n, l, n, Bm, l));
   float2 *Ab = nullptr, *Bb = nullptr;
   {
-    const int rc = svd_split_direct32<float2>(h, Bm, l, n, eff_cut, chi_max, &Ab, &Bb, o, *residual, fast);
+    const int rc = svd_split_direct32<float2>(h, Bm, l, n, cut_s, chi_max, &Ab, &Bb, o, *residual, fast,
+                                              cap_bound ? chi_max : 0);
     if (rc == QT_ENUMERIC) {  // the small SVD did not settle: exact FP64 path
       qt_dfree(h, Ab);
       qt_dfree(h, Bb);
@@ -852,6 +897,13 @@ int svd_split_chosen(qt_handle* h, float2* theta, int64_t m, int64_t n, double c
   float2* Af;
   QT_TRY(s.get(&Af, (size_t)m * k));
   QT_TRY(qt_gemm_any(h, QT_OP_N, QT_OP_N, m, k, l, one, Y, m, Ab, l, zero, Af, m));
+  if (e) {  // back to theta's scale: B', the values, the weights, the residual
+    QT_LAUNCH(h, scale_pow2_kernel<float2>, 256, 256, 0, Bb, (int64_t)k * n, up);
+    for (double& v : o->s) v *= up;
+    o->norm2 *= up * up;
+    o->discarded *= up * up;
+    *residual *= up;
+  }
   QT_TRY(qt_dmalloc(h, (void**)Aout, sizeof(TO) * m * k));
   QT_TRY(qt_dmalloc(h, (void**)Bout, sizeof(TO) * k * n));
   QT_TRY(qt_convert(h, Af, QT_C64, *Aout, sizeof(TO) == sizeof(float2) ? QT_C64 : QT_C128, m * k));

@@ -60,6 +60,7 @@ enum {
   QT_FLAG_INNER = 4,     // Jacobi: inner sweeps of the pair solvers this sweep
   QT_FLAG_OFFBIG = 5,    // Jacobi: OFFMAX over pairs of columns above 1e-3 ||X||_F (float bits)
   QT_FLAG_ABORT = 6,     // Jacobi sweep kernel: a bounded round wait gave up
+  QT_FLAG_OFFKEPT = 7,   // Jacobi sweep kernel: OFFMAX over pairs with a column above the keep threshold
   QT_FLAG_COUNT = 8
 };
 
@@ -222,13 +223,20 @@ int qt_norm2(qt_handle* h, const C* x, int64_t n, double* d_out);
 // TS = storage type.
 template <typename TS>
 int qt_jacobi_svd(qt_handle* h, TS* X, int64_t mm, int64_t nn, int64_t ldx, TS* V, int64_t ldv,
-                  double tol, int max_sweeps, int* sweeps_out, double nu_rel = -1.0);
+                  double tol, int max_sweeps, int* sweeps_out, double nu_rel = -1.0, int keep_count = 0);
 // The same with a caller-supplied partial-Gram workspace of qt_jacobi_layout() double2 entries.
 // nu_rel > 0: columns with norm <= nu_rel ||X||_F are frozen (not rotated,
 // not tested); <= 0: the default for the storage precision.
+// keep_count > 0: the caller keeps only the keep_count largest columns (a
+// chi_max cap); the FP32 sweep kernel then ends the iteration once the weight
+// outside the keep_count largest columns (an upper bound of the truncation
+// error) has settled -- it moved by at most 1e-3 of itself over a sweep and
+// 1e-2 over the one before -- or once a sweep rotated no pair holding a
+// column within a factor 4 of the cut or above it.  Only columns far below
+// the cut, which the caller discards, are left unconverged.
 template <typename TS>
 int qt_jacobi_svd_ws(qt_handle* h, TS* X, int64_t mm, int64_t nn, int64_t ldx, TS* V, int64_t ldv, double tol,
-                     int max_sweeps, int* sweeps_out, double2* parts, double nu_rel = -1.0);
+                     int max_sweeps, int* sweeps_out, double2* parts, double nu_rel = -1.0, int keep_count = 0);
 int qt_jacobi_layout(int64_t mm, int64_t nn, int* nb_out, int* chunks_out);
 
 // k_trunc.cu -----------------------------------------------------------------

@@ -131,3 +131,38 @@ def test_rank_features_match_oracle(engine):
     fr = O.rank_features(s_prev, g, w - 1, n, layer, 3, a.shape[0], b.shape[2], 8, 1e-10)
     np.testing.assert_allclose(f, fr, rtol=1e-5, atol=1e-6)
     eng.close()
+
+
+@pytest.mark.parametrize("scale", [1e11, 1e-13])
+def test_chosen_split_is_scale_invariant(engine, scale):
+    """complex64 storage keeps squared norms in FP32: theta' of norm ~1e22 (or
+    ~1e-26) would overflow (underflow) them.  The FP32 splits scale by a power
+    of two first, so the sketched and the direct split give the scaled
+    results of the unit-norm problem: same rank, values and error relative to
+    the scale, no fallback."""
+    rng = np.random.default_rng(3)
+    chi = 128
+    a, b, s = O.decay_theta_factors(chi, rng, decay=0.6)
+    g = O.haar_unitary(rng)
+    cutoff = 1e-3
+    ex = O.apply_2q([a.copy(), b.copy()], g, 1, cutoff, 0)
+    th = exact_theta(a.astype(np.complex64).astype(complex), b.astype(np.complex64).astype(complex), g)
+    for frac in (1.3 * ex.rank / (2 * chi), 1.0):  # sketched split, then the direct one
+        eng = engine.Engine(mode="chosen")
+        const_model(eng, min(1.0, frac))
+        m = eng.mps([(a * scale).astype(np.complex64), (b * scale).astype(np.complex64)], dtype=np.complex64)
+        st = m.apply_2q(g, 1, cutoff * scale * scale, 0)
+        assert not st["fallback"] and st["rank"] == ex.rank, (st, ex.rank)
+        approx = O.theta_of(m.site(1).astype(complex), m.site(2).astype(complex)) / (scale * scale)
+        err = np.linalg.norm(th - approx)
+        assert err <= 1.1 * np.sqrt(ex.discarded_weight), (err, np.sqrt(ex.discarded_weight))
+        m.free()
+        eng.close()
+    # the bare truncated SVD through the same FP32 split
+    M = (th * scale * scale).astype(np.complex64)
+    eng = engine.Engine(mode="chosen")
+    U, S, Vh, k, _ = eng.truncated_svd(M, cutoff * scale * scale, mode="chosen")
+    ref = np.linalg.svd(th, compute_uv=False)
+    assert k == ex.rank
+    np.testing.assert_allclose(S[:k] / (scale * scale), ref[:k], rtol=1e-4, atol=1e-6 * ref[0])
+    eng.close()
