@@ -227,7 +227,9 @@ int qt_mps_norm2(qt_handle* h, const qt_mps* mps, double* out);
  * followed by contract.  qt_mps_compress left-canonicalises with QRs,
  * optionally normalises, then truncates right to left by the tail rule of
  * src/svd.jl:29-33 and chi_max (ranks/discarded: nsites-1 entries, may be
- * NULL).  qt_mps_expect_mpo returns <psi|H|psi>/<psi|psi>. */
+ * NULL); mode picks the split as in qt_truncated_svd (complex128 sites:
+ * QT_MODE_CUSOLVER uses cuSOLVER, any other mode the FP64 Jacobi).
+ * qt_mps_expect_mpo returns <psi|H|psi>/<psi|psi>. */
 int qt_mps_apply_mpo(qt_handle* h, qt_mps* mps, const double* const* W, const int64_t* dims);
 int qt_mps_compress(qt_handle* h, qt_mps* mps, double cutoff, int chi_max, int mode, int normalize, int* ranks,
                     double* discarded);

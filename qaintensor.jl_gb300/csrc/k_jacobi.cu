@@ -1040,10 +1040,19 @@ pair_apply32_kernel(float2* __restrict__ X, int64_t ldx, int mm, float2* __restr
 constexpr int PS_SLAB = 256;                 // rows per slab
 constexpr int PS_LDS = JC + 2;               // slab row stride in float2 (16-byte aligned rows)
 constexpr int PS_TILES = 10;                 // upper 4x4 tiles of the 16x16 Gram
+constexpr int PS_TE = 16;                    // entries per tile
 constexpr int PS_NGRP = NTG / PS_TILES;      // 51 row groups per tile
 constexpr size_t PS_SMEM = 2 * PS_SLAB * PS_LDS * sizeof(float2);  // double-buffered slab, 73,728 bytes
 constexpr int PS_SPIN = 1 << 23;             // polls of a round wait before it gives up
-static_assert(PS_TILES * PS_NGRP * 16 <= 2 * PS_SLAB * PS_LDS, "Gram partials reuse the slab buffer");
+static_assert(PS_TILES * PS_NGRP * PS_TE <= 2 * PS_SLAB * PS_LDS, "Gram partials reuse the slab buffer");
+
+// tile -> (row quad ti, column quad tj), ti <= tj, ordered by ti
+__device__ inline void ps_tile(int tile, int& ti, int& tj) {
+  ti = 0;
+  int rem = tile;
+  while (rem >= 4 - ti) { rem -= 4 - ti; ti++; }
+  tj = ti + rem;
+}
 
 // table q and side (0: first block of the pair, 1: second) of block `blk` in
 // round `round` of the circle tournament over n players
@@ -1072,22 +1081,28 @@ struct sweep_solver {
   float d0[JC];
   float2 G[2][JC][JC + 1];
   float2 W[2][JC][JC + 1];
-  int inner_rot;
 };
 
 // partner of index y in inner round ir of the circle tournament over the 16
 // columns of a pair (the pairing of tournament(ir, ., 16)): 15 meets ir, the
-// others meet 2 ir - y (mod 15)
+// others meet 2 ir - y (mod 15).  (Pairing the two blocks' columns first and
+// each block's own after converged in more outer sweeps.)
 __device__ inline int inner_partner(int ir, int y) {
   if (y == JC - 1) return ir;
   if (y == ir) return JC - 1;
   return (2 * ir - y + (JC - 1)) % (JC - 1);
 }
 
-// The scaled pair solver with one barrier per inner round: thread (x, y) of
-// warps 0-7 computes the rotation of y's pair itself (the two half-warps
-// compute the same 16, bit-identically) and takes x's from lane x by shuffle,
-// then updates Ghat[x][y] and Wt[x][y] into the other buffer.  Same
+// named barrier of the 256 solver threads (warps 0-7)
+__device__ inline void solver_sync() { asm volatile("bar.sync 1, 256;" ::: "memory"); }
+
+// The scaled pair solver, run by warps 0-7 alone (the caller's other warps
+// skip it and wait at its next block barrier): thread (x, y) computes the
+// rotation of y's pair itself (the two half-warps compute the same 16,
+// bit-identically) and takes x's from lane x by shuffle, then updates
+// Ghat[x][y] and Wt[x][y] into the other buffer -- one named barrier per
+// inner round.  An inner round in which no pair needs a rotation is skipped
+// by every warp alike (a warp vote over the same 16 decisions).  Same
 // iteration as diagonalise_scaled2; the rotation is evaluated with the
 // special-function unit's square roots and reciprocals (a few ulps: the
 // rotation stays unitary to FP32 rounding, and the one-sided iteration
@@ -1095,78 +1110,75 @@ __device__ inline int inner_partner(int ir, int y) {
 __device__ int diagonalise_lanes(sweep_solver& sh, const int* col, float tol_inner, float nu2, int max_inner,
                                  int* buf_out) {
   const int t = threadIdx.x, x = (t >> 4) & 15, y = t & 15;
-  const bool owner = t < NGRAM;  // warps 0-7, whole warps
+  if (t >= NGRAM) return 0;  // warps 8-15
   const float tol2 = tol_inner * tol_inner;
   int cur = 0, sweep = 0;
   for (; sweep < max_inner; sweep++) {
+    bool rotated_any = false;
     for (int ir = 0; ir < JC - 1; ir++) {
-      if (owner) {
-        const int yp = inner_partner(ir, y), xp = inner_partner(ir, x);
-        const int p = min(y, yp), q = max(y, yp);
-        const float a = sh.d[cur][p], b = sh.d[cur][q];
-        const float2 gs = sh.G[cur][p][q];
-        const float ags2 = gs.x * gs.x + gs.y * gs.y;
-        float2 jpp = make_float2(1.f, 0.f), jqp = make_float2(0.f, 0.f), jpq = jqp, jqq = jpp;
-        float a2 = a, b2 = b;
-        const bool rotp = col[p] >= 0 && col[q] >= 0 && a > nu2 && b > nu2 && ags2 > tol2;
-        if (rotp) {
-          const float ria = rsqrtf(a), rib = rsqrtf(b), rags = rsqrtf(ags2);
-          const float sqa = a * ria, sqb = b * rib;
-          const float ag = ags2 * rags * sqa * sqb;  // |gamma|
-          const float zeta = __fdividef(b - a, 2.f * ag);
-          const float z2 = fmaf(zeta, zeta, 1.f);
-          const float r1 = z2 * rsqrtf(z2);
-          const float tt = copysignf(__fdividef(1.f, fabsf(zeta) + r1), zeta);
-          const float c = rsqrtf(fmaf(tt, tt, 1.f)), sn = c * tt;
-          const float2 e = make_float2(gs.x * rags, gs.y * rags);
-          a2 = fmaxf(fmaf(-tt, ag, a), nu2);  // a column driven to the noise level is frozen
-          b2 = fmaf(tt, ag, b);
-          const float ia2 = rsqrtf(a2), ib2 = rsqrtf(b2);
-          const float fa = sqa * ia2, fb = sqb * ib2, fab = sqb * ia2, fba = sqa * ib2;
-          jpp = make_float2(c * fa, 0.f);
-          jqp = make_float2(-sn * e.x * fab, sn * e.y * fab);  // -s conj(e) sqrt(b/a')
-          jpq = make_float2(sn * e.x * fba, sn * e.y * fba);   //  s e sqrt(a/b')
-          jqq = make_float2(c * fb, 0.f);
-        }
-        // column y of Jt: rows y and y'
-        const bool low = y == p;
-        const float2 jyy = low ? jpp : jqq, jpy = low ? jqp : jpq;
-        // column x of Jt from lane x (which holds y == x)
-        float2 jxx, jpx;
-        jxx.x = __shfl_sync(0xffffffffu, jyy.x, x);
-        jxx.y = __shfl_sync(0xffffffffu, jyy.y, x);
-        jpx.x = __shfl_sync(0xffffffffu, jpy.x, x);
-        jpx.y = __shfl_sync(0xffffffffu, jpy.y, x);
-        if (x == y) sh.d[cur ^ 1][y] = low ? a2 : b2;
-        if (rotp && x == 0) sh.inner_rot = sweep + 1;
-        float2 gnew = make_float2(0.f, 0.f);
-        if (xp == y && x != y) {
-          const bool rotated = jxx.x != 1.f || jxx.y != 0.f || jpx.x != 0.f || jpx.y != 0.f;
-          if (!rotated) gnew = sh.G[cur][x][y];
-        } else if (x != y) {
-          const float2 g_xy = sh.G[cur][x][y], g_xq = sh.G[cur][x][yp];
-          const float2 g_py = sh.G[cur][xp][y], g_pq = sh.G[cur][xp][yp];
-          const float2 hx = cadd(cmul(g_xy, jyy), cmul(g_xq, jpy));
-          const float2 hp = cadd(cmul(g_py, jyy), cmul(g_pq, jpy));
-          gnew = cadd(cmul(cconj(jxx), hx), cmul(cconj(jpx), hp));
-        }
-        sh.G[cur ^ 1][x][y] = gnew;
-        const float2 w_xy = sh.W[cur][x][y], w_xq = sh.W[cur][x][yp];
-        sh.W[cur ^ 1][x][y] = cadd(cmul(w_xy, jyy), cmul(w_xq, jpy));
+      const int yp = inner_partner(ir, y), xp = inner_partner(ir, x);
+      const int p = min(y, yp), q = max(y, yp);
+      const float a = sh.d[cur][p], b = sh.d[cur][q];
+      const float2 gs = sh.G[cur][p][q];
+      const float ags2 = gs.x * gs.x + gs.y * gs.y;
+      const bool rotp = col[p] >= 0 && col[q] >= 0 && a > nu2 && b > nu2 && ags2 > tol2;
+      if (!__any_sync(0xffffffffu, rotp)) continue;  // the same vote in every solver warp
+      rotated_any = true;
+      float2 jpp = make_float2(1.f, 0.f), jqp = make_float2(0.f, 0.f), jpq = jqp, jqq = jpp;
+      float a2 = a, b2 = b;
+      if (rotp) {
+        const float ria = rsqrtf(a), rib = rsqrtf(b), rags = rsqrtf(ags2);
+        const float sqa = a * ria, sqb = b * rib;
+        const float ag = ags2 * rags * sqa * sqb;  // |gamma|
+        const float zeta = __fdividef(b - a, 2.f * ag);
+        const float z2 = fmaf(zeta, zeta, 1.f);
+        const float r1 = z2 * rsqrtf(z2);
+        const float tt = copysignf(__fdividef(1.f, fabsf(zeta) + r1), zeta);
+        const float c = rsqrtf(fmaf(tt, tt, 1.f)), sn = c * tt;
+        const float2 e = make_float2(gs.x * rags, gs.y * rags);
+        a2 = fmaxf(fmaf(-tt, ag, a), nu2);  // a column driven to the noise level is frozen
+        b2 = fmaf(tt, ag, b);
+        const float ia2 = rsqrtf(a2), ib2 = rsqrtf(b2);
+        const float fa = sqa * ia2, fb = sqb * ib2, fab = sqb * ia2, fba = sqa * ib2;
+        jpp = make_float2(c * fa, 0.f);
+        jqp = make_float2(-sn * e.x * fab, sn * e.y * fab);  // -s conj(e) sqrt(b/a')
+        jpq = make_float2(sn * e.x * fba, sn * e.y * fba);   //  s e sqrt(a/b')
+        jqq = make_float2(c * fb, 0.f);
       }
+      // column y of Jt: rows y and y'
+      const bool low = y == p;
+      const float2 jyy = low ? jpp : jqq, jpy = low ? jqp : jpq;
+      // column x of Jt from lane x (which holds y == x)
+      float2 jxx, jpx;
+      jxx.x = __shfl_sync(0xffffffffu, jyy.x, x);
+      jxx.y = __shfl_sync(0xffffffffu, jyy.y, x);
+      jpx.x = __shfl_sync(0xffffffffu, jpy.x, x);
+      jpx.y = __shfl_sync(0xffffffffu, jpy.y, x);
+      if (x == y) sh.d[cur ^ 1][y] = low ? a2 : b2;
+      float2 gnew = make_float2(0.f, 0.f);
+      if (xp == y && x != y) {
+        const bool rotated = jxx.x != 1.f || jxx.y != 0.f || jpx.x != 0.f || jpx.y != 0.f;
+        if (!rotated) gnew = sh.G[cur][x][y];
+      } else if (x != y) {
+        const float2 g_xy = sh.G[cur][x][y], g_xq = sh.G[cur][x][yp];
+        const float2 g_py = sh.G[cur][xp][y], g_pq = sh.G[cur][xp][yp];
+        const float2 hx = cadd(cmul(g_xy, jyy), cmul(g_xq, jpy));
+        const float2 hp = cadd(cmul(g_py, jyy), cmul(g_pq, jpy));
+        gnew = cadd(cmul(cconj(jxx), hx), cmul(cconj(jpx), hp));
+      }
+      sh.G[cur ^ 1][x][y] = gnew;
+      const float2 w_xy = sh.W[cur][x][y], w_xq = sh.W[cur][x][yp];
+      sh.W[cur ^ 1][x][y] = cadd(cmul(w_xy, jyy), cmul(w_xq, jpy));
       cur ^= 1;
-      __syncthreads();
+      solver_sync();
     }
-    const int again = sh.inner_rot == sweep + 1;  // written before the round's closing barrier
-    __syncthreads();
-    if (!again) break;
+    if (!rotated_any) break;  // every solver warp took the same votes
   }
-  if (owner) {
+  {
     const float d0 = sh.d0[x];
     sh.W[cur][x][y] = d0 > 0.f ? cscale(sh.W[cur][x][y], sqrtf(sh.d[cur][y]) * rsqrtf(d0))
                                : make_float2(x == y ? 1.f : 0.f, 0.f);
   }
-  __syncthreads();
   *buf_out = cur;
   return sweep + (sweep < max_inner ? 1 : 0);
 }
@@ -1183,7 +1195,7 @@ jacobi_sweep32_kernel(float2* __restrict__ xb0, float2* __restrict__ xb1, int64_
                       unsigned long long* phase_ns) {
   extern __shared__ __align__(16) float2 ps_slab[];  // [2][PS_SLAB][PS_LDS]
   __shared__ __align__(16) float2 wsub[2][JC][JW];    // 16x8 unitary blocks that rebuild the two blocks
-  __shared__ float2 psum[3][PS_TILES * 16];
+  __shared__ float2 psum[3][PS_TILES * PS_TE];
   __shared__ float2 gram[NGRAM];
   __shared__ sweep_solver sh;
   __shared__ int col[JC], scol[2][JC], srcq[2], sside[2], srot[2];
@@ -1203,12 +1215,11 @@ jacobi_sweep32_kernel(float2* __restrict__ xb0, float2* __restrict__ xb1, int64_
   const float tolf = (float)tol;
   // slab rows: thread t rebuilds row (t & 255) of block (t >> 8)
   const int lr = t & (PS_SLAB - 1), h = t >> 8;
-  // Gram products: 4x4 tile (ti, tj), ti <= tj, row group grp
+  // Gram products: rows 4 ti .. 4 ti + 3 against columns 4 tj .. 4 tj + 3, row group grp
   const int tile = t / PS_NGRP, grp = t - PS_NGRP * (t / PS_NGRP);
   const bool act = tile < PS_TILES;
-  int ti = 0, rem = act ? tile : 0;
-  while (rem >= 4 - ti) { rem -= 4 - ti; ti++; }
-  const int tj = ti + rem;
+  int ti = 0, tj = 0;
+  if (act) ps_tile(tile, ti, tj);
   const int nslab = (mm + PS_SLAB - 1) / PS_SLAB;
   for (int r = 0; r < R; r++) {
     const int g = g0 + r;
@@ -1251,7 +1262,7 @@ jacobi_sweep32_kernel(float2* __restrict__ xb0, float2* __restrict__ xb1, int64_
     if (__syncthreads_or(gave_up)) return;
     phase(1);  // 0: waits
     pair_columns(r, q, nb, nn, col);
-    if (t == 0) { any_rot = 0; bad = 0; offmax_blk = 0; offbig_blk = 0; offkept_blk = 0; sh.inner_rot = 0; }
+    if (t == 0) { any_rot = 0; bad = 0; offmax_blk = 0; offbig_blk = 0; offkept_blk = 0; }
     if (prev && t < 2) {
       int qq, s;
       pair_of(rp, t == 0 ? bi : bj, nb, qq, s);
@@ -1301,18 +1312,30 @@ jacobi_sweep32_kernel(float2* __restrict__ xb0, float2* __restrict__ xb1, int64_
     };
     auto rebuild = [&](float2* out) {
       if (hrot) {
+        // two partial sums per output (the real and the imaginary part of
+        // x_k each feed their own): four independent FMAs per complex
+        // product instead of two dependent pairs
+        float2 ob[JW];
 #pragma unroll
-        for (int c = 0; c < JW; c++) out[c] = make_float2(0.f, 0.f);
+        for (int c = 0; c < JW; c++) { out[c] = make_float2(0.f, 0.f); ob[c] = out[c]; }
         asm volatile("" ::: "memory");  // keep wsub in shared memory
 #pragma unroll
         for (int k = 0; k < JC; k++) {
 #pragma unroll
           for (int c = 0; c < JW; c += 2) {
             const float4 w = *reinterpret_cast<const float4*>(&wsub[h][k][c]);
-            cfma(out[c], xr[k], make_float2(w.x, w.y));
-            cfma(out[c + 1], xr[k], make_float2(w.z, w.w));
+            out[c].x = fmaf(xr[k].x, w.x, out[c].x);
+            out[c].y = fmaf(xr[k].x, w.y, out[c].y);
+            ob[c].x = fmaf(-xr[k].y, w.y, ob[c].x);
+            ob[c].y = fmaf(xr[k].y, w.x, ob[c].y);
+            out[c + 1].x = fmaf(xr[k].x, w.z, out[c + 1].x);
+            out[c + 1].y = fmaf(xr[k].x, w.w, out[c + 1].y);
+            ob[c + 1].x = fmaf(-xr[k].y, w.w, ob[c + 1].x);
+            ob[c + 1].y = fmaf(xr[k].y, w.z, ob[c + 1].y);
           }
         }
+#pragma unroll
+        for (int c = 0; c < JW; c++) out[c] = cadd(out[c], ob[c]);
       } else {
 #pragma unroll
         for (int c = 0; c < JW; c++) out[c] = xr[c];
@@ -1331,9 +1354,9 @@ jacobi_sweep32_kernel(float2* __restrict__ xb0, float2* __restrict__ xb1, int64_
 #pragma unroll
       for (int c = 0; c < JW; c += 2) sp[c / 2] = make_float4(o[c].x, o[c].y, o[c + 1].x, o[c + 1].y);
     };
-    float2 acc[16];
+    float2 acc[PS_TE];
 #pragma unroll
-    for (int e = 0; e < 16; e++) acc[e] = make_float2(0.f, 0.f);
+    for (int e = 0; e < PS_TE; e++) acc[e] = make_float2(0.f, 0.f);
     load_row(src, ldx, mm, lr);
     build_slab(0);
     __syncthreads();
@@ -1378,25 +1401,24 @@ jacobi_sweep32_kernel(float2* __restrict__ xb0, float2* __restrict__ xb1, int64_
     float2* red = ps_slab;
     if (act) {
 #pragma unroll
-      for (int e = 0; e < 16; e++) red[(grp * PS_TILES + tile) * 16 + e] = acc[e];
+      for (int e = 0; e < PS_TE; e++) red[(grp * PS_TILES + tile) * PS_TE + e] = acc[e];
     }
     __syncthreads();
     static_assert(PS_NGRP == 3 * 17, "three partial sums of 17 row groups");
-    if (t < 3 * PS_TILES * 16) {
+    if (t < 3 * PS_TILES * PS_TE) {
       const int ent = t / 3, part = t % 3;
-      const float2* rp0 = red + (size_t)(part * 17) * PS_TILES * 16 + ent;
+      const float2* rp0 = red + (size_t)(part * 17) * PS_TILES * PS_TE + ent;
       float2 v = rp0[0];
 #pragma unroll
-      for (int gg = 1; gg < 17; gg++) v = cadd(v, rp0[(size_t)gg * PS_TILES * 16]);
+      for (int gg = 1; gg < 17; gg++) v = cadd(v, rp0[(size_t)gg * PS_TILES * PS_TE]);
       psum[part][ent] = v;
     }
     __syncthreads();
-    if (t < PS_TILES * 16) {
+    if (t < PS_TILES * PS_TE) {
       const float2 v = cadd(cadd(psum[0][t], psum[1][t]), psum[2][t]);
-      const int tl = t / 16, e = t % 16;
-      int ai = 0, rm = tl;
-      while (rm >= 4 - ai) { rm -= 4 - ai; ai++; }
-      const int aj = ai + rm;
+      int ai, aj;
+      ps_tile(t / PS_TE, ai, aj);
+      const int e = t % PS_TE;
       const int rw = 4 * ai + e / 4, cl = 4 * aj + e % 4;
       if (ai != aj || rw <= cl) {
         if (!isfinite(v.x) || !isfinite(v.y)) bad = 1;
@@ -1455,6 +1477,7 @@ jacobi_sweep32_kernel(float2* __restrict__ xb0, float2* __restrict__ xb1, int64_
       int buf = 0;
       const int inner = diagonalise_lanes(sh, col, tol_inner, nu2, max_inner, &buf);
       if (t == 0) atomicAdd(&flags[QT_FLAG_INNER], inner);
+      // each solver thread stores the entry it finished itself
       if (owner) __stcg(wbuf + (size_t)(g & 1) * pairs * NGRAM + (size_t)q * NGRAM + t, sh.W[buf][i][j]);
     }
     phase(4);  // 3: pair solver

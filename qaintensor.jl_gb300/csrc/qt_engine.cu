@@ -929,7 +929,10 @@ int qt_split_device(qt_handle* h, int dtype, const void* M, int64_t m, int64_t n
     double2* Mc;
     QT_TRY(s.get(&Mc, (size_t)m * n));
     QT_CHECK_CUDA(h, cudaMemcpyAsync(Mc, M, sizeof(double2) * m * n, cudaMemcpyDeviceToDevice, h->stream));
-    rc = svd_split_jacobi<double2, double2>(h, Mc, m, n, cutoff, chi_max, false, (double2**)A, (double2**)B, &o);
+    if (mode == QT_MODE_CUSOLVER)
+      rc = svd_split_cusolver<double2>(h, Mc, m, n, cutoff, chi_max, (double2**)A, (double2**)B, &o);
+    else
+      rc = svd_split_jacobi<double2, double2>(h, Mc, m, n, cutoff, chi_max, false, (double2**)A, (double2**)B, &o);
   } else if (mode == QT_MODE_CHOSEN) {
     qt_scratch s(h);
     double* dn;

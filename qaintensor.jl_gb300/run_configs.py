@@ -14,9 +14,10 @@ c3  64-qubit brickwork, complex64, chi_max 1024, cutoff 1e-8, chosen mode:
 c4  batched ensemble: circuits with qubits U[8,40], depth U[4,24], chi_max in
     {16,32,64,128}, complex64, cutoff 1e-8, one persistent kernel per layer in
     a CUDA graph: aggregate updates/s, <Z_1> error against the oracle on a sample.
-c5  40-site TFIM MPO (J=1, h ~ U[0.5,1.5]) applied 10 times to a random chi=512
-    complex64 MPS, each followed by a compression sweep to chi 512 at cutoff
-    1e-9: <H> against an FP64 device run on the same inputs, wall time.
+c5  40-site TFIM MPO (J=1, h ~ U[0.5,1.5]) applied 10 times to a random
+    normalised chi=512 complex64 MPS, each followed by a compression sweep to
+    chi 512 at cutoff 1e-9 and a renormalisation: <H> against an FP64 device
+    run (cuSOLVER splits) on the same inputs, wall time.
 """
 
 from __future__ import annotations
@@ -205,22 +206,35 @@ def c5(qt, args):
     h = rng.uniform(0.5, 1.5, n)
     mpo = O.tfim_mpo(n, 1.0, h)
     dims = [1] + [chi] * (n - 1) + [1]
+    # a random MPS with entries of variance 1/(2 chiL): each transfer step
+    # keeps the expected norm, and the state is normalised exactly below
     sites = [((rng.standard_normal((dims[i], 2, dims[i + 1])) + 1j * rng.standard_normal((dims[i], 2, dims[i + 1])))
-              / math.sqrt(2)).astype(np.complex64) for i in range(n)]
+              / math.sqrt(2 * 2 * dims[i])).astype(np.complex64) for i in range(n)]
     res = {"config": "c5", "chi": chi, "steps": steps}
-    for mode, dt in (("chosen", np.complex64), ("plain", np.complex128)):
+
+    def normalise(m):
+        # the power iteration's norm grows by up to ||H|| per application;
+        # <H> is scale-invariant, the storage is not
+        first = m.site(1)
+        m.upload_site(1, first / math.sqrt(m.norm2()))
+
+    # the FP64 reference run splits with cuSOLVER (FP64, the faster of the
+    # two FP64 paths at bond 3 chi)
+    for mode, dt in (("chosen", np.complex64), ("cusolver", np.complex128)):
         eng = qt.Engine(mode=mode, tc_gemm=1 if mode == "chosen" else 0)
         m = eng.mps([s.astype(dt) for s in sites], dtype=dt)
+        normalise(m)
         m.compress(cutoff, chi, mode=mode)
         t0 = time.perf_counter()
         for _ in range(steps):
             m.apply_mpo(mpo)
             m.compress(cutoff, chi, mode=mode)
+            normalise(m)
         sec = time.perf_counter() - t0
         res[mode] = {"seconds": sec, "energy": m.expect_mpo(mpo)}
         m.free()
         eng.close()
-    res["dE"] = abs(res["chosen"]["energy"] - res["plain"]["energy"])
+    res["dE"] = abs(res["chosen"]["energy"] - res["cusolver"]["energy"])
     return res
 
 

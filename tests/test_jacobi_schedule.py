@@ -47,7 +47,8 @@ def pair_of(r, blk, n):
 
 
 def inner_partner(ir, y, n=16):
-    """The pair solver's partner of column y in inner round ir."""
+    """The pair solver's partner of column y in inner round ir (the circle
+    tournament over the pair's 16 columns)."""
     if y == n - 1:
         return ir
     if y == ir:
