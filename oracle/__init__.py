@@ -7,6 +7,7 @@ legs of ``bench.py`` may import it.  It restates, in numpy/scipy FP64
 that the CUDA engine replaces:
 
 * ``contract_rep`` / ``ncon`` pairwise contraction   (src/contract.jl:39-60, 242-264)
+* ``contract_order`` contraction-order search        (src/contract.jl:8-32, 65-235)
 * ``contract_svd`` and its absolute tail-norm rule    (src/svd.jl:7-38, rule at :29-33)
 * ``switch!`` / ``permute!``                          (src/switch.jl:18-144 of the file)
 * ``MPS(psi)`` sequential SVD                         (src/mps.jl:55-89)

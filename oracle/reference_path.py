@@ -16,7 +16,8 @@ import numpy as np
 import scipy.linalg as sla
 
 __all__ = [
-    "QaintensorError", "Summation", "Network", "contract_rep", "ncon", "contract",
+    "QaintensorError", "Summation", "Network", "contract_rep", "contract_rep_costs", "contract_order", "ncon",
+    "contract",
     "svd_gesdd", "tail_rank", "contract_svd", "check_mps", "make_mps", "OpenMPS",
     "ClosedMPS", "PeriodicMPS", "contract_svd_mps", "mps_from_state", "switch_adjacent",
     "switch_wires", "switch_pairs", "permute_mps", "mpo_from_matrix", "decompose",
@@ -82,15 +83,80 @@ def contract_rep(net: Network) -> List[List[int]]:
     return indexlist
 
 
-def ncon(tensors: Sequence[np.ndarray], indexlist: Sequence[Sequence[int]]) -> np.ndarray:
+def contract_rep_costs(net: Network):
+    """src/contract.jl:8-32 (``contract_rep(net, optimize=true)``): the labels of
+    ``contract_rep`` plus each label's dimension (open legs under |label|)."""
+    indexlist = contract_rep(net)
+    costs = {}
+    for t, labels in zip(net.tensors, indexlist):
+        for leg, lab in enumerate(labels):
+            costs[abs(lab)] = t.shape[leg]
+    return costs, indexlist
+
+
+def contract_order(leg_costs, indexlist):
+    """src/contract.jl:183-235 (``contract_order``): the breadth-first search
+    for the cheapest pairwise contraction sequence of Pfeifer, Haegeman and
+    Verstraete (arXiv:1304.6112), with its cost cap, as the reference ports it
+    (``check_contraction!`` at :94-160, ``getBuildCost`` at :65-85).  An object
+    is (legs, tensors, sequence, cost); a pair of disjoint objects sharing a
+    leg builds the object of their union at cost prod(dims of all legs of
+    both) + both costs.  Returns (sequence of contracted labels, cost)."""
+    n = len(indexlist)
+    S = [[] for _ in range(n + 1)]
+    new = [[] for _ in range(n + 1)]
+    for i, labels in enumerate(indexlist):
+        S[1].append((frozenset(abs(x) for x in labels), frozenset([i]), [], 0))
+        new[1].append(True)
+    mu_old, mu_cap, mu_next = 0, 1, math.inf
+    while not S[n]:
+        for c in range(2, n + 1):
+            for d in range(1, c // 2 + 1):
+                a, b = d, c - d
+                for i, (la, ta, qa, ca) in enumerate(S[a]):
+                    for j, (lb, tb, qb, cb) in enumerate(S[b]):
+                        if ta & tb:
+                            continue
+                        common = la & lb
+                        if not common:
+                            continue
+                        free = la ^ lb
+                        cost = 1
+                        for leg in free | common:
+                            cost *= leg_costs[leg]
+                        cost += ca + cb
+                        if cost > mu_cap:
+                            mu_next = min(mu_next, cost)
+                            continue
+                        if not (new[a][i] or new[b][j]) and cost <= mu_old:
+                            continue
+                        tens = ta | tb
+                        seq = qa + qb + sorted(common)
+                        ptr = next((k for k, o in enumerate(S[a + b]) if o[1] == tens), None)
+                        if ptr is None:
+                            S[a + b].append((free, tens, seq, cost))
+                            new[a + b].append(True)
+                        elif S[a + b][ptr][3] > cost:
+                            S[a + b][ptr] = (free, tens, seq, cost)
+                            new[a + b][ptr] = True
+        if not S[n] and mu_next == math.inf:
+            raise QaintensorError("contract_order: the network is not connected")
+        mu_old, mu_cap, mu_next = mu_cap, mu_next, math.inf
+        for flags in new:
+            flags[:] = [False] * len(flags)
+    return S[n][0][2], S[n][0][3]
+
+
+def ncon(tensors: Sequence[np.ndarray], indexlist: Sequence[Sequence[int]], order=None) -> np.ndarray:
     """TensorOperations 3.1 ``ncon`` (called at src/contract.jl:257,263).
 
-    Positive labels are contracted pairwise in ascending label order (each
-    pairwise step contracts every label the two operands share); negative
-    labels stay open and the result's axes are ordered -1, -2, ...
+    Positive labels are contracted pairwise in ascending label order, or in
+    ``order`` when given (each pairwise step contracts every label the two
+    operands share); negative labels stay open and the result's axes are
+    ordered -1, -2, ...
     """
     work = [(np.asarray(t), list(l)) for t, l in zip(tensors, indexlist)]
-    for lab in sorted({v for l in indexlist for v in l if v > 0}):
+    for lab in (order if order is not None else sorted({v for l in indexlist for v in l if v > 0})):
         holders = [k for k, (_, l) in enumerate(work) if lab in l]
         if not holders:
             continue  # already consumed by an earlier multi-label pairwise step
@@ -118,10 +184,18 @@ def ncon(tensors: Sequence[np.ndarray], indexlist: Sequence[Sequence[int]]) -> n
     return np.transpose(t, order) if l else t
 
 
-def contract(net: Network) -> np.ndarray:
-    """src/contract.jl:242-264 with ``optimize=false``."""
+def contract(net: Network, optimize: bool = False) -> np.ndarray:
+    """src/contract.jl:242-264.  With ``optimize`` (:249-258) the labels are
+    renumbered by their position in ``contract_order``'s sequence and ncon
+    runs with ``order=sequence``, as the reference does."""
     if len(net.tensors) == 1:
         return np.transpose(net.tensors[0], [leg - 1 for (_, leg) in net.openidx])
+    if optimize:
+        costs, indexlist = contract_rep_costs(net)
+        sequence, _ = contract_order(costs, indexlist)
+        pos = {lab: k for k, lab in enumerate(sequence, 1)}
+        indexlist = [[pos[v] if v > 0 else v for v in l] for l in indexlist]
+        return ncon([t for t in net.tensors], indexlist, order=list(sequence))
     return ncon([t for t in net.tensors], contract_rep(net))
 
 

@@ -16,6 +16,7 @@ usable.
 from __future__ import annotations
 
 import ctypes as C
+import math
 import os
 from typing import List, Optional, Sequence
 
@@ -744,19 +745,91 @@ def contract_rep(tensors, contractions, openidx) -> List[List[int]]:
     return labels
 
 
-def contract(engine: "Engine", tensors, contractions, openidx) -> np.ndarray:
-    """``contract(net)`` of src/contract.jl:242-264 (optimize=false) with every
+def contract_order(shapes, labels):
+    """``contract_order`` of src/contract.jl:183-235: the cheapest pairwise
+    contraction sequence by the breadth-first search with a rising cost cap
+    of Pfeifer, Haegeman and Verstraete (arXiv:1304.6112), as the reference
+    ports it from opt_einsum.  Objects are bitmasks (tensors, legs by |label|);
+    the cost of joining two objects that share a leg is the product of the
+    dimensions of all their legs plus both build costs.  Same visiting order,
+    tie-breaking and cap updates as the reference, so the same sequence.
+    Returns (sequence of contracted labels, cost)."""
+    dim = {}
+    for shp, lab in zip(shapes, labels):
+        for d, v in zip(shp, lab):
+            dim[abs(v)] = int(d)
+    n = len(labels)
+    # level c holds objects built from c tensors: [legmask, tensormask, seq, cost, new]
+    level = [[] for _ in range(n + 1)]
+    for i, lab in enumerate(labels):
+        legs = 0
+        for v in lab:
+            legs |= 1 << abs(v)
+        level[1].append([legs, 1 << i, [], 0, True])
+    lo, cap, nxt = 0, 1, math.inf
+    while not level[n]:
+        for c in range(2, n + 1):
+            for d in range(1, c // 2 + 1):
+                dst = level[c]
+                for A in level[d]:
+                    for B in level[c - d]:
+                        if A[1] & B[1]:
+                            continue
+                        shared = A[0] & B[0]
+                        if not shared:
+                            continue
+                        cost = 1
+                        both, bit = A[0] | B[0], 0
+                        while both:
+                            if both & 1:
+                                cost *= dim[bit]
+                            both >>= 1
+                            bit += 1
+                        cost += A[3] + B[3]
+                        if cost > cap:
+                            nxt = min(nxt, cost)
+                            continue
+                        if not (A[4] or B[4]) and cost <= lo:
+                            continue
+                        tmask = A[1] | B[1]
+                        seq = A[2] + B[2] + [b for b in range(shared.bit_length()) if shared >> b & 1]
+                        hit = next((o for o in dst if o[1] == tmask), None)
+                        if hit is None:
+                            dst.append([A[0] ^ B[0], tmask, seq, cost, True])
+                        elif hit[3] > cost:
+                            hit[:] = [A[0] ^ B[0], tmask, seq, cost, True]
+        if not level[n] and nxt == math.inf:
+            raise QaintensorError("contract_order: the network is not connected")
+        lo, cap, nxt = cap, nxt, math.inf
+        for lv in level:
+            for o in lv:
+                o[4] = False
+    return level[n][0][2], level[n][0][3]
+
+
+def contract(engine: "Engine", tensors, contractions, openidx, optimize: bool = False, order=None) -> np.ndarray:
+    """``contract(net, optimize)`` of src/contract.jl:242-264 with every
     pairwise product on the GPU (``qt_contract_pair``).  The schedule is
-    TensorOperations.ncon's: positive labels in ascending order, each step
-    contracting every label the two operands share; a label repeated on one
-    tensor is traced (a product with the identity); disconnected parts are
-    joined by outer products; the result's axes run -1, -2, ...  The final
-    axis order is a host-side transpose of the result (layout only)."""
+    TensorOperations.ncon's: positive labels in ascending order (or in
+    ``order``), each step contracting every label the two operands share; a
+    label repeated on one tensor is traced (a product with the identity);
+    disconnected parts are joined by outer products; the result's axes run
+    -1, -2, ...  With ``optimize`` the labels are renumbered by their position
+    in ``contract_order``'s sequence and contracted with ``order=sequence``,
+    as the reference does.  The final axis order is a host-side transpose of
+    the result (layout only)."""
     if len(tensors) == 1:
         return np.transpose(np.asarray(tensors[0]), [leg - 1 for (_, leg) in openidx])
     labels = contract_rep(tensors, contractions, openidx)
+    if optimize and order is None:
+        if any(len({v for v in l if v > 0}) != sum(1 for v in l if v > 0) for l in labels):
+            raise QaintensorError("contract_order: a leg contracted with its own tensor (a trace) is not supported")
+        sequence, _ = contract_order([np.shape(t) for t in tensors], labels)
+        pos = {lab: k for k, lab in enumerate(sequence, 1)}
+        labels = [[pos[v] if v > 0 else v for v in l] for l in labels]
+        order = list(sequence)
     work = [(np.asarray(t), list(l)) for t, l in zip(tensors, labels)]
-    for lab in sorted({v for l in labels for v in l if v > 0}):
+    for lab in (order if order is not None else sorted({v for l in labels for v in l if v > 0})):
         holders = [k for k, (_, l) in enumerate(work) if lab in l]
         if not holders:
             continue  # consumed by an earlier multi-label step
@@ -793,3 +866,54 @@ def contract_svd_mps(engine: "Engine", tensors, contractions=(), er: float = 0.0
     for j in range(1, n):
         t = engine.contract_svd(t, tensors[j], (t.ndim, 1), er)
     return t
+
+
+def mps_from_state(engine: "Engine", psi, dtype=np.complex128) -> "DeviceMPS":
+    """``MPS(psi)`` of src/mps.jl:55-89 with every SVD on the GPU
+    (``qt_truncated_svd``, cutoff 0: only exactly-zero values are dropped): the
+    statevector (wire 1 = fastest index) is split site by site, U becoming
+    the site and diag(S) V^H carried to the next; returns the device MPS
+    (end sites (1,2,chi) / (chi,2,1), the reference's (2,chi) / (chi,2))."""
+    psi = np.asarray(psi)
+    n = psi.size
+    if n < 2 or n & (n - 1):
+        raise QaintensorError("Input state must have length 2^N")
+    M = n.bit_length() - 1
+    mode = "plain" if np.dtype(dtype) == np.complex128 else "chosen"
+    p = psi.astype(dtype).reshape((2, n // 2), order="F")
+    sites = []
+    lbond = 1
+    for bit in range(1, M):
+        U, S, Vh, k, _ = engine.truncated_svd(p.reshape((lbond * 2, -1), order="F"), 0.0, mode=mode)
+        sites.append(U.reshape((lbond, 2, k), order="F"))
+        p = (S[:, None] * Vh).astype(dtype)
+        lbond = k
+    sites.append(p.reshape((lbond, 2, 1), order="F"))
+    return engine.mps(sites, dtype=dtype)
+
+
+def mpo_from_matrix(engine: "Engine", m) -> List[np.ndarray]:
+    """``MPO(m)`` of src/mpo.jl:27-90 with every SVD on the GPU: the 2^M x 2^M
+    operator is reshaped to (o1,i1,o2,i2,...) (src/mpo.jl:41-51) and split
+    site by site.  Returns the reference's site tensors: first (out,in,b),
+    middle (b,out,in,b'), last (b,out,in); one qubit: the 2x2 matrix."""
+    m = np.asarray(m, dtype=np.complex128)
+    if m.ndim != 2 or m.shape[0] != m.shape[1]:
+        raise QaintensorError("MPO: the operator must be square")
+    M = m.shape[0].bit_length() - 1
+    if M < 1 or m.shape[0] != 1 << M:
+        raise QaintensorError("Need at least one qubit to act on.")
+    if M == 1:
+        return [m.reshape((2, 2), order="F")]
+    perm = [k for i in range(M) for k in (i, i + M)]
+    t = np.transpose(m.reshape((2,) * (2 * M), order="F"), perm).reshape((4, -1), order="F")
+    U, S, Vh, k, _ = engine.truncated_svd(t, 0.0)
+    sites = [U.reshape((2, 2, k), order="F")]
+    t = S[:, None] * Vh
+    for _ in range(2, M):
+        U, S, Vh, nk, _ = engine.truncated_svd(t.reshape((k * 4, -1), order="F"), 0.0)
+        sites.append(U.reshape((k, 2, 2, nk), order="F"))
+        t = S[:, None] * Vh
+        k = nk
+    sites.append(t.reshape((k, 2, 2), order="F"))
+    return sites

@@ -89,3 +89,67 @@ def test_switch_wires_and_permute_match_oracle(engine):
         m = eng.product_state(3)
         m.permute([1, 1, 2])
     eng.close()
+
+
+def test_optimised_order_network(engine):
+    """contract(net, optimize=true) (src/contract.jl:249-258): the planned
+    order on the GPU gives the oracle's tensor (test/test_tensor_circuit.jl:58
+    checks the same against the default order)."""
+    rng = np.random.default_rng(8)
+    n, chi = 5, 6
+    dims = [1] + [chi] * (n - 1) + [1]
+    sites = [crandn(rng, dims[i], 2, dims[i + 1]) for i in range(n)]
+    tensors = sites + [s.conj() for s in sites]
+    contractions = []
+    for i in range(1, n):
+        contractions.append([(i, 3), (i + 1, 1)])
+        contractions.append([(n + i, 3), (n + i + 1, 1)])
+    for i in range(2, n + 1):
+        contractions.append([(i, 2), (n + i, 2)])
+    openidx = [(1, 1), (n + 1, 1), (n, 3), (2 * n, 3), (1, 2), (n + 1, 2)]
+    net = O.Network(tensors, [O.Summation(s) for s in contractions], openidx)
+    eng = engine.Engine(mode="plain")
+    got = engine.contract(eng, tensors, contractions, openidx, optimize=True)
+    ref = O.contract(net)
+    np.testing.assert_allclose(got, O.contract(net, True), rtol=0, atol=1e-12 * np.abs(ref).max())
+    assert np.abs(got - ref).max() <= 1e-12 * np.abs(ref).max()
+    eng.close()
+
+
+@pytest.mark.parametrize("nq", [1, 2, 5, 8])
+def test_mps_from_state_on_gpu(engine, nq):
+    """MPS(psi) (src/mps.jl:55-89) with the SVDs on the GPU: the device MPS
+    contracts back to psi (test/test_mps.jl:34-49) and its bonds are the
+    oracle's."""
+    rng = np.random.default_rng(nq)
+    psi = crandn(rng, 2 ** nq)
+    eng = engine.Engine(mode="plain")
+    if nq == 1:
+        with pytest.raises(engine.QaintensorError, match=r"^Input state must have length 2\^N$"):
+            engine.mps_from_state(eng, crandn(rng, 3))
+        eng.close()
+        return
+    m = engine.mps_from_state(eng, psi)
+    sites = m.sites()
+    back = O.mps_to_state([s.astype(complex) for s in sites])
+    assert np.abs(back - psi).max() <= 1e-12 * np.abs(psi).max()
+    ref = O.mps_from_state(psi)
+    assert [s.shape[-1] for s in sites[:-1]] == [t.shape[-1] for t in ref.tensors[:-1]]
+    m.free()
+    eng.close()
+
+
+@pytest.mark.parametrize("nq", [1, 2, 3, 4])
+def test_mpo_from_matrix_on_gpu(engine, nq):
+    """MPO(m) (src/mpo.jl:27-90) with the SVDs on the GPU: the chain
+    contracts back to m the way the oracle's network does."""
+    rng = np.random.default_rng(10 + nq)
+    mat = crandn(rng, 2 ** nq, 2 ** nq)
+    eng = engine.Engine(mode="plain")
+    sites = engine.mpo_from_matrix(eng, mat)
+    ref = O.mpo_from_matrix(mat)
+    assert [s.shape for s in sites] == [t.shape for t in ref.tensors]
+    got = O.contract(O.Network(sites, ref.contractions, ref.openidx, "mpo"))
+    want = O.contract(ref)
+    assert np.abs(got - want).max() <= 1e-12 * np.abs(want).max()
+    eng.close()

@@ -85,6 +85,8 @@ def test_tensor_circuit_qft_on_general_network():
     for m, w in qft_gates(3):
         O.tensor_circuit(psi, m, w)
     close(O.contract(psi).reshape(-1, order="F"), ref)
+    # test/test_tensor_circuit.jl:58: the optimised contraction order
+    close(O.contract(psi, True).reshape(-1, order="F"), ref)
 
 
 def test_mps_constructor_exceptions():
