@@ -6,6 +6,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <numeric>
 
@@ -656,8 +657,12 @@ int svd_split_direct32(qt_handle* h, const float2* theta, int64_t m, int64_t n, 
   // projection B' = A'^H theta (from theta itself) need no correction
   const int e = fp32_scale_exponent(tn2);
   if (e) QT_LAUNCH(h, scale_pow2_kernel<float2>, 256, 256, 0, X, rows * cols, std::ldexp(1.0, -e));
+  // QT_JACOBI_FREEZE scales the fast freeze threshold (tuning)
+  static const double freeze_scale =
+      std::getenv("QT_JACOBI_FREEZE") ? std::atof(std::getenv("QT_JACOBI_FREEZE")) : 1.0;
   QT_TRY(qt_jacobi_svd<float2>(h, X, rows, cols, rows, V, cols, auto_tol(h, rows, true), h->cfg.max_sweeps,
-                               &o->sweeps, fast_freeze ? std::sqrt((double)rows) * 5.96e-8 : -1.0, keep_hint));
+                               &o->sweeps, fast_freeze ? freeze_scale * std::sqrt((double)rows) * 5.96e-8 : -1.0,
+                               keep_hint));
   double* sig;
   int* perm;
   QT_TRY(s.get(&sig, (size_t)cols));
