@@ -90,45 +90,63 @@ __global__ void __launch_bounds__(256) block_gram_kernel(const C* __restrict__ Y
   }
 }
 
-// Cholesky G = R^H R (R upper) in FP64 on one warp; R replaces the upper
-// triangle of G.  `shift` adds shift * trace(G) to the diagonal first.  A
+// Cholesky G = R^H R (R upper); R replaces the upper triangle of G (the
+// Gram is accumulated in FP64 either way).  RT is the arithmetic: FP64 for
+// an FP64 basis; FP32 for an FP32 basis, whose shifted first pass adds
+// 11 (m b + b (b+1)) u_fp32 (about 4 % of the trace at m = 2048) and whose
+// later passes see a block orthonormal to a few percent, so FP32 pivots
+// lose nothing the stored basis could keep (GB300 runs FP32 at 64x the FP64
+// rate).  `shift` adds shift * trace(G) to the diagonal first.  A
 // non-positive pivot sets QT_FLAG_CHOL and is replaced by a tiny positive
-// value.  Thread t owns column t.
-__global__ void chol_kernel(double2* __restrict__ G, int b, double shift, int* __restrict__ flags) {
-  __shared__ double2 R[BW][BW + 1];
-  __shared__ double rdiag[BW];  // 1 / R[k][k]: one division per pivot
+// value.  One thread per entry (32 x 32 threads), right-looking: at step k
+// one thread forms the pivot, the pivot row is scaled and the trailing upper
+// triangle updated, in barrier-separated phases.
+template <typename RT>
+__global__ void __launch_bounds__(BW * BW) chol_kernel(double2* __restrict__ G, int b, double shift,
+                                                       int* __restrict__ flags) {
+  typedef typename cplx_of<RT>::type CT;
+  __shared__ CT R[BW][BW + 1];
+  __shared__ RT piv[2];
   __shared__ double tr;
-  const int t = threadIdx.x;  // 32 threads
-  if (t == 0) {
-    double s = 0;
-    for (int i = 0; i < b; i++) s += G[i + BW * i].x;
-    tr = s;
+  const int t = threadIdx.x, i = t / BW, j = t % BW;  // thread t owns entry (i, j)
+  const double2 g = (i < b && j < b && i <= j) ? G[i + BW * j] : make_double2(0, 0);
+  if (t < 32) {
+    double s = (t < b) ? G[t + BW * t].x : 0.0;
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (t == 0) tr = s;
   }
-  __syncwarp();
-  for (int i = 0; i < BW; i++) R[i][t] = (t < b && i <= t) ? G[i + BW * t] : make_double2(0, 0);
-  __syncwarp();
-  if (t < b) R[t][t] = make_double2(R[t][t].x + shift * tr, 0.0);
-  __syncwarp();
+  __syncthreads();
+  R[i][j] = ccast<CT>(i == j && i < b ? make_double2(g.x + shift * tr, 0.0) : g);
+  __syncthreads();
   for (int k = 0; k < b; k++) {
+    // row k: R[k][k] = sqrt(d), R[k][j] /= R[k][k] for j > k.  One thread
+    // forms the pivot.  FP64: 1/sqrt(d) from the single-precision estimate
+    // refined by two Newton steps y <- y (3 - d y^2) / 2 (quadratic
+    // convergence: ~2^-22 -> 2^-44 -> below 2^-52); sqrt(d) = d / sqrt(d).
     if (t == 0) {
-      double d = R[k][k].x;
-      if (!(d > 0.0)) {
+      RT d = R[k][k].x;
+      if (!(d > (RT)0)) {
         atomicOr(&flags[QT_FLAG_CHOL], 1);
-        d = fabs(tr) * 1e-30 + 1e-300;
+        d = (RT)(fabs(tr) * 1e-30 + (sizeof(RT) == 8 ? 1e-300 : 1e-37));
       }
-      const double r = sqrt(d);
-      R[k][k] = make_double2(r, 0.0);
-      rdiag[k] = 1.0 / r;
+      RT y = (RT)rsqrtf((float)d);
+      if (sizeof(RT) == 8) {
+        if (!(y > (RT)0) || isinf(y)) y = (RT)(1.0 / sqrt((double)d));  // d outside the FP32 range
+        y = y * ((RT)1.5 - (RT)0.5 * d * y * y);
+        y = y * ((RT)1.5 - (RT)0.5 * d * y * y);
+      }
+      piv[0] = d * y;
+      piv[1] = y;
     }
-    __syncwarp();
-    if (t > k && t < b) R[k][t] = cscale(R[k][t], rdiag[k]);
-    __syncwarp();
-    // trailing update of the upper triangle: A[i][t] -= conj(R[k][i]) R[k][t], k < i <= t
-    if (t > k && t < b)
-      for (int i = k + 1; i <= t; i++) R[i][t] = csub(R[i][t], cmul(cconj(R[k][i]), R[k][t]));
-    __syncwarp();
+    __syncthreads();
+    if (i == k && j == k) R[k][k] = mk(piv[0], (RT)0);
+    if (i == k && j > k && j < b) R[k][j] = cscale(R[k][j], piv[1]);
+    __syncthreads();
+    // trailing update: R[i][j] -= conj(R[k][i]) R[k][j], k < i <= j
+    if (i > k && j >= i && j < b) R[i][j] = csub(R[i][j], cmul(cconj(R[k][i]), R[k][j]));
+    __syncthreads();
   }
-  for (int i = 0; i < BW; i++) G[i + BW * t] = (i <= t) ? R[i][t] : make_double2(0, 0);
+  G[i + BW * j] = (i <= j) ? ccast<double2>(R[i][j]) : make_double2(0, 0);
 }
 
 // Yb <- Yb R^{-1} (R upper triangular b x b): each thread forward-substitutes
@@ -163,6 +181,119 @@ __global__ void __launch_bounds__(128) apply_rinv_kernel(C* __restrict__ Y, int6
   }
 }
 
+// Block Gram-Schmidt projection of the block Yb (m x b, b <= 32) against the
+// j0 columns before it: coef = Y[:, :j0]^H Yb, then Yb -= Y[:, :j0] coef.
+// The coefficients are summed over row chunks of PJ_ROWS rows: each CTA of
+// proj_coef_kernel owns one chunk and 128 of the j0 columns (4 x 4 entries
+// per thread, rows staged 32 at a time) and writes its partial; the chunks
+// are added in chunk order by coef_reduce_kernel (reproducible, no atomics).
+constexpr int PJ_ROWS = 128;  // rows per coefficient chunk
+constexpr int PJ_K = 128;     // previous columns per coefficient CTA
+constexpr int PJ_R = 16;      // rows per CTA of the update
+template <typename C>
+__global__ void __launch_bounds__(256) proj_coef_kernel(const C* __restrict__ Y, int64_t m, int j0,
+                                                        const C* __restrict__ Yb, int b, C* __restrict__ part) {
+  constexpr int SR = sizeof(C) == 8 ? 32 : 16;  // rows staged at a time (static shared memory <= 48 KB)
+  __shared__ C Ys[SR][PJ_K + 1];
+  __shared__ C Bs[SR][BW + 1];
+  const int t = threadIdx.x, kq = t & 31, jq = t >> 5;  // entries k = 4 kq + a, j = 4 jq + c
+  const int64_t r_begin = (int64_t)blockIdx.x * PJ_ROWS, r_end = min(m, r_begin + (int64_t)PJ_ROWS);
+  const int k0 = blockIdx.y * PJ_K;
+  C acc[4][4];
+#pragma unroll
+  for (int a = 0; a < 4; a++)
+#pragma unroll
+    for (int c = 0; c < 4; c++) acc[a][c] = czero<C>();
+  for (int64_t r0 = r_begin; r0 < r_end; r0 += SR) {
+    for (int e = t; e < SR * PJ_K; e += 256) {
+      const int rr = e % SR, kk = e / SR;
+      const int64_t r = r0 + rr;
+      Ys[rr][kk] = (r < r_end && k0 + kk < j0) ? Y[r + m * (int64_t)(k0 + kk)] : czero<C>();
+    }
+    for (int e = t; e < SR * BW; e += 256) {
+      const int rr = e % SR, jj = e / SR;
+      const int64_t r = r0 + rr;
+      Bs[rr][jj] = (r < r_end && jj < b) ? Yb[r + m * (int64_t)jj] : czero<C>();
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int rr = 0; rr < SR; rr++) {
+      C y[4], z[4];
+#pragma unroll
+      for (int a = 0; a < 4; a++) y[a] = Ys[rr][4 * kq + a];
+#pragma unroll
+      for (int c = 0; c < 4; c++) z[c] = Bs[rr][4 * jq + c];
+#pragma unroll
+      for (int a = 0; a < 4; a++)
+#pragma unroll
+        for (int c = 0; c < 4; c++) cfma_conj(acc[a][c], y[a], z[c]);
+    }
+    __syncthreads();
+  }
+  // part[chunk][k][j], k over the padded j0
+  const int jp = gridDim.y * PJ_K;
+#pragma unroll
+  for (int a = 0; a < 4; a++)
+#pragma unroll
+    for (int c = 0; c < 4; c++)
+      part[((size_t)blockIdx.x * jp + k0 + 4 * kq + a) * BW + 4 * jq + c] = acc[a][c];
+}
+
+template <typename C>
+__global__ void coef_reduce_kernel(const C* __restrict__ part, int nchunk, int jp, int j0, C* __restrict__ coef) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;  // e = k * BW + j
+  if (e >= j0 * BW) return;
+  C v = part[e];
+  for (int c = 1; c < nchunk; c++) v = cadd(v, part[(size_t)c * jp * BW + e]);
+  coef[e] = v;
+}
+
+// Yb[r][j] -= sum_k Y[r][k] coef[k][j]: PJ_R rows per CTA, thread (row t >> 4,
+// columns 2 (t & 15), + 1), previous columns staged KT at a time.
+template <typename C>
+__global__ void __launch_bounds__(256) proj_apply_kernel(const C* __restrict__ Y, int64_t m, int j0,
+                                                         const C* __restrict__ coef, C* __restrict__ Yb, int b) {
+  constexpr int KT = sizeof(C) == 8 ? 64 : 32;  // static shared memory <= 48 KB
+  __shared__ __align__(16) C Cs[KT][BW];
+  __shared__ C Ys[PJ_R][KT + 1];
+  const int t = threadIdx.x, rl = t >> 4, jp = t & 15;
+  const int64_t r = (int64_t)blockIdx.x * PJ_R + rl;
+  C a0 = czero<C>(), a1 = czero<C>();
+  for (int k0 = 0; k0 < j0; k0 += KT) {
+    for (int e = t; e < KT * BW; e += 256) {
+      const int kk = e / BW, jj = e % BW;
+      Cs[kk][jj] = (k0 + kk < j0) ? coef[(size_t)(k0 + kk) * BW + jj] : czero<C>();
+    }
+    for (int e = t; e < PJ_R * KT; e += 256) {
+      const int rr = e % PJ_R, kk = e / PJ_R;
+      const int64_t gr = (int64_t)blockIdx.x * PJ_R + rr;
+      Ys[rr][kk] = (gr < m && k0 + kk < j0) ? Y[gr + m * (int64_t)(k0 + kk)] : czero<C>();
+    }
+    __syncthreads();
+#pragma unroll 8
+    for (int kk = 0; kk < KT; kk++) {
+      const C y = Ys[rl][kk];
+      cfma(a0, y, Cs[kk][2 * jp]);
+      cfma(a1, y, Cs[kk][2 * jp + 1]);
+    }
+    __syncthreads();
+  }
+  if (r < m) {
+    if (2 * jp < b) Yb[r + m * (int64_t)(2 * jp)] = csub(Yb[r + m * (int64_t)(2 * jp)], a0);
+    if (2 * jp + 1 < b) Yb[r + m * (int64_t)(2 * jp + 1)] = csub(Yb[r + m * (int64_t)(2 * jp + 1)], a1);
+  }
+}
+
+template <typename C>
+int block_project(qt_handle* h, const C* Y, int64_t m, int j0, C* Yb, int b, C* part, C* coef) {
+  const int nchunk = (int)((m + PJ_ROWS - 1) / PJ_ROWS), nk = (j0 + PJ_K - 1) / PJ_K;
+  QT_LAUNCH(h, proj_coef_kernel<C>, dim3(nchunk, nk), 256, 0, Y, m, j0, Yb, b, part);
+  QT_LAUNCH(h, coef_reduce_kernel<C>, (unsigned)((j0 * BW + 255) / 256), 256, 0, (const C*)part, nchunk, nk * PJ_K,
+            j0, coef);
+  QT_LAUNCH(h, proj_apply_kernel<C>, (unsigned)((m + PJ_R - 1) / PJ_R), 256, 0, Y, m, j0, (const C*)coef, Yb, b);
+  return QT_OK;
+}
+
 template <typename C>
 int block_cholqr(qt_handle* h, C* Yb, int64_t m, int b, bool shifted, double2* dG) {
   QT_CHECK_CUDA(h, cudaMemsetAsync(dG, 0, sizeof(double2) * BW * BW, h->stream));
@@ -173,7 +304,7 @@ int block_cholqr(qt_handle* h, C* Yb, int64_t m, int b, bool shifted, double2* d
   // stored in the element type of Y)
   const double u = (sizeof(typename real_of<C>::type) == 8) ? 1.11e-16 : 5.96e-8;
   const double shift = shifted ? 11.0 * ((double)m * b + (double)b * (b + 1)) * u : 0.0;
-  QT_LAUNCH(h, chol_kernel, 1, 32, 0, dG, b, shift, h->d_flags);
+  QT_LAUNCH(h, chol_kernel<typename real_of<C>::type>, 1, BW * BW, 0, dG, b, shift, h->d_flags);
   QT_LAUNCH(h, apply_rinv_kernel<C>, (unsigned)std::min<int64_t>((m + 127) / 128, 4 * 152), 128, 0, Yb, m, b,
             (const double2*)dG);
   return QT_OK;
@@ -196,19 +327,16 @@ int qt_orthonormalize(qt_handle* h, C* Y, int64_t m, int64_t l) {
   if (l > m) return qt_fail(h, QT_EINVAL, "orthonormalize: more columns than rows");
   qt_scratch s(h);
   double2* dG;
-  C* coef;
+  C *coef, *part;
+  const int64_t nchunk = (m + PJ_ROWS - 1) / PJ_ROWS, lpad = (l + PJ_K - 1) / PJ_K * PJ_K;
   QT_TRY(s.get(&dG, BW * BW));
   QT_TRY(s.get(&coef, (size_t)l * BW));
-  C one, zero, mone;
-  one.x = 1; one.y = 0; zero.x = 0; zero.y = 0; mone.x = -1; mone.y = 0;
+  QT_TRY(s.get(&part, (size_t)nchunk * lpad * BW));
   for (int64_t j0 = 0; j0 < l; j0 += BW) {
     const int b = (int)std::min<int64_t>(BW, l - j0);
     C* Yb = Y + m * j0;
     for (int pass = 0; pass < 2; pass++) {
-      if (j0 > 0) {
-        QT_TRY(qt_gemm_any(h, QT_OP_C, QT_OP_N, j0, b, m, one, Y, m, Yb, m, zero, coef, j0));
-        QT_TRY(qt_gemm_any(h, QT_OP_N, QT_OP_N, m, b, j0, mone, Y, m, coef, j0, one, Yb, m));
-      }
+      if (j0 > 0) QT_TRY(block_project<C>(h, Y, m, (int)j0, Yb, b, part, coef));
       QT_TRY(block_cholqr<C>(h, Yb, m, b, pass == 0, dG));
     }
     // one more CholeskyQR (shifted CholeskyQR3): after a shifted pass with
