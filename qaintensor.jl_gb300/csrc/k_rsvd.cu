@@ -106,7 +106,8 @@ __global__ void __launch_bounds__(BW * BW) chol_kernel(double2* __restrict__ G, 
                                                        int* __restrict__ flags) {
   typedef typename cplx_of<RT>::type CT;
   __shared__ CT R[BW][BW + 1];
-  __shared__ RT piv[2];
+  __shared__ CT X[BW][BW + 1];
+  __shared__ RT piv[2], rdiag[BW];
   __shared__ double tr;
   const int t = threadIdx.x, i = t / BW, j = t % BW;  // thread t owns entry (i, j)
   const double2 g = (i < b && j < b && i <= j) ? G[i + BW * j] : make_double2(0, 0);
@@ -137,6 +138,7 @@ __global__ void __launch_bounds__(BW * BW) chol_kernel(double2* __restrict__ G, 
       }
       piv[0] = d * y;
       piv[1] = y;
+      rdiag[k] = y;
     }
     __syncthreads();
     if (i == k && j == k) R[k][k] = mk(piv[0], (RT)0);
@@ -146,38 +148,51 @@ __global__ void __launch_bounds__(BW * BW) chol_kernel(double2* __restrict__ G, 
     if (i > k && j >= i && j < b) R[i][j] = csub(R[i][j], cmul(cconj(R[k][i]), R[k][j]));
     __syncthreads();
   }
+  // X = R^{-1} (upper) by column sweeps of R X = I, one entry per thread:
+  // for k = b-1 .. 0, row k of X is final once scaled by 1 / R[k][k], and
+  // its multiples R[r][k] X[k][:] are removed from the rows r < k.
+  X[i][j] = mk((RT)(i == j && i < b ? 1 : 0), (RT)0);
+  __syncthreads();
+  for (int k = b - 1; k >= 0; k--) {
+    if (i == k) X[k][j] = cscale(X[k][j], rdiag[k]);
+    __syncthreads();
+    if (i < k) X[i][j] = csub(X[i][j], cmul(R[i][k], X[k][j]));
+    __syncthreads();
+  }
   G[i + BW * j] = (i <= j) ? ccast<double2>(R[i][j]) : make_double2(0, 0);
+  G[BW * BW + i + BW * j] = ccast<double2>(X[i][j]);
 }
 
-// Yb <- Yb R^{-1} (R upper triangular b x b): each thread forward-substitutes
-// one row (y R = x, y_j = (x_j - sum_{k<j} y_k R_kj) / R_jj) in the element
-// precision of Y, with R rounded to it.
+// Yb <- Yb R^{-1} with the explicit inverse X = R^{-1} (upper triangular,
+// formed by chol_kernel): 16 rows per CTA, thread (row t >> 4, columns
+// 2 (t & 15) and + 1), out_j = sum_{k <= j} y_k X[k][j] in the element
+// precision of Y.  The block's rows are read into shared memory before any
+// is written.
 template <typename C>
-__global__ void __launch_bounds__(128) apply_rinv_kernel(C* __restrict__ Y, int64_t m, int b, const double2* __restrict__ R) {
-  typedef typename real_of<C>::type RS;
-  __shared__ C Rs[BW][BW + 1];
-  __shared__ RS rinv[BW];
-  for (int e = threadIdx.x; e < BW * BW; e += blockDim.x) {
-    const int i = e % BW, j = e / BW;
-    Rs[i][j] = (i < b && j < b) ? ccast<C>(R[e]) : czero<C>();
+__global__ void __launch_bounds__(256) apply_rinv_kernel(C* __restrict__ Y, int64_t m, int b,
+                                                         const double2* __restrict__ Xinv) {
+  __shared__ C Xs[BW][BW + 1];
+  __shared__ C Ys[16][BW + 1];
+  const int t = threadIdx.x, rl = t >> 4, jp = t & 15;
+  const int64_t r0 = (int64_t)blockIdx.x * 16;
+  for (int e = t; e < BW * BW; e += 256) Xs[e % BW][e / BW] = ccast<C>(Xinv[e]);
+  for (int e = t; e < 16 * BW; e += 256) {
+    const int rr = e % 16, c = e / 16;
+    Ys[rr][c] = (r0 + rr < m && c < b) ? Y[r0 + rr + m * (int64_t)c] : czero<C>();
   }
-  for (int j = threadIdx.x; j < BW; j += blockDim.x) rinv[j] = (j < b) ? (RS)(1.0 / R[j + BW * j].x) : (RS)0;
   __syncthreads();
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
-    C y[BW];
-#pragma unroll
-    for (int j = 0; j < BW; j++) {
-      if (j >= b) break;
-      C s = Y[i + m * (int64_t)j];
-#pragma unroll
-      for (int k = 0; k < j; k++) {
-        const C r = Rs[k][j];
-        s.x -= y[k].x * r.x - y[k].y * r.y;
-        s.y -= y[k].x * r.y + y[k].y * r.x;
-      }
-      y[j] = cscale(s, rinv[j]);
-      Y[i + m * (int64_t)j] = y[j];
-    }
+  const int j0 = 2 * jp, j1 = 2 * jp + 1;
+  C a0 = czero<C>(), a1 = czero<C>();
+#pragma unroll 8
+  for (int k = 0; k < BW; k++) {
+    const C y = Ys[rl][k];
+    if (k <= j0) cfma(a0, y, Xs[k][j0]);
+    if (k <= j1) cfma(a1, y, Xs[k][j1]);
+  }
+  const int64_t r = r0 + rl;
+  if (r < m) {
+    if (j0 < b) Y[r + m * (int64_t)j0] = a0;
+    if (j1 < b) Y[r + m * (int64_t)j1] = a1;
   }
 }
 
@@ -185,15 +200,17 @@ __global__ void __launch_bounds__(128) apply_rinv_kernel(C* __restrict__ Y, int6
 // j0 columns before it: coef = Y[:, :j0]^H Yb, then Yb -= Y[:, :j0] coef.
 // The coefficients are summed over row chunks of PJ_ROWS rows: each CTA of
 // proj_coef_kernel owns one chunk and 128 of the j0 columns (4 x 4 entries
-// per thread, rows staged 32 at a time) and writes its partial; the chunks
-// are added in chunk order by coef_reduce_kernel (reproducible, no atomics).
-constexpr int PJ_ROWS = 128;  // rows per coefficient chunk
+// per thread, rows staged 32 (FP64: 16) at a time, the next stage loaded
+// into registers meanwhile) and writes its partial; the chunks are added in
+// chunk order by coef_reduce_kernel (reproducible, no atomics).
+constexpr int PJ_ROWS = 64;   // rows per coefficient chunk
 constexpr int PJ_K = 128;     // previous columns per coefficient CTA
 constexpr int PJ_R = 16;      // rows per CTA of the update
 template <typename C>
 __global__ void __launch_bounds__(256) proj_coef_kernel(const C* __restrict__ Y, int64_t m, int j0,
                                                         const C* __restrict__ Yb, int b, C* __restrict__ part) {
   constexpr int SR = sizeof(C) == 8 ? 32 : 16;  // rows staged at a time (static shared memory <= 48 KB)
+  constexpr int NY = SR * PJ_K / 256, NB = SR * BW / 256;
   __shared__ C Ys[SR][PJ_K + 1];
   __shared__ C Bs[SR][BW + 1];
   const int t = threadIdx.x, kq = t & 31, jq = t >> 5;  // entries k = 4 kq + a, j = 4 jq + c
@@ -204,18 +221,30 @@ __global__ void __launch_bounds__(256) proj_coef_kernel(const C* __restrict__ Y,
   for (int a = 0; a < 4; a++)
 #pragma unroll
     for (int c = 0; c < 4; c++) acc[a][c] = czero<C>();
+  // the next stage's values wait in registers while the current one is used
+  C py[NY], pb[NB];
+  auto fetch = [&](int64_t r0) {
+#pragma unroll
+    for (int u = 0; u < NY; u++) {
+      const int e = t + 256 * u, rr = e % SR, kk = e / SR;
+      const int64_t r = r0 + rr;
+      py[u] = (r < r_end && k0 + kk < j0) ? Y[r + m * (int64_t)(k0 + kk)] : czero<C>();
+    }
+#pragma unroll
+    for (int u = 0; u < NB; u++) {
+      const int e = t + 256 * u, rr = e % SR, jj = e / SR;
+      const int64_t r = r0 + rr;
+      pb[u] = (r < r_end && jj < b) ? Yb[r + m * (int64_t)jj] : czero<C>();
+    }
+  };
+  fetch(r_begin);
   for (int64_t r0 = r_begin; r0 < r_end; r0 += SR) {
-    for (int e = t; e < SR * PJ_K; e += 256) {
-      const int rr = e % SR, kk = e / SR;
-      const int64_t r = r0 + rr;
-      Ys[rr][kk] = (r < r_end && k0 + kk < j0) ? Y[r + m * (int64_t)(k0 + kk)] : czero<C>();
-    }
-    for (int e = t; e < SR * BW; e += 256) {
-      const int rr = e % SR, jj = e / SR;
-      const int64_t r = r0 + rr;
-      Bs[rr][jj] = (r < r_end && jj < b) ? Yb[r + m * (int64_t)jj] : czero<C>();
-    }
+#pragma unroll
+    for (int u = 0; u < NY; u++) { const int e = t + 256 * u; Ys[e % SR][e / SR] = py[u]; }
+#pragma unroll
+    for (int u = 0; u < NB; u++) { const int e = t + 256 * u; Bs[e % SR][e / SR] = pb[u]; }
     __syncthreads();
+    if (r0 + SR < r_end) fetch(r0 + SR);
 #pragma unroll 4
     for (int rr = 0; rr < SR; rr++) {
       C y[4], z[4];
@@ -254,22 +283,35 @@ template <typename C>
 __global__ void __launch_bounds__(256) proj_apply_kernel(const C* __restrict__ Y, int64_t m, int j0,
                                                          const C* __restrict__ coef, C* __restrict__ Yb, int b) {
   constexpr int KT = sizeof(C) == 8 ? 64 : 32;  // static shared memory <= 48 KB
+  constexpr int NC = KT * BW / 256, NY = PJ_R * KT / 256;
   __shared__ __align__(16) C Cs[KT][BW];
   __shared__ C Ys[PJ_R][KT + 1];
   const int t = threadIdx.x, rl = t >> 4, jp = t & 15;
   const int64_t r = (int64_t)blockIdx.x * PJ_R + rl;
   C a0 = czero<C>(), a1 = czero<C>();
-  for (int k0 = 0; k0 < j0; k0 += KT) {
-    for (int e = t; e < KT * BW; e += 256) {
-      const int kk = e / BW, jj = e % BW;
-      Cs[kk][jj] = (k0 + kk < j0) ? coef[(size_t)(k0 + kk) * BW + jj] : czero<C>();
+  // the next tile waits in registers while the current one is used
+  C pc[NC], py[NY];
+  auto fetch = [&](int k0) {
+#pragma unroll
+    for (int u = 0; u < NC; u++) {
+      const int e = t + 256 * u, kk = e / BW, jj = e % BW;
+      pc[u] = (k0 + kk < j0) ? coef[(size_t)(k0 + kk) * BW + jj] : czero<C>();
     }
-    for (int e = t; e < PJ_R * KT; e += 256) {
-      const int rr = e % PJ_R, kk = e / PJ_R;
+#pragma unroll
+    for (int u = 0; u < NY; u++) {
+      const int e = t + 256 * u, rr = e % PJ_R, kk = e / PJ_R;
       const int64_t gr = (int64_t)blockIdx.x * PJ_R + rr;
-      Ys[rr][kk] = (gr < m && k0 + kk < j0) ? Y[gr + m * (int64_t)(k0 + kk)] : czero<C>();
+      py[u] = (gr < m && k0 + kk < j0) ? Y[gr + m * (int64_t)(k0 + kk)] : czero<C>();
     }
+  };
+  fetch(0);
+  for (int k0 = 0; k0 < j0; k0 += KT) {
+#pragma unroll
+    for (int u = 0; u < NC; u++) { const int e = t + 256 * u; Cs[e / BW][e % BW] = pc[u]; }
+#pragma unroll
+    for (int u = 0; u < NY; u++) { const int e = t + 256 * u; Ys[e % PJ_R][e / PJ_R] = py[u]; }
     __syncthreads();
+    if (k0 + KT < j0) fetch(k0 + KT);
 #pragma unroll 8
     for (int kk = 0; kk < KT; kk++) {
       const C y = Ys[rl][kk];
@@ -296,7 +338,7 @@ int block_project(qt_handle* h, const C* Y, int64_t m, int j0, C* Yb, int b, C* 
 
 template <typename C>
 int block_cholqr(qt_handle* h, C* Yb, int64_t m, int b, bool shifted, double2* dG) {
-  QT_CHECK_CUDA(h, cudaMemsetAsync(dG, 0, sizeof(double2) * BW * BW, h->stream));
+  QT_CHECK_CUDA(h, cudaMemsetAsync(dG, 0, sizeof(double2) * BW * BW, h->stream));  // the Gram; chol writes R, R^{-1}
   const unsigned gg = (unsigned)std::min<int64_t>((m + GR - 1) / GR, 2 * 152);
   QT_LAUNCH(h, block_gram_kernel<C>, gg, 256, 0, Yb, m, b, dG);
   // shift of shifted CholeskyQR3, sized by the unit roundoff of the stored
@@ -305,8 +347,7 @@ int block_cholqr(qt_handle* h, C* Yb, int64_t m, int b, bool shifted, double2* d
   const double u = (sizeof(typename real_of<C>::type) == 8) ? 1.11e-16 : 5.96e-8;
   const double shift = shifted ? 11.0 * ((double)m * b + (double)b * (b + 1)) * u : 0.0;
   QT_LAUNCH(h, chol_kernel<typename real_of<C>::type>, 1, BW * BW, 0, dG, b, shift, h->d_flags);
-  QT_LAUNCH(h, apply_rinv_kernel<C>, (unsigned)std::min<int64_t>((m + 127) / 128, 4 * 152), 128, 0, Yb, m, b,
-            (const double2*)dG);
+  QT_LAUNCH(h, apply_rinv_kernel<C>, (unsigned)((m + 15) / 16), 256, 0, Yb, m, b, (const double2*)dG + BW * BW);
   return QT_OK;
 }
 
@@ -329,7 +370,7 @@ int qt_orthonormalize(qt_handle* h, C* Y, int64_t m, int64_t l) {
   double2* dG;
   C *coef, *part;
   const int64_t nchunk = (m + PJ_ROWS - 1) / PJ_ROWS, lpad = (l + PJ_K - 1) / PJ_K * PJ_K;
-  QT_TRY(s.get(&dG, BW * BW));
+  QT_TRY(s.get(&dG, 2 * BW * BW));
   QT_TRY(s.get(&coef, (size_t)l * BW));
   QT_TRY(s.get(&part, (size_t)nchunk * lpad * BW));
   for (int64_t j0 = 0; j0 < l; j0 += BW) {
