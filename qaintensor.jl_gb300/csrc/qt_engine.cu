@@ -632,10 +632,13 @@ int fp32_scale_exponent(double norm2) {
 // rotate rounding noise.
 // `keep_hint` > 0: the rank is pinned at that cap, so the Jacobi may stop once
 // the columns at and above the cut have converged.
+// `proj` (m x proj_n, ld m), when given: B' is the projection A'^H proj of
+// that matrix instead of A'^H theta (a sketch theta = proj Y with orthonormal
+// Y: the exact projection of the full matrix), scaled by `out_scale`.
 template <typename TO>
 int svd_split_direct32(qt_handle* h, const float2* theta, int64_t m, int64_t n, double cutoff, int chi_max,
                        TO** Aout, TO** Bout, SvdOut* o, double extra_tail = -1.0, bool fast_freeze = false,
-                       int keep_hint = 0) {
+                       int keep_hint = 0, const float2* proj = nullptr, int64_t proj_n = 0, double out_scale = 1.0) {
   qt_scratch s(h);
   const bool wide = m < n;
   const int64_t rows = wide ? n : m, cols = wide ? m : n;
@@ -682,11 +685,13 @@ int svd_split_direct32(qt_handle* h, const float2* theta, int64_t m, int64_t n, 
     QT_TRY(choose_rank(h, o->s, cutoff, chi_max, o));
   }
   const int k = o->k;
-  const double sc = renorm_scale(h, *o);
+  const double sc = renorm_scale(h, *o) * out_scale;
   const float2 one = make_float2(1, 0), zero = make_float2(0, 0);
+  const float2* psrc = proj ? proj : theta;
+  const int64_t pn = proj ? proj_n : n;
   float2 *At, *Bt;
   QT_TRY(s.get(&At, (size_t)m * k));
-  QT_TRY(s.get(&Bt, (size_t)k * n));
+  QT_TRY(s.get(&Bt, (size_t)k * pn));
   float2 *A0, *G, *W;
   QT_TRY(s.get(&A0, (size_t)m * k));
   QT_TRY(s.get(&G, (size_t)k * k));
@@ -696,17 +701,17 @@ int svd_split_direct32(qt_handle* h, const float2* theta, int64_t m, int64_t n, 
   QT_TRY(qt_gemm_any(h, QT_OP_C, QT_OP_N, k, k, m, one, A0, m, A0, m, zero, G, k));
   QT_LAUNCH(h, newton_schulz_kernel, 256, 256, 0, G, k, W);
   QT_TRY(qt_gemm_any(h, QT_OP_N, QT_OP_N, m, k, k, one, A0, m, W, k, zero, At, m));
-  QT_TRY(qt_gemm_any(h, QT_OP_C, QT_OP_N, k, n, m, one, At, m, theta, m, zero, Bt, k));
+  QT_TRY(qt_gemm_any(h, QT_OP_C, QT_OP_N, k, pn, m, one, At, m, psrc, m, zero, Bt, k));
   {
     // the kept values as reported: norms of the rows of B' = A'^H theta (an
     // exact projection, free of the small drift of the Jacobi column norms)
-    QT_LAUNCH(h, row_norms_kernel, (unsigned)k, 256, 0, Bt, k, n, sig);
+    QT_LAUNCH(h, row_norms_kernel, (unsigned)k, 256, 0, Bt, k, pn, sig);
     QT_CHECK_CUDA(h, cudaMemcpyAsync(o->s.data(), sig, sizeof(double) * k, cudaMemcpyDeviceToHost, h->stream));
   }
   QT_TRY(qt_dmalloc(h, (void**)Aout, sizeof(TO) * m * k));
-  QT_TRY(qt_dmalloc(h, (void**)Bout, sizeof(TO) * k * n));
+  QT_TRY(qt_dmalloc(h, (void**)Bout, sizeof(TO) * k * pn));
   QT_LAUNCH(h, (convert_scale_kernel<float2, TO>), 256, 256, 0, At, *Aout, (int64_t)m * k, 1.0);
-  QT_LAUNCH(h, (convert_scale_kernel<float2, TO>), 256, 256, 0, Bt, *Bout, (int64_t)k * n, sc);
+  QT_LAUNCH(h, (convert_scale_kernel<float2, TO>), 256, 256, 0, Bt, *Bout, (int64_t)k * pn, sc);
   return QT_OK;
 }
 
@@ -844,21 +849,25 @@ int svd_split_chosen(qt_handle* h, float2* theta, int64_t m, int64_t n, double c
   if (e) QT_LAUNCH(h, scale_pow2_kernel<float2>, 256, 256, 0, theta, m * n, 1.0 / up);
   const double cut_s = e ? eff_cut / up : eff_cut;
   const float2 one = make_float2(1, 0), zero = make_float2(0, 0), mone = make_float2(-1, 0);
-  float2 *om, *Y, *Z, *BH;
-  QT_TRY(s.get(&om, (size_t)n * l));
-  QT_TRY(s.get(&Y, (size_t)m * l));
-  QT_TRY(s.get(&Z, (size_t)n * l));
-  QT_TRY(s.get(&BH, (size_t)n * l));
+  // The sketch spans theta's row space: Y (n x l) orthonormal, C = theta Y
+  // (m x l) tall, so its one-sided Jacobi carries no V; A' comes from C and
+  // B' = A'^H theta is the exact projection of the whole matrix.
+  float2 *om, *Y, *Z, *Cm, *Rm;
+  QT_TRY(s.get(&om, (size_t)m * l));
+  QT_TRY(s.get(&Y, (size_t)n * l));
+  QT_TRY(s.get(&Z, (size_t)m * l));
+  QT_TRY(s.get(&Cm, (size_t)m * l));
+  QT_TRY(s.get(&Rm, (size_t)m * n));
   QT_CHECK_CUDA(h, cudaMemsetAsync(h->d_flags + QT_FLAG_CHOL, 0, sizeof(int), h->stream));
-  // range finder: Y = theta Omega, q rounds of subspace iteration
-  QT_TRY(qt_gaussian<float2>(h, om, n, l, n, h->cfg.seed + 0x9E37ull * (++h->sketch_counter)));
-  QT_TRY(qt_gemm_any(h, QT_OP_N, QT_OP_N, m, l, n, one, theta, m, om, n, zero, Y, m));
-  QT_TRY(qt_orthonormalize<float2>(h, Y, m, l));
+  // range finder: Y = theta^H Omega, q rounds of subspace iteration
+  QT_TRY(qt_gaussian<float2>(h, om, m, l, m, h->cfg.seed + 0x9E37ull * (++h->sketch_counter)));
+  QT_TRY(qt_gemm_any(h, QT_OP_C, QT_OP_N, n, l, m, one, theta, m, om, m, zero, Y, n));
+  QT_TRY(qt_orthonormalize<float2>(h, Y, n, l));
   for (int q = 0; q < h->cfg.power_iters; q++) {
-    QT_TRY(qt_gemm_any(h, QT_OP_C, QT_OP_N, n, l, m, one, theta, m, Y, m, zero, Z, n));
-    QT_TRY(qt_orthonormalize<float2>(h, Z, n, l));
-    QT_TRY(qt_gemm_any(h, QT_OP_N, QT_OP_N, m, l, n, one, theta, m, Z, n, zero, Y, m));
-    QT_TRY(qt_orthonormalize<float2>(h, Y, m, l));
+    QT_TRY(qt_gemm_any(h, QT_OP_N, QT_OP_N, m, l, n, one, theta, m, Y, n, zero, Z, m));
+    QT_TRY(qt_orthonormalize<float2>(h, Z, m, l));
+    QT_TRY(qt_gemm_any(h, QT_OP_C, QT_OP_N, n, l, m, one, theta, m, Z, m, zero, Y, n));
+    QT_TRY(qt_orthonormalize<float2>(h, Y, n, l));
   }
   {
     // a Cholesky pivot that vanished means the sketch held fewer than l
@@ -871,26 +880,23 @@ int svd_split_chosen(qt_handle* h, float2* theta, int64_t m, int64_t n, double c
       return QT_OK;
     }
   }
-  // B^H = theta^H Q (n x l); residual theta - Q B
-  QT_TRY(qt_gemm_any(h, QT_OP_C, QT_OP_N, n, l, m, one, theta, m, Y, m, zero, BH, n));
-  QT_TRY(qt_gemm_any(h, QT_OP_N, QT_OP_C, m, n, l, mone, Y, m, BH, n, one, theta, m));
-  QT_TRY(qt_norm2<float2>(h, theta, m * n, dn));
+  // C = theta Y; residual theta - C Y^H (its weight is a tail value of the rule)
+  QT_TRY(qt_gemm_any(h, QT_OP_N, QT_OP_N, m, l, n, one, theta, m, Y, n, zero, Cm, m));
+  QT_CHECK_CUDA(h, cudaMemcpyAsync(Rm, theta, sizeof(float2) * m * n, cudaMemcpyDeviceToDevice, h->stream));
+  QT_TRY(qt_gemm_any(h, QT_OP_N, QT_OP_C, m, n, l, mone, Cm, m, Y, n, one, Rm, m));
+  QT_TRY(qt_norm2<float2>(h, Rm, m * n, dn));
   double res2 = 0;
   QT_CHECK_CUDA(h, cudaMemcpyAsync(&res2, dn, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
   QT_CHECK_CUDA(h, cudaStreamSynchronize(h->stream));
   *residual = std::sqrt(res2);
-  // small SVD of B = Q^H theta' (l x n, wide), the residual weight counted in
-  // the tail rule
-  float2* Bm;
-  QT_TRY(s.get(&Bm, (size_t)l * n));
-  QT_TRY(qt_adjoint_copy<float2>(h, BH, n, l, n, Bm, l));
-  float2 *Ab = nullptr, *Bb = nullptr;
+  // the split of the tall C (m x l): A' from its Jacobi, B' = A'^H theta
   {
-    const int rc = svd_split_direct32<float2>(h, Bm, l, n, cut_s, chi_max, &Ab, &Bb, o, *residual, fast,
-                                              cap_bound ? chi_max : 0);
+    const int rc = svd_split_direct32<TO>(h, Cm, m, l, cut_s, chi_max, Aout, Bout, o, *residual, fast,
+                                          cap_bound ? chi_max : 0, theta, n, up);
     if (rc == QT_ENUMERIC) {  // the small SVD did not settle: exact FP64 path
-      qt_dfree(h, Ab);
-      qt_dfree(h, Bb);
+      qt_dfree(h, *Aout);
+      qt_dfree(h, *Bout);
+      *Aout = *Bout = nullptr;
       *fallback = 2;
       return QT_OK;
     }
@@ -898,29 +904,18 @@ int svd_split_chosen(qt_handle* h, float2* theta, int64_t m, int64_t n, double c
   }
   const bool held_by_cap = chi_max > 0 && chi_max + std::max(0, h->cfg.oversample) <= l;
   if (o->k_cut > (int)l && !held_by_cap) {  // the cutoff needs more than the sketch holds
-    qt_dfree(h, Ab);
-    qt_dfree(h, Bb);
+    qt_dfree(h, *Aout);
+    qt_dfree(h, *Bout);
+    *Aout = *Bout = nullptr;
     *fallback = 1;
     return QT_OK;
   }
-  const int k = o->k;
-  // A' = Q Ab (m x k); B' = Bb
-  float2* Af;
-  QT_TRY(s.get(&Af, (size_t)m * k));
-  QT_TRY(qt_gemm_any(h, QT_OP_N, QT_OP_N, m, k, l, one, Y, m, Ab, l, zero, Af, m));
-  if (e) {  // back to theta's scale: B', the values, the weights, the residual
-    QT_LAUNCH(h, scale_pow2_kernel<float2>, 256, 256, 0, Bb, (int64_t)k * n, up);
+  if (e) {  // back to theta's scale: the values, the weights, the residual (B' is scaled already)
     for (double& v : o->s) v *= up;
     o->norm2 *= up * up;
     o->discarded *= up * up;
     *residual *= up;
   }
-  QT_TRY(qt_dmalloc(h, (void**)Aout, sizeof(TO) * m * k));
-  QT_TRY(qt_dmalloc(h, (void**)Bout, sizeof(TO) * k * n));
-  QT_TRY(qt_convert(h, Af, QT_C64, *Aout, sizeof(TO) == sizeof(float2) ? QT_C64 : QT_C128, m * k));
-  QT_TRY(qt_convert(h, Bb, QT_C64, *Bout, sizeof(TO) == sizeof(float2) ? QT_C64 : QT_C128, (int64_t)k * n));
-  qt_dfree(h, Ab);
-  qt_dfree(h, Bb);
   return QT_OK;
 }
 
