@@ -820,7 +820,8 @@ int svd_split_chosen(qt_handle* h, float2* theta, int64_t m, int64_t n, double c
   const bool cap_bound = chi_max > 0 && chi_max < kmin && kpred > 0 && kpred + h->cfg.oversample >= 0.9 * chi_max;
   // (QT_CAP_SKETCH overrides the factor; tuning)
   static const double cap_mult = std::getenv("QT_CAP_SKETCH") ? std::atof(std::getenv("QT_CAP_SKETCH")) : 1.25;
-  if (cap_bound) l = std::max<int64_t>(l, (int64_t)(cap_mult * chi_max));
+  // (and by at least 64 columns: at chi = 64 a sketch of 80 left 1.006 x)
+  if (cap_bound) l = std::max<int64_t>(l, std::max<int64_t>((int64_t)(cap_mult * chi_max), chi_max + 64));
   l = ((l + 7) / 8) * 8;
   *fallback = 0;
   *residual = 0;

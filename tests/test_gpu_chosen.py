@@ -166,3 +166,36 @@ def test_chosen_split_is_scale_invariant(engine, scale):
     assert k == ex.rank
     np.testing.assert_allclose(S[:k] / (scale * scale), ref[:k], rtol=1e-4, atol=1e-6 * ref[0])
     eng.close()
+
+
+@pytest.mark.parametrize("chil,chir", [(96, 160), (160, 96)])
+def test_sketch_path_on_rectangular_theta(engine, chil, chir):
+    """The sketched split on a rectangular theta' (2 chiL x 2 chiR, both
+    orientations): the row-space sketch, the tall C = theta' Y and the
+    projection B' = A'^H theta' keep the exact rank and the truncation
+    error within 1.1x of the exact SVD's."""
+    rng = np.random.default_rng(chil + 3 * chir)
+    chim = 48
+    a = (rng.standard_normal((chil, 2, chim)) + 1j * rng.standard_normal((chil, 2, chim))) * 0.7 ** np.arange(chim)
+    b = rng.standard_normal((chim, 2, chir)) + 1j * rng.standard_normal((chim, 2, chir))
+    nrm = np.linalg.norm(O.theta_of(a, b))
+    a /= np.sqrt(nrm)
+    b /= np.sqrt(nrm)
+    g = O.haar_unitary(rng)
+    cutoff = 1e-3
+    a64, b64 = a.astype(np.complex64).astype(complex), b.astype(np.complex64).astype(complex)
+    ex = O.apply_2q([a64.copy(), b64.copy()], g, 1, cutoff, 0)
+    eng = engine.Engine(mode="chosen")
+    const_model(eng, min(1.0, 1.3 * ex.rank / (2 * min(chil, chir))))
+    m = eng.mps([a.astype(np.complex64), b.astype(np.complex64)], dtype=np.complex64)
+    st = m.apply_2q(g, 1, cutoff, 0)
+    assert st["sketch_size"] > 0 and not st["fallback"], st
+    assert st["rank"] == ex.rank, (st, ex.rank)
+    th = exact_theta(a64, b64, g)
+    approx = O.theta_of(m.site(1).astype(complex), m.site(2).astype(complex))
+    err = np.linalg.norm(th - approx)
+    assert err <= 1.1 * np.sqrt(ex.discarded_weight), (err, np.sqrt(ex.discarded_weight))
+    A = m.site(1).reshape((2 * chil, -1), order="F").astype(complex)
+    np.testing.assert_allclose(A.conj().T @ A, np.eye(A.shape[1]), atol=2e-5)
+    m.free()
+    eng.close()
