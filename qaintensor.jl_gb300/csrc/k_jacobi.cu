@@ -1837,6 +1837,7 @@ int qt_jacobi_svd_ws(qt_handle* h, TS* X, int64_t mm, int64_t nn, int64_t ldx, T
       }
     }
   }
+  if (phase_ns) QT_CHECK_CUDA(h, cudaStreamSynchronize(h->stream));  // the counters are written on h->stream
   if (phase_ns && sweep_kernel) {
     unsigned long long hp[4];
     QT_CHECK_CUDA(h, cudaMemcpy(hp, phase_ns, sizeof(hp), cudaMemcpyDeviceToHost));

@@ -8,11 +8,17 @@
 // rank-deficient blocks still factor.  Block Gram matrices are accumulated in
 // FP64 from the stored values and factored in FP64; the basis itself is
 // stored in the element type of Y.
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <type_traits>
 
 #include "qt_internal.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace {
 
@@ -196,6 +202,406 @@ __global__ void __launch_bounds__(256) apply_rinv_kernel(C* __restrict__ Y, int6
   }
 }
 
+constexpr int CQ_CS = 8;             // CTAs per cluster
+constexpr int CQ_LDY = BW + 2;       // row stride of the staged rows: 272 B, an odd number of 16-byte granules
+constexpr int CQ_TILES = 36;         // upper 4 x 4 tiles of the 32 x 32 Gram, tile (ti <= tj) at tj (tj+1)/2 + ti
+constexpr int CQ_E = CQ_TILES * 16;  // Gram entries held, e = 36 (4 (i & 3) + (j & 3)) + tile
+constexpr int CQ_GROUPS = 7;         // row groups of the Gram threads (7 x 36 = 252 of 256 threads)
+constexpr int CQ_RS = BW + 1;        // row stride of R
+
+__device__ inline void cq_tile(int T, int& ti, int& tj) {
+  ti = T;
+  tj = 0;
+  while (ti > tj) {
+    ti -= tj + 1;
+    tj++;
+  }
+}
+
+// float-float (hi, lo) + (h2, l2), normalised (TwoSum; Ogita-Rump-Oishi
+// cascaded summation: FP64-like accuracy at FP32 cost)
+__device__ inline void ff_add1(float& h, float& l, float h2, float l2) {
+  const float s = h + h2, bb = s - h;
+  const float e = ((h - (s - bb)) + (h2 - bb)) + (l + l2);
+  h = s + e;
+  l = e - (h - s);
+}
+// float-float complex (re hi, re lo, im hi, im lo)
+__device__ inline float4 ff4_add(float4 a, const float4 b) {
+  ff_add1(a.x, a.y, b.x, b.y);
+  ff_add1(a.z, a.w, b.z, b.w);
+  return a;
+}
+
+// rows staged per CTA: 32 NRB, padded to whole row groups of the Gram
+__host__ __device__ constexpr int cq_alloc_rows(int nrb) { return (32 * nrb + CQ_GROUPS - 1) / CQ_GROUPS * CQ_GROUPS; }
+__host__ __device__ constexpr size_t cq_smem_bytes(int nrb) {
+  return (size_t)cq_alloc_rows(nrb) * CQ_LDY * sizeof(float2) + (size_t)(CQ_GROUPS + 3) * CQ_E * sizeof(float4) +
+         (size_t)BW * CQ_RS * sizeof(float2) + (size_t)BW * BW * sizeof(float2) +
+         BW * sizeof(double) + BW * sizeof(float) + 16;
+}
+
+// CholeskyQR passes of one FP32 block (m x b, b <= 32) in one launch: a
+// thread-block cluster of CQ_CS CTAs holds the block's rows in shared memory
+// (CTA q: rows 32 NRB q .. 32 NRB (q+1) - 1, zero-padded), and each pass
+//   (A) forms the CTA's partial Gram: thread (row group g, upper 4 x 4 tile)
+//       sums its rows g, g + 7, ... in FP32 (about 37 products per entry);
+//   (B) adds the row groups in order in float-float;
+//   (C) reduce-scatter over the cluster through distributed shared memory:
+//       CTA q owns the entries e = q (mod CQ_CS) and adds the ranks in order;
+//   (D) every CTA gathers the summed Gram;
+//   (E) G (+ shift trace(G) on the diagonal) = R^H R and X = R^{-1} in FP32,
+//       blocked by 8 columns -- every CTA computes the same R and X from the
+//       same Gram;
+//   (F) the rows are replaced by rows X (X upper triangular).
+// The loops that carry shared-memory loads have no data-dependent exits, so
+// the loads of a step issue together.  The rows go back to global memory
+// after the last pass.  Every CTA passes the same cluster barriers (two per
+// pass and one before leaving, so that no CTA exits while another may still
+// read its shared memory).
+template <int NRB>
+__global__ void __launch_bounds__(256, 1) cholqr_cluster_kernel(float2* __restrict__ Y, int64_t m, int b, int npass,
+                                                            double shift0, int* __restrict__ flags,
+                                                            unsigned long long* __restrict__ phase_ns) {
+  constexpr int ROWS = 32 * NRB, AROWS = cq_alloc_rows(NRB), GROWS = AROWS / CQ_GROUPS;
+  cg::cluster_group cluster = cg::this_cluster();
+  const int crank = (int)cluster.block_rank();
+  unsigned long long tp = 0;
+  auto phase = [&](int ph) {  // optional diagnostics: CTA 0's SM cycles per phase into phase_ns[ph - 1]
+    if (phase_ns && crank == 0 && threadIdx.x == 0) {
+      const unsigned long long tn = (unsigned long long)clock64();
+      if (ph > 0) atomicAdd(&phase_ns[ph - 1], tn - tp);
+      tp = tn;
+    }
+  };
+  phase(0);
+  extern __shared__ __align__(16) unsigned char cq_smem[];
+  float2* Ys = (float2*)cq_smem;                                  // [AROWS][CQ_LDY]
+  float4* Gt = (float4*)(cq_smem + (size_t)AROWS * CQ_LDY * sizeof(float2));  // [CQ_GROUPS][CQ_E]
+  float4* Gp = Gt + CQ_GROUPS * CQ_E;                             // [2][CQ_E] partial of this CTA
+  float4* Gr = Gp + 2 * CQ_E;                                     // [CQ_E] cluster sums owned here
+  float2* Gl = (float2*)(Gr + CQ_E);                              // [BW][CQ_RS] the Gram in FP32, then R
+  float2* Xs = Gl + BW * CQ_RS;                                   // [BW][BW] R^{-1}
+  double* Gd = (double*)(Xs + BW * BW);                           // [BW] diagonal of the Gram
+  float* Ry = (float*)(Gd + BW);                                  // [BW] 1 / R[k][k], then the tiny pivot
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+  const int64_t r0 = (int64_t)crank * ROWS;
+  // stage: warp w loads columns 4w .. 4w+3, lane l the rows l + 32 u
+  {
+    float2 v[4][NRB];
+#pragma unroll
+    for (int cc = 0; cc < 4; cc++)
+#pragma unroll
+      for (int u = 0; u < NRB; u++) {
+        const int c = 4 * w + cc;
+        const int64_t r = r0 + lane + 32 * u;
+        v[cc][u] = (r < m && c < b) ? Y[r + m * (int64_t)c] : make_float2(0.f, 0.f);
+      }
+#pragma unroll
+    for (int cc = 0; cc < 4; cc++)
+#pragma unroll
+      for (int u = 0; u < NRB; u++) Ys[(lane + 32 * u) * CQ_LDY + 4 * w + cc] = v[cc][u];
+    for (int e = t; e < (AROWS - ROWS) * CQ_LDY; e += 256) Ys[ROWS * CQ_LDY + e] = make_float2(0.f, 0.f);
+  }
+  const int g = t / CQ_TILES, T = t % CQ_TILES;
+  int ti, tj;
+  cq_tile(T, ti, tj);
+  __syncthreads();
+  phase(1);  // staging
+  for (int p = 0; p < npass; p++) {
+    // (A) partial Gram of the rows g, g + 7, g + 14, ... for one upper tile
+    if (g < CQ_GROUPS) {
+      float2 acc[16];
+#pragma unroll
+      for (int k = 0; k < 16; k++) acc[k] = make_float2(0.f, 0.f);
+#pragma unroll 4
+      for (int q = 0; q < GROWS; q++) {
+        const float4* row = (const float4*)(Ys + (g + CQ_GROUPS * q) * CQ_LDY);
+        const float4 a01 = row[2 * ti], a23 = row[2 * ti + 1], b01 = row[2 * tj], b23 = row[2 * tj + 1];
+        const float2 av[4] = {make_float2(a01.x, a01.y), make_float2(a01.z, a01.w), make_float2(a23.x, a23.y),
+                              make_float2(a23.z, a23.w)};
+        const float2 bv[4] = {make_float2(b01.x, b01.y), make_float2(b01.z, b01.w), make_float2(b23.x, b23.y),
+                              make_float2(b23.z, b23.w)};
+#pragma unroll
+        for (int a = 0; a < 4; a++)
+#pragma unroll
+          for (int c = 0; c < 4; c++) cfma_conj(acc[4 * a + c], av[a], bv[c]);
+      }
+#pragma unroll
+      for (int k = 0; k < 16; k++) Gt[g * CQ_E + k * CQ_TILES + T] = make_float4(acc[k].x, 0.f, acc[k].y, 0.f);
+    }
+    __syncthreads();
+    phase(2);  // Gram
+    // (B) the row groups in order
+    float4* gp = Gp + (p & 1) * CQ_E;
+    for (int e = t; e < CQ_E; e += 256) {
+      float4 v = Gt[e];
+#pragma unroll
+      for (int gg = 1; gg < CQ_GROUPS; gg++) v = ff4_add(v, Gt[gg * CQ_E + e]);
+      gp[e] = v;
+    }
+    cluster.sync();
+    phase(3);  // row groups + barrier
+    // (C) this CTA's entries summed over the cluster in rank order
+    if (crank + CQ_CS * t < CQ_E) {
+      const int e = crank + CQ_CS * t;
+      float4 v[CQ_CS];
+#pragma unroll
+      for (int q = 0; q < CQ_CS; q++) v[q] = cluster.map_shared_rank(gp, q)[e];
+#pragma unroll
+      for (int q = 1; q < CQ_CS; q++) v[0] = ff4_add(v[0], v[q]);
+      Gr[e] = v[0];
+    }
+    cluster.sync();
+    phase(4);  // reduce-scatter + barrier
+    // (D) the whole Gram, rounded to FP32 (the diagonal kept in FP64 too)
+    {
+      float4 v[3];
+#pragma unroll
+      for (int u = 0; u < 3; u++) {
+        const int e = t + 256 * u;
+        if (e < CQ_E) v[u] = cluster.map_shared_rank(Gr, e % CQ_CS)[e];
+      }
+#pragma unroll
+      for (int u = 0; u < 3; u++) {
+        const int e = t + 256 * u;
+        if (e < CQ_E) {
+          int ei, ej;
+          cq_tile(e % CQ_TILES, ei, ej);
+          const int k = e / CQ_TILES, i = 4 * ei + (k >> 2), j = 4 * ej + (k & 3);
+          Gl[i * CQ_RS + j] = make_float2(v[u].x + v[u].y, v[u].z + v[u].w);
+          if (i == j) Gd[i] = (double)v[u].x + (double)v[u].y;
+        }
+      }
+    }
+    __syncthreads();
+    phase(5);  // gather
+    // (E) R = chol(G + shift trace(G) I) in place of the Gram's upper
+    // triangle, then X = R^{-1}, both blocked by 8 columns.  Cholesky: for
+    // each diagonal block, warp 0 runs its 8 pivot steps on the block's rows
+    // of every column to the right (lane l: column k0 + l, an 8-row register
+    // window moving down one row per step, rows travelling by shuffles), then
+    // all threads subtract the block's rank-8 product from the trailing upper
+    // triangle.  Inverse: the four 8 x 8 diagonal blocks by column sweeps (one
+    // warp each), then the blocks at distance d = 1, 2, 3 from the diagonal,
+    // X_ij = -X_ii (sum_{i < l <= j} R_il X_lj).  Pivots past b are skipped
+    // (1 / R[k][k] = 0 there), so X is zero outside the leading b x b block.
+    {
+      float* trs = (float*)(Ry + BW);
+      if (w == 0) {
+        double tr = lane < b ? Gd[lane] : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) tr += __shfl_xor_sync(0xffffffffu, tr, o);
+        const double shift = p == 0 ? shift0 : 0.0;
+        if (lane < b) Gl[lane * CQ_RS + lane] = make_float2((float)(Gd[lane] + shift * tr), 0.f);
+        Ry[lane] = 0.f;
+        if (lane == 0) trs[0] = (float)(fabs(tr) * 1e-30 + 1e-37);
+      }
+      __syncthreads();
+      for (int k0 = 0; k0 < b; k0 += 8) {
+        if (w == 0) {
+          const int col = k0 + lane;
+          float2 c[8];
+#pragma unroll
+          for (int r = 0; r < 8; r++)
+            c[r] = (col < BW && k0 + r <= col) ? Gl[(k0 + r) * CQ_RS + col] : make_float2(0.f, 0.f);
+#pragma unroll
+          for (int kk = 0; kk < 8; kk++) {
+            const int k = k0 + kk;
+            if (k < b) {
+              float d = __shfl_sync(0xffffffffu, c[0].x, kk);
+              if (!(d > 0.f)) {
+                if (lane == 0 && crank == 0) atomicOr(&flags[QT_FLAG_CHOL], 1);
+                d = trs[0];
+              }
+              const float y = rsqrtf(d);
+              const float2 rk =
+                  lane == kk ? make_float2(d * y, 0.f) : (lane > kk ? cscale(c[0], y) : make_float2(0.f, 0.f));
+              if (col < BW) Gl[k * CQ_RS + col] = rk;  // row k of R (zeros left of the diagonal)
+              if (lane == 0) Ry[k] = y;
+#pragma unroll
+              for (int r = 1; r < 8; r++) {
+                float2 rkr;  // R[k][k + r] from lane kk + r (slots past the block are discarded)
+                rkr.x = __shfl_sync(0xffffffffu, rk.x, min(kk + r, 31));
+                rkr.y = __shfl_sync(0xffffffffu, rk.y, min(kk + r, 31));
+                c[r - 1] = csub(c[r], cmul(cconj(rkr), rk));
+              }
+            }
+          }
+        }
+        __syncthreads();
+        const int base = k0 + 8, n2 = BW - base;
+        for (int e = t; e < n2 * n2; e += 256) {
+          const int i = base + e / n2, j = base + e % n2;
+          if (i <= j) {
+            float2 v = Gl[i * CQ_RS + j];
+#pragma unroll
+            for (int q = 0; q < 8; q++) v = csub(v, cmul(cconj(Gl[(k0 + q) * CQ_RS + i]), Gl[(k0 + q) * CQ_RS + j]));
+            Gl[i * CQ_RS + j] = v;
+          }
+        }
+        __syncthreads();
+      }
+      phase(6);  // Cholesky
+      // diagonal blocks of X; the blocks below the diagonal are zero
+      if (w < 4 && lane < 8) {
+        const int k0 = 8 * w;
+        float2 x[8];
+#pragma unroll
+        for (int r = 0; r < 8; r++) x[r] = make_float2(r == lane ? 1.f : 0.f, 0.f);
+#pragma unroll
+        for (int kk = 7; kk >= 0; kk--) {
+          x[kk] = cscale(x[kk], Ry[k0 + kk]);
+#pragma unroll
+          for (int i = 0; i < kk; i++) x[i] = csub(x[i], cmul(Gl[(k0 + i) * CQ_RS + k0 + kk], x[kk]));
+        }
+#pragma unroll
+        for (int r = 0; r < 8; r++) Xs[(k0 + r) * BW + k0 + lane] = x[r];
+      }
+      for (int e = t; e < BW * BW; e += 256)
+        if ((e / BW) / 8 > (e % BW) / 8) Xs[e] = make_float2(0.f, 0.f);
+      __syncthreads();
+      float2* Tb = (float2*)Gt;  // free during (E)
+      for (int d = 1; d < 4; d++) {
+        const int bi = t / 64, a = (t / 8) % 8, cc = t % 8, bj = bi + d, i = 8 * bi + a, j = 8 * bj + cc;
+        if (bj < 4) {
+          float2 v = make_float2(0.f, 0.f);
+          for (int l = 8 * (bi + 1); l < 8 * (bj + 1); l++) cfma(v, Gl[i * CQ_RS + l], Xs[l * BW + j]);
+          Tb[t] = v;
+        }
+        __syncthreads();
+        if (bj < 4) {
+          float2 v = make_float2(0.f, 0.f);
+#pragma unroll
+          for (int q = 0; q < 8; q++) cfma(v, Xs[i * BW + 8 * bi + q], Tb[64 * bi + 8 * q + cc]);
+          Xs[i * BW + j] = make_float2(-v.x, -v.y);
+        }
+        __syncthreads();
+      }
+    }
+    phase(7);  // inverse
+    // (F) rows <- rows X: warp w owns columns 4 cg .. 4 cg + 3 (warps w and
+    // w + 4 share a scheduler and take column groups w and 7 - w, which
+    // balances the triangle), lane l the rows l + 32 rb
+    {
+      const int cgp = w < 4 ? w : 11 - w, j0 = 4 * cgp, kend = min(j0 + 4, b);
+      float2 acc[NRB][4];
+#pragma unroll
+      for (int rb = 0; rb < NRB; rb++)
+#pragma unroll
+        for (int c = 0; c < 4; c++) acc[rb][c] = make_float2(0.f, 0.f);
+      for (int k = 0; k < kend; k += 2) {
+        const float4 xa = *(const float4*)(Xs + k * BW + j0), xb = *(const float4*)(Xs + k * BW + j0 + 2);
+        const float4 xc = *(const float4*)(Xs + (k + 1) * BW + j0), xd = *(const float4*)(Xs + (k + 1) * BW + j0 + 2);
+        const float2 x0[4] = {make_float2(xa.x, xa.y), make_float2(xa.z, xa.w), make_float2(xb.x, xb.y),
+                              make_float2(xb.z, xb.w)};
+        const float2 x1[4] = {make_float2(xc.x, xc.y), make_float2(xc.z, xc.w), make_float2(xd.x, xd.y),
+                              make_float2(xd.z, xd.w)};
+        float4 y[NRB];
+#pragma unroll
+        for (int rb = 0; rb < NRB; rb++) y[rb] = *(const float4*)(Ys + (rb * 32 + lane) * CQ_LDY + k);
+#pragma unroll
+        for (int rb = 0; rb < NRB; rb++) {
+          const float2 y0 = make_float2(y[rb].x, y[rb].y), y1 = make_float2(y[rb].z, y[rb].w);
+#pragma unroll
+          for (int c = 0; c < 4; c++) {
+            cfma(acc[rb][c], y0, x0[c]);
+            cfma(acc[rb][c], y1, x1[c]);
+          }
+        }
+      }
+      __syncthreads();  // every row has been read
+#pragma unroll
+      for (int rb = 0; rb < NRB; rb++)
+#pragma unroll
+        for (int c = 0; c < 4; c++)
+          if (j0 + c < b) Ys[(rb * 32 + lane) * CQ_LDY + j0 + c] = acc[rb][c];
+      __syncthreads();
+    }
+    phase(8);  // update
+  }
+#pragma unroll
+  for (int cc = 0; cc < 4; cc++)
+#pragma unroll
+    for (int u = 0; u < NRB; u++) {
+      const int c = 4 * w + cc;
+      const int64_t r = r0 + lane + 32 * u;
+      if (r < m && c < b) Y[r + m * (int64_t)c] = Ys[(lane + 32 * u) * CQ_LDY + c];
+    }
+  cluster.sync();  // no CTA leaves while another may still read its shared memory
+  phase(9);  // write-back + barrier
+}
+
+typedef void (*cq_kernel_t)(float2*, int64_t, int, int, double, int*, unsigned long long*);
+cq_kernel_t cq_kernel(int nrb) {
+  switch (nrb) {
+    case 1: return cholqr_cluster_kernel<1>;
+    case 2: return cholqr_cluster_kernel<2>;
+    case 4: return cholqr_cluster_kernel<4>;
+    default: return cholqr_cluster_kernel<8>;
+  }
+}
+
+// Row blocks (of 32) per CTA of the cluster CholeskyQR for m rows (0: the
+// block does not fit and the four-kernel passes are used).
+// QT_CHOLQR_CLUSTER=0 disables it.
+int cq_nrb(int64_t m) {
+  static int ok = -1;
+  if (ok < 0) {
+    ok = 1;
+    for (int nrb = 1; nrb <= 8 && ok; nrb *= 2) {
+      const size_t smem = cq_smem_bytes(nrb);
+      ok = 0;
+      if (cudaFuncSetAttribute(cq_kernel(nrb), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) ==
+          cudaSuccess) {
+        cudaLaunchConfig_t lc = {};
+        lc.gridDim = dim3(CQ_CS);
+        lc.blockDim = dim3(256);
+        lc.dynamicSmemBytes = smem;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = CQ_CS;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        lc.attrs = attr;
+        lc.numAttrs = 1;
+        int nc = 0;
+        if (cudaOccupancyMaxActiveClusters(&nc, cq_kernel(nrb), &lc) == cudaSuccess && nc > 0) ok = 1;
+      }
+    }
+    cudaGetLastError();
+  }
+  const char* env = std::getenv("QT_CHOLQR_CLUSTER");
+  if (!ok || (env && env[0] == '0')) return 0;
+  for (int nrb = 1; nrb <= 8; nrb *= 2)
+    if ((int64_t)CQ_CS * 32 * nrb >= m) return nrb;
+  return 0;
+}
+
+int block_cholqr_cluster(qt_handle* h, float2* Yb, int64_t m, int b, int nrb, int npass, bool shifted,
+                         unsigned long long* phase_ns) {
+  const double shift = shifted ? 11.0 * ((double)m * b + (double)b * (b + 1)) * 5.96e-8 : 0.0;
+  cudaLaunchConfig_t lc = {};
+  lc.gridDim = dim3(CQ_CS);
+  lc.blockDim = dim3(256);
+  lc.dynamicSmemBytes = cq_smem_bytes(nrb);
+  lc.stream = h->stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = CQ_CS;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  lc.attrs = attr;
+  lc.numAttrs = 1;
+  if (h->prof) qt_prof_before(h, "cholqr_cluster_kernel");
+  const cudaError_t e =
+      cudaLaunchKernelEx(&lc, cq_kernel(nrb), Yb, m, b, npass, shift, h->d_flags, phase_ns);
+  if (h->prof) qt_prof_after(h);
+  h->launches++;
+  if (e != cudaSuccess) return qt_fail(h, QT_ECUDA, std::string("launch cholqr_cluster_kernel: ") + cudaGetErrorString(e));
+  return QT_OK;
+}
+
 // Block Gram-Schmidt projection of the block Yb (m x b, b <= 32) against the
 // j0 columns before it: coef = Y[:, :j0]^H Yb, then Yb -= Y[:, :j0] coef.
 // The coefficients are summed over row chunks of PJ_ROWS rows: each CTA of
@@ -373,9 +779,41 @@ int qt_orthonormalize(qt_handle* h, C* Y, int64_t m, int64_t l) {
   QT_TRY(s.get(&dG, 2 * BW * BW));
   QT_TRY(s.get(&coef, (size_t)l * BW));
   QT_TRY(s.get(&part, (size_t)nchunk * lpad * BW));
+  int nrb = 0;
+  unsigned long long* phase_ns = nullptr;
+  // QT_CHOLQR_PHASES=1 prints the average SM cycles per phase of the
+  // cluster CholeskyQR (CTA 0's clock) after each orthonormalisation
+  static const bool phases = std::getenv("QT_CHOLQR_PHASES") != nullptr;
+  if constexpr (std::is_same<C, float2>::value) {
+    nrb = cq_nrb(m);
+    if (nrb > 0 && phases) {
+      QT_TRY(s.get(&phase_ns, 16));
+      QT_CHECK_CUDA(h, cudaMemsetAsync(phase_ns, 0, 16 * sizeof(unsigned long long), h->stream));
+    }
+  }
+  int cq_launches = 0, cq_passes = 0;
   for (int64_t j0 = 0; j0 < l; j0 += BW) {
     const int b = (int)std::min<int64_t>(BW, l - j0);
     C* Yb = Y + m * j0;
+    if constexpr (std::is_same<C, float2>::value) {
+      if (nrb > 0) {
+        // the same passes as below with each run of CholeskyQR passes in one
+        // cluster launch: shifted, (projection,) plain, plain
+        if (j0 > 0) {
+          QT_TRY(block_project<C>(h, Y, m, (int)j0, Yb, b, part, coef));
+          QT_TRY(block_cholqr_cluster(h, Yb, m, b, nrb, 1, true, phase_ns));
+          QT_TRY(block_project<C>(h, Y, m, (int)j0, Yb, b, part, coef));
+          QT_TRY(block_cholqr_cluster(h, Yb, m, b, nrb, 2, false, phase_ns));
+          cq_launches += 2;
+          cq_passes += 3;
+        } else {
+          QT_TRY(block_cholqr_cluster(h, Yb, m, b, nrb, 3, true, phase_ns));
+          cq_launches += 1;
+          cq_passes += 3;
+        }
+        continue;
+      }
+    }
     for (int pass = 0; pass < 2; pass++) {
       if (j0 > 0) QT_TRY(block_project<C>(h, Y, m, (int)j0, Yb, b, part, coef));
       QT_TRY(block_cholqr<C>(h, Yb, m, b, pass == 0, dG));
@@ -383,6 +821,18 @@ int qt_orthonormalize(qt_handle* h, C* Y, int64_t m, int64_t l) {
     // one more CholeskyQR (shifted CholeskyQR3): after a shifted pass with
     // the FP32 shift the block is only well conditioned, not orthonormal
     if (sizeof(typename real_of<C>::type) == 4) QT_TRY(block_cholqr<C>(h, Yb, m, b, false, dG));
+  }
+  if (phase_ns && cq_launches > 0) {
+    unsigned long long hp[9];
+    QT_CHECK_CUDA(h, cudaStreamSynchronize(h->stream));
+    QT_CHECK_CUDA(h, cudaMemcpy(hp, phase_ns, sizeof(hp), cudaMemcpyDeviceToHost));
+    const char* nm[9] = {"stage", "gram", "groups+barrier", "scatter+barrier", "gather", "cholesky", "inverse",
+                         "update", "writeback+barrier"};
+    std::fprintf(stderr, "cluster CholeskyQR, %d launches, %d passes; SM kilocycles per launch (stage, writeback) "
+                 "or pass:", cq_launches, cq_passes);
+    for (int i = 0; i < 9; i++)
+      std::fprintf(stderr, " %s %.2f", nm[i], hp[i] * 1e-3 / (i == 0 || i == 8 ? cq_launches : cq_passes));
+    std::fprintf(stderr, "\n");
   }
   return QT_OK;
 }

@@ -145,3 +145,33 @@ def test_sweep_kernel_equals_two_launch_round_fp32(engine, shape):
     for U, S, Vh, kk in ((U0, S0, V0, k0), (U1, S1, V1, k1)):
         err = np.linalg.norm((U * S) @ Vh - M32)
         assert err <= 1.1 * np.sqrt(np.sum(ref[kk:] ** 2)) + floor, (err, floor)
+
+
+@pytest.mark.parametrize("chi", [200, 512])
+def test_cluster_cholqr_equals_four_kernel_passes(engine, monkeypatch, chi):
+    """The sketch basis orthonormalised by the one-launch cluster CholeskyQR
+    (the block's rows in the shared memory of 8 CTAs) and by the four-kernel
+    passes (QT_CHOLQR_CLUSTER=0) gives the same truncation of a rank-deficient
+    theta' at the chi cap: same rank, error within 1.1x of the exact SVD's,
+    values within 1e-4 of the largest.  chi = 200 sketches 264 columns (a
+    last block of 8) over 400 rows (CTAs of 64 rows, the last ones padded)."""
+    import oracle as O
+    rng = np.random.default_rng(5 * chi)
+    a, b, _ = O.decay_theta_factors(chi, rng, 0.97)
+    g = O.haar_unitary(rng)
+    th = O.apply_gate_to_theta(O.theta_of(a.astype(np.complex64).astype(complex), b.astype(np.complex64).astype(complex)),
+                               g, chi, chi).astype(np.complex64)
+    ref = np.linalg.svd(th.astype(complex), compute_uv=False)
+    exact = np.sqrt(np.sum(ref[chi:] ** 2))
+    out = []
+    for flag in ("1", "0"):
+        monkeypatch.setenv("QT_CHOLQR_CLUSTER", flag)
+        eng = engine.Engine(mode="chosen", tc_gemm=1)
+        U, S, Vh, k, _ = eng.truncated_svd(th, 1e-6, chi_max=chi, mode="chosen")
+        eng.close()
+        assert k == chi
+        err = np.linalg.norm((U * S) @ Vh - th.astype(complex))
+        assert err <= 1.1 * exact, (flag, err, exact)
+        assert np.abs(U.conj().T @ U - np.eye(k)).max() <= 1e-4
+        out.append(S[:k])
+    assert np.abs(out[0] - out[1]).max() <= 1e-4 * ref[0]
