@@ -202,7 +202,6 @@ __global__ void __launch_bounds__(256) apply_rinv_kernel(C* __restrict__ Y, int6
   }
 }
 
-constexpr int CQ_CS = 8;             // CTAs per cluster
 constexpr int CQ_LDY = BW + 2;       // row stride of the staged rows: 272 B, an odd number of 16-byte granules
 constexpr int CQ_TILES = 36;         // upper 4 x 4 tiles of the 32 x 32 Gram, tile (ti <= tj) at tj (tj+1)/2 + ti
 constexpr int CQ_E = CQ_TILES * 16;  // Gram entries held, e = 36 (4 (i & 3) + (j & 3)) + tile
@@ -242,13 +241,13 @@ __host__ __device__ constexpr size_t cq_smem_bytes(int nrb) {
 }
 
 // CholeskyQR passes of one FP32 block (m x b, b <= 32) in one launch: a
-// thread-block cluster of CQ_CS CTAs holds the block's rows in shared memory
+// thread-block cluster of CS CTAs holds the block's rows in shared memory
 // (CTA q: rows 32 NRB q .. 32 NRB (q+1) - 1, zero-padded), and each pass
 //   (A) forms the CTA's partial Gram: thread (row group g, upper 4 x 4 tile)
 //       sums its rows g, g + 7, ... in FP32 (about 37 products per entry);
 //   (B) adds the row groups in order in float-float;
 //   (C) reduce-scatter over the cluster through distributed shared memory:
-//       CTA q owns the entries e = q (mod CQ_CS) and adds the ranks in order;
+//       CTA q owns the entries e = q (mod CS) and adds the ranks in order;
 //   (D) every CTA gathers the summed Gram;
 //   (E) G (+ shift trace(G) on the diagonal) = R^H R and X = R^{-1} in FP32,
 //       blocked by 8 columns -- every CTA computes the same R and X from the
@@ -259,7 +258,7 @@ __host__ __device__ constexpr size_t cq_smem_bytes(int nrb) {
 // after the last pass.  Every CTA passes the same cluster barriers (two per
 // pass and one before leaving, so that no CTA exits while another may still
 // read its shared memory).
-template <int NRB>
+template <int NRB, int CS>
 __global__ void __launch_bounds__(256, 1) cholqr_cluster_kernel(float2* __restrict__ Y, int64_t m, int b, int npass,
                                                             double shift0, int* __restrict__ flags,
                                                             unsigned long long* __restrict__ phase_ns) {
@@ -343,13 +342,13 @@ __global__ void __launch_bounds__(256, 1) cholqr_cluster_kernel(float2* __restri
     cluster.sync();
     phase(3);  // row groups + barrier
     // (C) this CTA's entries summed over the cluster in rank order
-    if (crank + CQ_CS * t < CQ_E) {
-      const int e = crank + CQ_CS * t;
-      float4 v[CQ_CS];
+    if (crank + CS * t < CQ_E) {
+      const int e = crank + CS * t;
+      float4 v[CS];
 #pragma unroll
-      for (int q = 0; q < CQ_CS; q++) v[q] = cluster.map_shared_rank(gp, q)[e];
+      for (int q = 0; q < CS; q++) v[q] = cluster.map_shared_rank(gp, q)[e];
 #pragma unroll
-      for (int q = 1; q < CQ_CS; q++) v[0] = ff4_add(v[0], v[q]);
+      for (int q = 1; q < CS; q++) v[0] = ff4_add(v[0], v[q]);
       Gr[e] = v[0];
     }
     cluster.sync();
@@ -360,7 +359,7 @@ __global__ void __launch_bounds__(256, 1) cholqr_cluster_kernel(float2* __restri
 #pragma unroll
       for (int u = 0; u < 3; u++) {
         const int e = t + 256 * u;
-        if (e < CQ_E) v[u] = cluster.map_shared_rank(Gr, e % CQ_CS)[e];
+        if (e < CQ_E) v[u] = cluster.map_shared_rank(Gr, e % CS)[e];
       }
 #pragma unroll
       for (int u = 0; u < 3; u++) {
@@ -533,69 +532,83 @@ __global__ void __launch_bounds__(256, 1) cholqr_cluster_kernel(float2* __restri
 }
 
 typedef void (*cq_kernel_t)(float2*, int64_t, int, int, double, int*, unsigned long long*);
-cq_kernel_t cq_kernel(int nrb) {
-  switch (nrb) {
-    case 1: return cholqr_cluster_kernel<1>;
-    case 2: return cholqr_cluster_kernel<2>;
-    case 4: return cholqr_cluster_kernel<4>;
-    default: return cholqr_cluster_kernel<8>;
-  }
-}
-
-// Row blocks (of 32) per CTA of the cluster CholeskyQR for m rows (0: the
-// block does not fit and the four-kernel passes are used).
-// QT_CHOLQR_CLUSTER=0 disables it.
-int cq_nrb(int64_t m) {
-  static int ok = -1;
-  if (ok < 0) {
-    ok = 1;
-    for (int nrb = 1; nrb <= 8 && ok; nrb *= 2) {
-      const size_t smem = cq_smem_bytes(nrb);
-      ok = 0;
-      if (cudaFuncSetAttribute(cq_kernel(nrb), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) ==
-          cudaSuccess) {
-        cudaLaunchConfig_t lc = {};
-        lc.gridDim = dim3(CQ_CS);
-        lc.blockDim = dim3(256);
-        lc.dynamicSmemBytes = smem;
-        cudaLaunchAttribute attr[1];
-        attr[0].id = cudaLaunchAttributeClusterDimension;
-        attr[0].val.clusterDim.x = CQ_CS;
-        attr[0].val.clusterDim.y = 1;
-        attr[0].val.clusterDim.z = 1;
-        lc.attrs = attr;
-        lc.numAttrs = 1;
-        int nc = 0;
-        if (cudaOccupancyMaxActiveClusters(&nc, cq_kernel(nrb), &lc) == cudaSuccess && nc > 0) ok = 1;
-      }
+cq_kernel_t cq_kernel(int nrb, int cs) {
+  if (cs == 16) {
+    switch (nrb) {
+      case 1: return cholqr_cluster_kernel<1, 16>;
+      case 2: return cholqr_cluster_kernel<2, 16>;
+      case 4: return cholqr_cluster_kernel<4, 16>;
+      default: return cholqr_cluster_kernel<8, 16>;
     }
-    cudaGetLastError();
   }
-  const char* env = std::getenv("QT_CHOLQR_CLUSTER");
-  if (!ok || (env && env[0] == '0')) return 0;
-  for (int nrb = 1; nrb <= 8; nrb *= 2)
-    if ((int64_t)CQ_CS * 32 * nrb >= m) return nrb;
-  return 0;
+  switch (nrb) {
+    case 1: return cholqr_cluster_kernel<1, 8>;
+    case 2: return cholqr_cluster_kernel<2, 8>;
+    case 4: return cholqr_cluster_kernel<4, 8>;
+    default: return cholqr_cluster_kernel<8, 8>;
+  }
 }
 
-int block_cholqr_cluster(qt_handle* h, float2* Yb, int64_t m, int b, int nrb, int npass, bool shifted,
-                         unsigned long long* phase_ns) {
-  const double shift = shifted ? 11.0 * ((double)m * b + (double)b * (b + 1)) * 5.96e-8 : 0.0;
+cudaLaunchConfig_t cq_config(int nrb, int cs, cudaLaunchAttribute* attr) {
   cudaLaunchConfig_t lc = {};
-  lc.gridDim = dim3(CQ_CS);
+  lc.gridDim = dim3(cs);
   lc.blockDim = dim3(256);
   lc.dynamicSmemBytes = cq_smem_bytes(nrb);
-  lc.stream = h->stream;
-  cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeClusterDimension;
-  attr[0].val.clusterDim.x = CQ_CS;
+  attr[0].val.clusterDim.x = cs;
   attr[0].val.clusterDim.y = 1;
   attr[0].val.clusterDim.z = 1;
   lc.attrs = attr;
   lc.numAttrs = 1;
+  return lc;
+}
+
+// Shape of the cluster CholeskyQR for m rows: *cs CTAs of 32 nrb rows, the
+// largest cluster the GPU schedules (16, else 8) for m > 256, then the fewest
+// rows per CTA; nrb = 0 when the block does not fit (m > 16 * 256, or no
+// cluster launch) and the four-kernel passes are used.  QT_CHOLQR_CLUSTER=0
+// disables it, QT_CHOLQR_CLUSTER=8 keeps clusters of 8.
+int cq_shape(int64_t m, int* cs) {
+  static int ok[2] = {-1, -1};  // cluster sizes 8 and 16 launchable for every nrb
+  if (ok[0] < 0) {
+    for (int ci = 0; ci < 2; ci++) {
+      const int c = ci ? 16 : 8;
+      ok[ci] = 1;
+      for (int nrb = 1; nrb <= 8 && ok[ci]; nrb *= 2) {
+        ok[ci] = 0;
+        cq_kernel_t k = cq_kernel(nrb, c);
+        if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cq_smem_bytes(nrb)) !=
+            cudaSuccess)
+          continue;
+        if (c == 16 && cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess)
+          continue;
+        cudaLaunchAttribute attr[1];
+        cudaLaunchConfig_t lc = cq_config(nrb, c, attr);
+        int nc = 0;
+        if (cudaOccupancyMaxActiveClusters(&nc, k, &lc) == cudaSuccess && nc > 0) ok[ci] = 1;
+      }
+      cudaGetLastError();
+    }
+  }
+  const char* env = std::getenv("QT_CHOLQR_CLUSTER");
+  if (env && env[0] == '0') return 0;
+  const bool keep8 = env && env[0] == '8';
+  *cs = (ok[1] && !keep8 && m > 256) ? 16 : (ok[0] ? 8 : 0);
+  if (*cs == 0) return 0;
+  for (int nrb = 1; nrb <= 8; nrb *= 2)
+    if ((int64_t)(*cs) * 32 * nrb >= m) return nrb;
+  return 0;
+}
+
+int block_cholqr_cluster(qt_handle* h, float2* Yb, int64_t m, int b, int nrb, int cs, int npass, bool shifted,
+                         unsigned long long* phase_ns) {
+  const double shift = shifted ? 11.0 * ((double)m * b + (double)b * (b + 1)) * 5.96e-8 : 0.0;
+  cudaLaunchAttribute attr[1];
+  cudaLaunchConfig_t lc = cq_config(nrb, cs, attr);
+  lc.stream = h->stream;
   if (h->prof) qt_prof_before(h, "cholqr_cluster_kernel");
   const cudaError_t e =
-      cudaLaunchKernelEx(&lc, cq_kernel(nrb), Yb, m, b, npass, shift, h->d_flags, phase_ns);
+      cudaLaunchKernelEx(&lc, cq_kernel(nrb, cs), Yb, m, b, npass, shift, h->d_flags, phase_ns);
   if (h->prof) qt_prof_after(h);
   h->launches++;
   if (e != cudaSuccess) return qt_fail(h, QT_ECUDA, std::string("launch cholqr_cluster_kernel: ") + cudaGetErrorString(e));
@@ -779,13 +792,13 @@ int qt_orthonormalize(qt_handle* h, C* Y, int64_t m, int64_t l) {
   QT_TRY(s.get(&dG, 2 * BW * BW));
   QT_TRY(s.get(&coef, (size_t)l * BW));
   QT_TRY(s.get(&part, (size_t)nchunk * lpad * BW));
-  int nrb = 0;
+  int nrb = 0, cs = 0;
   unsigned long long* phase_ns = nullptr;
   // QT_CHOLQR_PHASES=1 prints the average SM cycles per phase of the
   // cluster CholeskyQR (CTA 0's clock) after each orthonormalisation
   static const bool phases = std::getenv("QT_CHOLQR_PHASES") != nullptr;
   if constexpr (std::is_same<C, float2>::value) {
-    nrb = cq_nrb(m);
+    nrb = cq_shape(m, &cs);
     if (nrb > 0 && phases) {
       QT_TRY(s.get(&phase_ns, 16));
       QT_CHECK_CUDA(h, cudaMemsetAsync(phase_ns, 0, 16 * sizeof(unsigned long long), h->stream));
@@ -801,13 +814,13 @@ int qt_orthonormalize(qt_handle* h, C* Y, int64_t m, int64_t l) {
         // cluster launch: shifted, (projection,) plain, plain
         if (j0 > 0) {
           QT_TRY(block_project<C>(h, Y, m, (int)j0, Yb, b, part, coef));
-          QT_TRY(block_cholqr_cluster(h, Yb, m, b, nrb, 1, true, phase_ns));
+          QT_TRY(block_cholqr_cluster(h, Yb, m, b, nrb, cs, 1, true, phase_ns));
           QT_TRY(block_project<C>(h, Y, m, (int)j0, Yb, b, part, coef));
-          QT_TRY(block_cholqr_cluster(h, Yb, m, b, nrb, 2, false, phase_ns));
+          QT_TRY(block_cholqr_cluster(h, Yb, m, b, nrb, cs, 2, false, phase_ns));
           cq_launches += 2;
           cq_passes += 3;
         } else {
-          QT_TRY(block_cholqr_cluster(h, Yb, m, b, nrb, 3, true, phase_ns));
+          QT_TRY(block_cholqr_cluster(h, Yb, m, b, nrb, cs, 3, true, phase_ns));
           cq_launches += 1;
           cq_passes += 3;
         }
@@ -828,8 +841,8 @@ int qt_orthonormalize(qt_handle* h, C* Y, int64_t m, int64_t l) {
     QT_CHECK_CUDA(h, cudaMemcpy(hp, phase_ns, sizeof(hp), cudaMemcpyDeviceToHost));
     const char* nm[9] = {"stage", "gram", "groups+barrier", "scatter+barrier", "gather", "cholesky", "inverse",
                          "update", "writeback+barrier"};
-    std::fprintf(stderr, "cluster CholeskyQR, %d launches, %d passes; SM kilocycles per launch (stage, writeback) "
-                 "or pass:", cq_launches, cq_passes);
+    std::fprintf(stderr, "cluster CholeskyQR (%d CTAs of %d rows), %d launches, %d passes; SM kilocycles per "
+                 "launch (stage, writeback) or pass:", cs, 32 * nrb, cq_launches, cq_passes);
     for (int i = 0; i < 9; i++)
       std::fprintf(stderr, " %s %.2f", nm[i], hp[i] * 1e-3 / (i == 0 || i == 8 ? cq_launches : cq_passes));
     std::fprintf(stderr, "\n");
