@@ -404,11 +404,14 @@ __global__ void __launch_bounds__(256, 1) cholqr_cluster_kernel(float2* __restri
 #pragma unroll
           for (int r = 0; r < 8; r++)
             c[r] = (col < BW && k0 + r <= col) ? Gl[(k0 + r) * CQ_RS + col] : make_float2(0.f, 0.f);
+          // dn: the next pivot as seen by its own lane (lane kk + 1 holds
+          // R[k][k + 1] itself), so the pivot chain needs no row shuffle
+          float dn = c[0].x;
 #pragma unroll
           for (int kk = 0; kk < 8; kk++) {
             const int k = k0 + kk;
             if (k < b) {
-              float d = __shfl_sync(0xffffffffu, c[0].x, kk);
+              float d = __shfl_sync(0xffffffffu, dn, kk);
               if (!(d > 0.f)) {
                 if (lane == 0 && crank == 0) atomicOr(&flags[QT_FLAG_CHOL], 1);
                 d = trs[0];
@@ -416,6 +419,7 @@ __global__ void __launch_bounds__(256, 1) cholqr_cluster_kernel(float2* __restri
               const float y = rsqrtf(d);
               const float2 rk =
                   lane == kk ? make_float2(d * y, 0.f) : (lane > kk ? cscale(c[0], y) : make_float2(0.f, 0.f));
+              dn = c[1].x - (rk.x * rk.x + rk.y * rk.y);
               if (col < BW) Gl[k * CQ_RS + col] = rk;  // row k of R (zeros left of the diagonal)
               if (lane == 0) Ry[k] = y;
 #pragma unroll
@@ -429,14 +433,17 @@ __global__ void __launch_bounds__(256, 1) cholqr_cluster_kernel(float2* __restri
           }
         }
         __syncthreads();
-        const int base = k0 + 8, n2 = BW - base;
-        for (int e = t; e < n2 * n2; e += 256) {
-          const int i = base + e / n2, j = base + e % n2;
-          if (i <= j) {
-            float2 v = Gl[i * CQ_RS + j];
+        // trailing upper triangle: warp w the rows k0 + 8 + w, + 16, ...;
+        // lane j column j (two partial sums)
+        for (int i = k0 + 8 + w; i < BW; i += 8) {
+          if (lane >= i) {
+            float2 v0 = Gl[i * CQ_RS + lane], v1 = make_float2(0.f, 0.f);
 #pragma unroll
-            for (int q = 0; q < 8; q++) v = csub(v, cmul(cconj(Gl[(k0 + q) * CQ_RS + i]), Gl[(k0 + q) * CQ_RS + j]));
-            Gl[i * CQ_RS + j] = v;
+            for (int q = 0; q < 8; q += 2) {
+              v0 = csub(v0, cmul(cconj(Gl[(k0 + q) * CQ_RS + i]), Gl[(k0 + q) * CQ_RS + lane]));
+              v1 = csub(v1, cmul(cconj(Gl[(k0 + q + 1) * CQ_RS + i]), Gl[(k0 + q + 1) * CQ_RS + lane]));
+            }
+            Gl[i * CQ_RS + lane] = cadd(v0, v1);
           }
         }
         __syncthreads();
