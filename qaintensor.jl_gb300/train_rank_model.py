@@ -94,6 +94,7 @@ def main():
     ap.add_argument("--epochs", type=int, default=200)
     ap.add_argument("--seed", type=int, default=2026)
     ap.add_argument("--out", default=os.path.join(HERE, "rank_model_params.npy"))
+    ap.add_argument("--log", default="", help="also save the logged (features, rank) samples to this .npz")
     args = ap.parse_args()
     import __graft_entry__ as g
     qt = g.load_package()
@@ -116,7 +117,8 @@ def main():
                "epochs": args.epochs, "seed": args.seed, "circuits": args.circuits, "bonds": args.bonds}
     with open(os.path.join(HERE, "rank_model_train.json"), "w") as f:
         json.dump(summary, f, indent=1)
-    np.savez_compressed(os.path.join(ROOT, "gpurun_out", "rank_log.npz"), X=X, Y=Y)
+    if args.log:
+        np.savez_compressed(args.log, X=X, Y=Y)
     print(json.dumps(summary))
     eng.close()
 
