@@ -1,7 +1,9 @@
-"""Run the workload configurations of the benchmark plan on the GPU and print
-one JSON object per configuration (seeded synthetic inputs throughout).
+"""Run the workload configurations of the benchmark plan and print one JSON
+object per configuration (seeded synthetic inputs throughout).  The script
+sits with the tests because the oracle is its checker.
 
-    python qaintensor.jl_gb300/run_configs.py c1 c2 c4 c5 [--c3-depth 20] [--c4-circuits 4096]
+    python tests/run_configs.py c1 c2 c4 c5 [--c3-depth 20] [--c4-circuits 4096]
+    python tests/run_configs.py cpu [--cpu-reps 5]        (no GPU needed)
 
 c1  12-qubit brickwork, depth 8, Haar gates, cutoff 1e-10, chi_max 32, plain
     FP64: ranks and <Z_1> against the FP64 oracle, amplitudes against the dense
@@ -18,6 +20,11 @@ c5  40-site TFIM MPO (J=1, h ~ U[0.5,1.5]) applied 10 times to a random
     normalised chi=512 complex64 MPS, each followed by a compression sweep to
     chi 512 at cutoff 1e-9 and a renormalisation: <H> against an FP64 device
     run (cuSOLVER splits) on the same inputs, wall time.
+cpu the CPU restatement of the reference path (the oracle's update: theta,
+    gate fold, gesdd, tail rule) at chi in {64, 256, 1024} on the c2 inputs,
+    complex128 (the oracle itself) and complex64 (the same steps in single
+    precision, cgesdd), with OpenBLAS on all host threads and on one thread:
+    updates/s as the median of --cpu-reps timed updates after one warm-up.
 """
 
 from __future__ import annotations
@@ -238,6 +245,61 @@ def c5(qt, args):
     return res
 
 
+def _cpu_update(O, a, b, g, chi, dtype):
+    """One update of the oracle's path in `dtype`: for complex128 the oracle's
+    own apply_2q; for complex64 its steps with every array in complex64."""
+    if dtype == np.complex128:
+        sites = [a.copy(), b.copy()]
+        O.apply_2q(sites, g, 1, 1e-6, chi)
+        return sites[0], sites[1]
+    chil, chir = a.shape[0], b.shape[2]
+    th = O.theta_of(a, b)
+    t4 = th.reshape((chil, 2, 2, chir), order="F")
+    g4 = np.asarray(g, dtype=np.complex64).reshape((2, 2, 2, 2), order="F")
+    th = np.einsum("pqrs,arsb->apqb", g4, t4).reshape((2 * chil, 2 * chir), order="F")
+    u, s, vh = O.svd_gesdd(th)
+    k = min(O.tail_rank(s.astype(np.float64), 1e-6, clamp=True), chi)
+    a2 = u[:, :k].reshape((chil, 2, k), order="F")
+    b2 = (s[:k, None] * vh[:k, :]).reshape((k, 2, chir), order="F")
+    return a2, b2
+
+
+def cpu1(qt, args):
+    """Timings at the thread count this process was started with."""
+    import oracle as O
+    rows = []
+    for chi in args.c2_chis:
+        for dtype in (np.complex128, np.complex64):
+            rng = np.random.default_rng(chi)
+            a, b, _ = O.decay_theta_factors(chi, rng)
+            g = O.haar_unitary(rng)
+            a, b = a.astype(dtype), b.astype(dtype)
+            _cpu_update(O, a, b, g, chi, dtype)
+            ts = []
+            for _ in range(args.cpu_reps):
+                t0 = time.perf_counter()
+                _cpu_update(O, a, b, g, chi, dtype)
+                ts.append(time.perf_counter() - t0)
+            ts.sort()
+            med = ts[len(ts) // 2]
+            rows.append({"chi": chi, "dtype": "c128" if dtype == np.complex128 else "c64",
+                         "ms_per_update": 1e3 * med, "updates_per_s": 1.0 / med})
+    return {"config": "cpu1", "threads": os.environ.get("OPENBLAS_NUM_THREADS", "default"), "rows": rows}
+
+
+def cpu(qt, args):
+    """cpu1 in child processes with OpenBLAS on all host threads and on one."""
+    import subprocess
+    out = {"config": "cpu", "host_cores": os.cpu_count(), "runs": []}
+    for threads in (os.cpu_count(), 1):
+        env = dict(os.environ, OPENBLAS_NUM_THREADS=str(threads), OMP_NUM_THREADS=str(threads))
+        cmd = [sys.executable, os.path.abspath(__file__), "cpu1", "--cpu-reps", str(args.cpu_reps), "--c2-chis"] + \
+            [str(c) for c in args.c2_chis]
+        res = subprocess.run(cmd, env=env, capture_output=True, text=True, check=True)
+        out["runs"].append(json.loads(res.stdout.strip().splitlines()[-1]))
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("configs", nargs="+")
@@ -248,12 +310,15 @@ def main():
     ap.add_argument("--c4-check", type=int, default=24)
     ap.add_argument("--c5-chi", type=int, default=512)
     ap.add_argument("--c5-steps", type=int, default=10)
+    ap.add_argument("--cpu-reps", type=int, default=5)
     args = ap.parse_args()
-    import __graft_entry__ as g
-    qt = g.load_package()
+    qt = None
+    if any(c not in ("cpu", "cpu1") for c in args.configs):
+        import __graft_entry__ as g
+        qt = g.load_package()
     for c in args.configs:
         t0 = time.perf_counter()
-        r = {"c1": c1, "c2": c2, "c3": c3, "c4": c4, "c5": c5}[c](qt, args)
+        r = {"c1": c1, "c2": c2, "c3": c3, "c4": c4, "c5": c5, "cpu": cpu, "cpu1": cpu1}[c](qt, args)
         r["wall_seconds"] = time.perf_counter() - t0
         print(json.dumps(r), flush=True)
 
