@@ -1,13 +1,18 @@
 // Randomized-SVD helpers: Gaussian probes and the sketch orthogonalisation.
 //
 // The range finder (Halko, Martinsson and Tropp 2011, Alg. 4.1/4.4) needs an
-// orthonormal basis of Y = theta' Omega.  It is built by block classical
+// orthonormal basis of the sketch Y.  It is built by block classical
 // Gram-Schmidt with one re-orthogonalisation pass (BCGS2), each 32-column
-// block orthonormalised internally by CholeskyQR2 -- the first pass shifted
+// block orthonormalised by CholeskyQR passes -- the first one shifted
 // (Fukaya, Kannan, Nakatsukasa, Zhang, Yamamoto 2020) so that numerically
-// rank-deficient blocks still factor.  Block Gram matrices are accumulated in
-// FP64 from the stored values and factored in FP64; the basis itself is
-// stored in the element type of Y.
+// rank-deficient blocks still factor, and a third one for an FP32 basis.  The
+// basis is stored in the element type of Y.  Two CholeskyQR implementations:
+//   - FP32 blocks of up to 4096 rows: one thread-block cluster launch per run
+//     of passes (cholqr_cluster_kernel).  The block's rows stay in shared
+//     memory; the Gram is summed in FP32 tiles and float-float across row
+//     groups and CTAs, and R and R^{-1} are formed in FP32.
+//   - FP64 blocks and taller FP32 blocks: four launches per pass (the Gram in
+//     FP64 over many CTAs, a one-CTA Cholesky and inverse, the block update).
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
