@@ -812,14 +812,15 @@ int svd_split_chosen(qt_handle* h, float2* theta, int64_t m, int64_t n, double c
   // A rank predicted at the chi_max cap is pinned there by a spectrum that
   // is still decaying slowly at the cap; a sketch of cap + oversample then
   // misses the kept space by far more than the exact truncation does, so the
-  // sketch is widened to 1.25 x the cap.  With one power iteration that keeps
+  // sketch is widened to 1.125 x the cap.  With one power iteration that keeps
   // the truncation error within 1.0001 of the exact split at chi = 1024
-  // (1.1 x: 1.0011; no power iteration: 1.10), and the Jacobi on the
-  // sketched matrix, free of the FP32 noise columns of theta', settles in 5
-  // sweeps instead of ~20 on the whole theta'.
+  // (1152 columns: 1.00008; 1216: 1.00006; 1280: 1.00005; no power
+  // iteration at 1280: 1.10), and the Jacobi on the sketched matrix, free of
+  // the FP32 noise columns of theta', settles in 5 sweeps instead of ~20 on
+  // the whole theta'.
   const bool cap_bound = chi_max > 0 && chi_max < kmin && kpred > 0 && kpred + h->cfg.oversample >= 0.9 * chi_max;
   // (QT_CAP_SKETCH overrides the factor; tuning)
-  static const double cap_mult = std::getenv("QT_CAP_SKETCH") ? std::atof(std::getenv("QT_CAP_SKETCH")) : 1.25;
+  static const double cap_mult = std::getenv("QT_CAP_SKETCH") ? std::atof(std::getenv("QT_CAP_SKETCH")) : 1.125;
   // (and by at least 64 columns: at chi = 64 a sketch of 80 left 1.006 x)
   if (cap_bound) l = std::max<int64_t>(l, std::max<int64_t>((int64_t)(cap_mult * chi_max), chi_max + 64));
   l = ((l + 7) / 8) * 8;
