@@ -1,0 +1,71 @@
+"""The bench's N > 1 plumbing (replicas only: one process per GPU, no
+collective on the data path) as two gloo ranks on the CPU: the max and sum
+reductions every rank sees, the whole-job value (updates of all ranks over
+the slowest rank's time), per-rank inputs, and the reference arm that rank 0
+alone runs and prints."""
+import json
+import os
+import socket
+import subprocess
+import sys
+
+import pytest
+
+pytest.importorskip("torch")
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+WORKER = r"""
+import argparse, json, sys
+sys.path.insert(0, %(root)r)
+import bench
+d = bench.Dist()
+r = d.rank
+out = {"rank": r, "world": d.world, "max": d.max(float(r + 1)), "sum": d.sum(float(r + 1))}
+# timing as bench_ours aggregates it: 5 updates per rank, rank r took 100 (r + 1) ms
+out["value"] = d.sum(5) / (d.max(100.0 * (r + 1)) / 1e3)
+# per-rank inputs: the seeds bench_ours uses
+a0, _, _ = bench.decay_pair(4, 1001 + 2 * r)
+out["a0"] = [float(a0.real.sum()), float(a0.imag.sum())]
+line = bench.bench_reference(argparse.Namespace(chi=8, steps=2, warmup=1), d)
+out["ref"] = line
+d.barrier()
+d.close()
+print(json.dumps(out))
+"""
+
+
+def free_port():
+    with socket.socket(socket.AF_INET, socket.SOCK_STREAM) as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def test_two_gloo_ranks():
+    port = free_port()
+    procs = []
+    for r in range(2):
+        env = dict(os.environ, RANK=str(r), WORLD_SIZE="2", LOCAL_RANK=str(r), MASTER_ADDR="127.0.0.1",
+                   MASTER_PORT=str(port))
+        procs.append(subprocess.Popen([sys.executable, "-c", WORKER % {"root": ROOT}], env=env,
+                                      stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True))
+    res = []
+    for p in procs:
+        try:
+            out, err = p.communicate(timeout=180)
+        except subprocess.TimeoutExpired:
+            for q in procs:
+                q.kill()
+            raise
+        assert p.returncode == 0, err[-2000:]
+        res.append(json.loads(out.strip().splitlines()[-1]))
+    res.sort(key=lambda x: x["rank"])
+    for x in res:
+        assert x["world"] == 2
+        assert x["max"] == 2.0 and x["sum"] == 3.0
+        assert x["value"] == pytest.approx(10 / 0.2)  # 10 updates over the slower rank's 200 ms
+    assert res[0]["a0"] != res[1]["a0"]  # each replica runs its own inputs
+    ref = res[0]["ref"]
+    assert res[1]["ref"] is None  # the other ranks do no work in the reference arm
+    assert ref["impl"] == "reference" and ref["value"] > 0 and ref["steps"] == 2
+    assert ref["e2e"]["h2d_bytes_per_step"] == 0 and ref["cpu_baseline"]["kind"] == "port"
