@@ -171,39 +171,92 @@ def c3(qt, args):
             "sketched": sum(1 for s in stats if s["sketch_size"] > 0), "rank_model": model, "ZZ": zz}
 
 
-def c4(qt, args):
-    import oracle as O
-    rng = np.random.default_rng(4096)
-    nc = args.c4_circuits
+def c4_circuits(nc, rng):
+    """The ensemble: (qubits, depth, chi_max, brickwork gates) per circuit."""
     circuits = []
     for c in range(nc):
         n = int(rng.integers(8, 41))
         depth = int(rng.integers(4, 25))
         chi = int(rng.choice([16, 32, 64, 128]))
         circuits.append((n, depth, chi, brickwork(n, depth, rng)))
-    layers = [[] for _ in range(max(c[1] for c in circuits))]
-    for ci, (_, _, _, gates) in enumerate(circuits):
-        for (layer, w, g) in gates:
-            layers[layer - 1].append((ci, w, g))
+    return circuits
+
+
+def lpt_shards(costs, world):
+    """Circuits to ranks, longest estimated cost first, each to the least
+    loaded rank (ties to the lower rank).  Every rank computes the same
+    assignment from the same costs; returns each rank's sorted indices."""
+    order = sorted(range(len(costs)), key=lambda i: (-costs[i], i))
+    load = [0.0] * world
+    shards = [[] for _ in range(world)]
+    for i in order:
+        r = min(range(world), key=lambda q: (load[q], q))
+        shards[r].append(i)
+        load[r] += costs[i]
+    return [sorted(s) for s in shards]
+
+
+def gather_by_circuit(dist, idx, vals, nc):
+    """Every rank's per-circuit values in global circuit order (the one
+    collective of the sharded ensemble, after the timed region)."""
+    parts = [(idx, vals)]
+    if dist is not None and dist.world > 1:
+        parts = [None] * dist.world
+        dist.dist.all_gather_object(parts, (list(idx), list(vals)))
+    out = [None] * nc
+    for ids, vs in parts:
+        for i, v in zip(ids, vs):
+            out[i] = v
+    return out
+
+
+def c4(qt, args):
+    """The batched ensemble, sharded by circuit over the ranks when launched
+    with one process per GPU (RANK, WORLD_SIZE, LOCAL_RANK): each rank runs
+    its circuits on its own GPU with no collective in the timed region; the
+    rate is all ranks' updates over the slowest rank's time."""
+    import oracle as O
+    dist = getattr(args, "dist", None)
+    world, rank, local = (dist.world, dist.rank, dist.local) if dist is not None else (1, 0, 0)
+    rng = np.random.default_rng(4096)
+    nc = args.c4_circuits
+    circuits = c4_circuits(nc, rng)
+    # cost estimate: bond updates (depth (n-1)/2) times chi_max^3
+    mine = lpt_shards([c[1] * (c[0] - 1) / 2 * c[2] ** 3 for c in circuits], world)[rank]
+    layers = [[] for _ in range(max([circuits[ci][1] for ci in mine], default=0))]
+    for j, ci in enumerate(mine):
+        for (layer, w, g) in circuits[ci][3]:
+            layers[layer - 1].append((j, w, g))
     ntask = sum(len(l) for l in layers)
-    eng = qt.Engine(mode="chosen")
-    b = qt.Batch(eng, [c[0] for c in circuits], [c[2] for c in circuits])
+    eng = qt.Engine(mode="chosen", device=local)
+    b = qt.Batch(eng, [circuits[ci][0] for ci in mine], [circuits[ci][2] for ci in mine])
     b.run(layers, 1e-8, use_graph=True)  # capture + first run (warm-up)
     b.reset()
     eng.sync()
+    if dist is not None:
+        dist.barrier()
     t0 = time.perf_counter()
     b.replay()
+    eng.sync()
     dt = time.perf_counter() - t0
-    z = b.expect_z(1)
+    if dist is not None:
+        dt, ntask_all = dist.max(dt), int(dist.sum(ntask))
+    else:
+        ntask_all = ntask
+    z = gather_by_circuit(dist, mine, [float(v) for v in b.expect_z(1)], nc)
+    b.free()
+    eng.close()
     errs = []
-    for ci in rng.choice(nc, size=min(nc, args.c4_check), replace=False):
-        n, depth, chi, gates = circuits[ci]
-        if chi > 32 or n > 24:
-            continue
-        sites, _ = O.run_brickwork(n, gates, 1e-8, chi)
-        errs.append(abs(z[ci] - O.expect_z(sites, 1)))
-    return {"config": "c4", "circuits": nc, "updates": ntask, "seconds": dt, "updates_per_s": ntask / dt,
-            "Z1_err_max_sample": max(errs) if errs else None, "checked": len(errs)}
+    if rank == 0:
+        for ci in rng.choice(nc, size=min(nc, args.c4_check), replace=False):
+            n, depth, chi, gates = circuits[ci]
+            if chi > 32 or n > 24:
+                continue
+            sites, _ = O.run_brickwork(n, gates, 1e-8, chi)
+            errs.append(abs(z[ci] - O.expect_z(sites, 1)))
+    return {"config": "c4", "circuits": nc, "ranks": world, "updates": ntask_all, "seconds": dt,
+            "updates_per_s": ntask_all / dt, "Z1_err_max_sample": max(errs) if errs else None,
+            "checked": len(errs)}
 
 
 def c5(qt, args):
@@ -316,11 +369,22 @@ def main():
     if any(c not in ("cpu", "cpu1") for c in args.configs):
         import __graft_entry__ as g
         qt = g.load_package()
+    # one process per GPU (torchrun): only c4 shards; rank 0 prints
+    args.dist = None
+    if int(os.environ.get("WORLD_SIZE", "1")) > 1:
+        import bench
+        args.dist = bench.Dist()
+    rank = args.dist.rank if args.dist is not None else 0
     for c in args.configs:
+        if c != "c4" and rank != 0:
+            continue
         t0 = time.perf_counter()
         r = {"c1": c1, "c2": c2, "c3": c3, "c4": c4, "c5": c5, "cpu": cpu, "cpu1": cpu1}[c](qt, args)
         r["wall_seconds"] = time.perf_counter() - t0
-        print(json.dumps(r), flush=True)
+        if rank == 0:
+            print(json.dumps(r), flush=True)
+    if args.dist is not None:
+        args.dist.close()
 
 
 if __name__ == "__main__":

@@ -1,8 +1,11 @@
-"""The bench's N > 1 plumbing (replicas only: one process per GPU, no
-collective on the data path) as two gloo ranks on the CPU: the max and sum
-reductions every rank sees, the whole-job value (updates of all ranks over
-the slowest rank's time), per-rank inputs, and the reference arm that rank 0
-alone runs and prints."""
+"""The N > 1 plumbing as two gloo ranks on the CPU (one process per GPU, no
+collective on the data path):
+- bench.py: the max and sum reductions every rank sees, the whole-job value
+  (updates of all ranks over the slowest rank's time), per-rank inputs, and
+  the reference arm that rank 0 alone runs and prints;
+- the sharded batched ensemble of tests/run_configs.py (c4): the
+  circuit-to-rank assignment, the summed update count and the final gather
+  of per-circuit values, with a stand-in engine in place of the GPU."""
 import json
 import os
 import socket
@@ -69,3 +72,76 @@ def test_two_gloo_ranks():
     assert res[1]["ref"] is None  # the other ranks do no work in the reference arm
     assert ref["impl"] == "reference" and ref["value"] > 0 and ref["steps"] == 2
     assert ref["e2e"]["h2d_bytes_per_step"] == 0 and ref["cpu_baseline"]["kind"] == "port"
+
+
+C4_WORKER = r"""
+import argparse, json, sys, types
+import numpy as np
+sys.path.insert(0, %(root)r)
+sys.path.insert(0, %(tests)r)
+import bench
+import run_configs as R
+d = bench.Dist()
+
+class Engine:
+    def __init__(self, mode, device=0):
+        self.device = device
+    def sync(self):
+        pass
+    def close(self):
+        pass
+
+class Batch:
+    def __init__(self, eng, nqubits, chi_max):
+        self.nq = list(nqubits)
+    def run(self, layers, cutoff, use_graph=True):
+        self.ntask = sum(len(l) for l in layers)
+    def reset(self):
+        pass
+    def replay(self):
+        pass
+    def expect_z(self, i):
+        return np.asarray(self.nq, dtype=float)  # stand-in value per circuit: its qubit count
+    def free(self):
+        pass
+
+nc = 40
+res = R.c4(types.SimpleNamespace(Engine=Engine, Batch=Batch), argparse.Namespace(c4_circuits=nc, c4_check=0, dist=d))
+circuits = R.c4_circuits(nc, np.random.default_rng(4096))
+costs = [c[1] * (c[0] - 1) / 2 * c[2] ** 3 for c in circuits]
+shards = R.lpt_shards(costs, d.world)
+z = R.gather_by_circuit(d, shards[d.rank], [float(circuits[i][0]) for i in shards[d.rank]], nc)
+d.close()
+print(json.dumps({"rank": d.rank, "res": res, "shards": shards, "z": z, "n": [c[0] for c in circuits],
+                  "tasks": sum(len(c[3]) for c in circuits), "costs": costs}))
+"""
+
+
+def test_sharded_ensemble_two_gloo_ranks():
+    port = free_port()
+    procs = []
+    for r in range(2):
+        env = dict(os.environ, RANK=str(r), WORLD_SIZE="2", LOCAL_RANK=str(r), MASTER_ADDR="127.0.0.1",
+                   MASTER_PORT=str(port))
+        procs.append(subprocess.Popen([sys.executable, "-c", C4_WORKER % {"root": ROOT, "tests": os.path.join(ROOT, "tests")}],
+                                      env=env, stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True))
+    res = []
+    for p in procs:
+        try:
+            out, err = p.communicate(timeout=180)
+        except subprocess.TimeoutExpired:
+            for q in procs:
+                q.kill()
+            raise
+        assert p.returncode == 0, err[-2000:]
+        res.append(json.loads(out.strip().splitlines()[-1]))
+    res.sort(key=lambda x: x["rank"])
+    shards = res[0]["shards"]
+    assert shards == res[1]["shards"]  # every rank computes the same assignment
+    assert sorted(shards[0] + shards[1]) == list(range(40))  # disjoint, complete
+    load = [sum(res[0]["costs"][i] for i in s) for s in shards]
+    assert max(load) - min(load) <= max(res[0]["costs"])  # LPT: within one circuit of balance
+    for x in res:
+        assert x["res"]["ranks"] == 2
+        assert x["res"]["updates"] == x["tasks"]  # the ranks' update counts add up to the ensemble's
+        assert x["z"] == [float(n) for n in x["n"]]  # the gather puts every circuit's value in its place
