@@ -23,6 +23,8 @@ __all__ = [
     "switch_wires", "switch_pairs", "permute_mps", "mpo_from_matrix", "decompose",
     "extend_mpo", "apply_mpo", "apply_mpo_matrix", "tensor_circuit", "apply_statevector",
     "is_power_two",
+    "shift_pair",
+    "shift_summation",
 ]
 
 
@@ -60,6 +62,16 @@ class Network:
 def is_power_two(i: int) -> bool:
     """src/helper.jl:24-27."""
     return i != 0 and (i & (i - 1)) == 0
+
+
+def shift_pair(p: Tuple[int, int], step: int) -> Tuple[int, int]:
+    """src/helper.jl:15-17: the (tensor, leg) pair with the tensor moved by step."""
+    return (p[0] + step, p[1])
+
+
+def shift_summation(s: "Summation", step: int) -> "Summation":
+    """src/helper.jl:6-8: both pairs of a contraction shifted by step."""
+    return Summation([shift_pair(s.idx[i], step) for i in range(2)])
 
 
 # --------------------------------------------------------------------------
@@ -565,14 +577,12 @@ def apply_mpo(psi: Network, mpo: Network, iwire: Sequence[int]) -> Network:
     # own bonds carry it across non-adjacent wires.
     out = Network(list(psi.tensors) + list(mpo.tensors),
                   [Summation(list(s.idx)) for s in psi.contractions]
-                  + [Summation([(a + step, b) for (a, b) in s.idx]) for s in mpo.contractions],
+                  + [shift_summation(s, step) for s in mpo.contractions],
                   list(psi.openidx), "general")
     for i, w in enumerate(iwire, 1):
-        t, leg = mpo.openidx[i + N - 1]
-        out.contractions.append(Summation([psi.openidx[w - 1], (t + step, leg)]))
+        out.contractions.append(Summation([psi.openidx[w - 1], shift_pair(mpo.openidx[i + N - 1], step)]))
     for i, q in enumerate(iwire, 1):
-        t, leg = mpo.openidx[i - 1]
-        out.openidx[q - 1] = (t + step, leg)
+        out.openidx[q - 1] = shift_pair(mpo.openidx[i - 1], step)
     return out
 
 
