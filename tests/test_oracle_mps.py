@@ -120,6 +120,18 @@ def test_open_closed_mps_and_exceptions():
         O.ClosedMPS([T3, T1, T2])
 
 
+def test_copy_is_independent():
+    # test/test_mps.jl:275-288: a copy equals the original, and replacing a
+    # tensor of the original leaves the copy alone
+    rng = np.random.default_rng(12)
+    mps = O.ClosedMPS([rng.random((2, 5)), rng.random((5, 2, 3)), rng.random((3, 2))])
+    cp = mps.copy()
+    assert all(np.array_equal(x, y) for x, y in zip(cp.tensors, mps.tensors))
+    assert cp.contractions == mps.contractions and cp.openidx == mps.openidx
+    mps.tensors[0] = rng.random((2, 5))
+    assert not np.array_equal(mps.tensors[0], cp.tensors[0])
+
+
 @pytest.mark.parametrize("seed", [7, 8, 9])
 def test_permute_mps(seed):
     # test/test_mps.jl:157-174
