@@ -120,6 +120,14 @@ def test_open_closed_mps_and_exceptions():
         O.ClosedMPS([T3, T1, T2])
 
 
+def test_single_tensor_network_contracts_to_itself():
+    # test/test_tensor_circuit.jl:21-31: one tensor, both legs open
+    rng = np.random.default_rng(13)
+    t = rng.standard_normal((2, 6)) + 1j * rng.standard_normal((2, 6))
+    net = O.Network([t], [], [(1, 1), (1, 2)])
+    np.testing.assert_allclose(O.contract(net), t, rtol=0, atol=1e-15)
+
+
 def test_copy_is_independent():
     # test/test_mps.jl:275-288: a copy equals the original, and replacing a
     # tensor of the original leaves the copy alone
