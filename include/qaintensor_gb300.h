@@ -50,9 +50,12 @@ typedef enum { QT_C64 = 0, QT_C128 = 1 } qt_dtype;
 
 typedef enum {
   QT_MODE_PLAIN = 0,     /* FP64 everywhere: FP64 GEMM + exact FP64 one-sided Jacobi SVD */
-  QT_MODE_CHOSEN = 1,    /* FP32-level products, randomized SVD sized by the rank
-                            predictor, FP64 orthogonalisation / small SVD / tail sums;
-                            exact FP64 SVD as fallback */
+  QT_MODE_CHOSEN = 1,    /* complex64: FP32-level products (tcgen05 split-TF32x3),
+                            randomized range finder sized by the rank predictor,
+                            FP32-storage Jacobi split with FP64 norms and tail sums;
+                            the exact FP64 split as fallback, also whenever the rank
+                            decision at the caller's cutoff lies below the FP32
+                            resolution and no certificate holds (qt_cert_counters) */
   QT_MODE_CUSOLVER = 2   /* cross-check: FP64 GEMM + cuSOLVER zgesvd (library) */
 } qt_mode;
 
@@ -67,8 +70,9 @@ typedef struct {
   int use_rank_model;      /* size the sketch with the learned-rank MLP when trained */
   int max_sweeps;          /* Jacobi sweep limit */
   double jacobi_tol;       /* Jacobi orthogonality tolerance (relative) */
-  double noise_floor;      /* chosen mode: tail norms below noise_floor*||theta|| are
-                              below the FP32-level arithmetic and are not resolved */
+  double noise_floor;      /* chosen mode: resolution of the FP32-level split relative to
+                              ||theta||_F (0: 4 sqrt(max(m, n)) 2^-24); a cutoff below it is
+                              honoured through a certificate or the exact FP64 split */
   uint64_t seed;           /* sketch RNG seed */
   int tc_gemm;             /* chosen mode: 1 = tcgen05 split-TF32x3 products, 0 = FP32 SIMT */
   int jacobi_kernel;       /* Jacobi round: 0 = automatic (FP32 storage: one cooperative launch per
@@ -78,6 +82,8 @@ typedef struct {
                               memory), 1 = three kernels (Gram partials, pair solver, rotation),
                               2 = the one-launch cluster round, 3 = FP32 two launches per round
                               (Gram + pair solver, then rotation) */
+  double cap_sketch;       /* chosen mode: sketch width of a rank pinned at the chi_max cap, as a
+                              multiple of chi_max (0: 1.125; the autotuner chooses it per chi_max) */
 } qt_config;
 
 typedef struct {
@@ -114,6 +120,15 @@ int64_t qt_launch_count(const qt_handle* h);
  * (every column of X once per round), out[7] bytes of X and V columns
  * written by rotations (out holds 8 doubles). */
 int qt_work_counters(const qt_handle* h, double* out);
+
+/* Chosen-mode rank decisions issued by this handle since creation (no
+ * counterpart in the reference), out[4]: [0] decided by the exact FP64
+ * fallback (no certificate), [1] cutoff at or above the FP32 resolution,
+ * [2] certified by the chi_max cap (the computed tail beyond chi_max exceeds
+ * cutoff + resolution), [3] certified by the exact rank bound (exactly as
+ * many values above the resolution as the gate's operator-Schmidt rank times
+ * the inner bond or the Hilbert-space dimensions allow). */
+int qt_cert_counters(const qt_handle* h, int64_t* out);
 
 /* ---- measurement helpers ------------------------------------------------ */
 /* CUDA events on the handle's stream: record into slot 0..7, elapsed a -> b. */
@@ -158,8 +173,9 @@ int qt_gemm(qt_handle* h, int dtype, int opA, int opB, int64_t M, int64_t N, int
  * svd() calls at src/svd.jl:26-27, src/switch.jl (svd of the swapped pair),
  * src/mps.jl:63,73, src/mpo.jl:53,62, src/decompose.jl:26,38.
  * mode PLAIN: FP64 one-sided Jacobi; CUSOLVER: zgesvd; CHOSEN with a
- * complex64 M: FP32-storage Jacobi, cutoff floored at 4 sqrt(max(m,n))
- * 5.96e-8 ||M||_F (values below are FP32 rounding noise). */
+ * complex64 M: FP32-storage Jacobi when the cutoff is at or above its
+ * resolution 4 sqrt(max(m,n)) 5.96e-8 ||M||_F or the chi_max cap decides the
+ * rank, the exact FP64 split otherwise. */
 int qt_truncated_svd(qt_handle* h, int dtype, int64_t m, int64_t n, const void* M,
                      double cutoff, int chi_max, int mode,
                      void* U, double* S, void* Vh, int* k, double* discarded);
@@ -268,8 +284,10 @@ int qt_rank_features_of(const qt_mps* mps, int site, const double* G, double cut
  * (circuit, site, gate) tasks; tasks of one layer must touch disjoint sites.
  * Each layer runs as one persistent kernel whose CTAs take tasks from a
  * device counter (mixed precision: FP32 products and Jacobi, FP64 norms and
- * tail rule, effective cutoff max(cutoff, floor ||theta'||)); the whole
- * program is captured in one CUDA graph when use_graph is set. */
+ * tail rule at the caller's cutoff; a rank decision below the FP32 resolution
+ * that neither the cap nor the exact rank bound certifies is redone as an
+ * FP64 split by the same CTA); the whole program is captured in one CUDA
+ * graph when use_graph is set. */
 int qt_batch_create(qt_handle* h, int ncirc, const int* nqubits, const int* chi_max, qt_batch** out);
 int qt_batch_free(qt_handle* h, qt_batch* b);
 int qt_batch_run(qt_handle* h, qt_batch* b, int nlayers, const int* layer_start, const int* circ, const int* site,
@@ -277,6 +295,15 @@ int qt_batch_run(qt_handle* h, qt_batch* b, int nlayers, const int* layer_start,
 int qt_batch_replay(qt_handle* h, qt_batch* b);
 int qt_batch_reset(qt_handle* h, qt_batch* b);
 int qt_batch_task_stats(qt_handle* h, const qt_batch* b, int* rank, int* sweeps, float* discarded);
+/* Launch shape of the persistent layer kernel for circuits whose bond cap
+ * lies in the bucket bucket_cap (16: caps <= 16, 32, 64, 128): threads per CTA
+ * (128, 256 or 512) and CTAs per SM (1 to 4).  A program runs one launch per
+ * layer and bucket; set the shapes before qt_batch_run (the graph captures
+ * them).  Defaults 256 threads, 1 CTA per SM; the autotuner chooses them. */
+int qt_batch_set_launch(qt_handle* h, qt_batch* b, int bucket_cap, int threads, int ctas_per_sm);
+int qt_batch_get_launch(const qt_batch* b, int bucket_cap, int* threads, int* ctas_per_sm);
+/* Rank decisions of the last program's tasks by certificate, as qt_cert_counters. */
+int qt_batch_cert_counts(qt_handle* h, const qt_batch* b, int64_t* out /* 4 */);
 int qt_batch_bond_dims(qt_handle* h, const qt_batch* b, int circ, int* dims /* nqubits + 1 */);
 int qt_batch_download_site(qt_handle* h, const qt_batch* b, int circ, int site, void* host);
 int qt_batch_expect_z(qt_handle* h, qt_batch* b, int site, double* out /* one per circuit */);

@@ -58,12 +58,15 @@ class EngineError(RuntimeError):
         self.code = code
 
 
+CERT_NAMES = ("fallback", "resolved", "cap", "struct")
+
+
 class QtConfig(C.Structure):
     _fields_ = [("device", C.c_int), ("mode", C.c_int), ("cutoff", C.c_double), ("chi_max", C.c_int),
                 ("oversample", C.c_int), ("power_iters", C.c_int), ("renormalize", C.c_int),
                 ("use_rank_model", C.c_int), ("max_sweeps", C.c_int), ("jacobi_tol", C.c_double),
                 ("noise_floor", C.c_double), ("seed", C.c_uint64), ("tc_gemm", C.c_int),
-                ("jacobi_kernel", C.c_int)]
+                ("jacobi_kernel", C.c_int), ("cap_sketch", C.c_double)]
 
 
 class QtUpdateStats(C.Structure):
@@ -95,6 +98,7 @@ def library() -> C.CDLL:
         "qt_abi_version": (I, []),
         "qt_launch_count": (L, [P]),
         "qt_work_counters": (I, [P, C.POINTER(D)]),
+        "qt_cert_counters": (I, [P, C.POINTER(L)]),
         "qt_gemm": (I, [P, I, I, I, L, L, L, C.POINTER(D), P, L, P, L, C.POINTER(D), P, L]),
         "qt_contract_pair": (I, [P, I, I, C.POINTER(L), P, I, C.POINTER(L), P, I, C.POINTER(I), C.POINTER(I), P]),
         "qt_truncated_svd": (I, [P, I, L, L, P, D, I, I, P, C.POINTER(D), P, C.POINTER(I), C.POINTER(D)]),
@@ -141,6 +145,9 @@ def library() -> C.CDLL:
         "qt_batch_replay": (I, [P, P]),
         "qt_batch_reset": (I, [P, P]),
         "qt_batch_task_stats": (I, [P, P, P, P, P]),
+        "qt_batch_cert_counts": (I, [P, P, C.POINTER(L)]),
+        "qt_batch_set_launch": (I, [P, P, I, I, I]),
+        "qt_batch_get_launch": (I, [P, I, C.POINTER(I), C.POINTER(I)]),
         "qt_batch_bond_dims": (I, [P, P, I, P]),
         "qt_batch_download_site": (I, [P, P, I, I, P]),
         "qt_batch_expect_z": (I, [P, P, I, P]),
@@ -249,6 +256,15 @@ class Engine:
         return {"jacobi_bytes": out[0], "jacobi_rounds": out[1], "tc_flops": out[2], "tc_launches": out[3],
                 "jacobi_pairs": out[4], "jacobi_inner_sweeps": out[5], "jacobi_gram_bytes": out[6],
                 "jacobi_rot_bytes": out[7]}
+
+    def cert_counters(self) -> dict:
+        """Chosen-mode rank decisions since creation, by how they were decided:
+        ``fallback`` (exact FP64 split, no certificate), ``resolved`` (cutoff at
+        or above the FP32 resolution), ``cap`` (chi_max binds with margin),
+        ``struct`` (the exact rank bound is met)."""
+        out = (C.c_int64 * 4)()
+        self._check(self._lib.qt_cert_counters(self._h, out))
+        return dict(zip(CERT_NAMES, (int(v) for v in out)))
 
     def sync(self):
         self._check(self._lib.qt_sync(self._h))
@@ -657,6 +673,23 @@ class Batch:
         if n:
             self.eng._check(self.eng._lib.qt_batch_task_stats(self.eng._h, self._p, _ptr(r), _ptr(sw), _ptr(d)))
         return r, sw, d
+
+    def set_launch(self, bucket_cap: int, threads: int, ctas_per_sm: int):
+        """Launch shape of the layer kernel for circuits with bond caps in the
+        bucket ``bucket_cap`` (16, 32, 64, 128); takes effect at the next run."""
+        self.eng._check(self.eng._lib.qt_batch_set_launch(self.eng._h, self._p, int(bucket_cap), int(threads),
+                                                          int(ctas_per_sm)))
+
+    def get_launch(self, bucket_cap: int):
+        t, c = C.c_int(), C.c_int()
+        self.eng._check(self.eng._lib.qt_batch_get_launch(self._p, int(bucket_cap), C.byref(t), C.byref(c)))
+        return t.value, c.value
+
+    def cert_counts(self) -> dict:
+        """Rank decisions of the last program's tasks, as Engine.cert_counters."""
+        out = (C.c_int64 * 4)()
+        self.eng._check(self.eng._lib.qt_batch_cert_counts(self.eng._h, self._p, out))
+        return dict(zip(CERT_NAMES, (int(v) for v in out)))
 
     def bond_dims(self, c: int):
         out = np.zeros(int(self.nqubits[c]) + 1, dtype=np.int32)

@@ -10,8 +10,10 @@
 //   theta' = G (A B)            FP32, gate folded per (a, b), kept in a per-CTA slab
 //   one-sided Jacobi on theta'  FP32 columns, warps on disjoint column pairs of a
 //                               round-robin round, rotation angles in FP64
-//   sigma_j = ||x_j||           FP64, bitonic sort, tail rule (FP64, sequential),
-//                               effective cutoff max(cutoff, floor ||theta'||), cap
+//   sigma_j = ||x_j||           FP64, bitonic sort, tail rule (FP64, sequential) at
+//                               the caller's cutoff, cap; a decision below the FP32
+//                               resolution without a certificate (cap or exact rank
+//                               bound) is redone as an FP64 split in the same CTA
 //   A' = x_perm(j) / sigma_j    written into site slot w
 //   B' = A'^H theta'            written into site slot w+1 (no V accumulation)
 //   bonds[w+1] = k
@@ -21,11 +23,13 @@
 // other CTAs: a CTA stops when the counter passes the task count.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <vector>
 
 #include "qt_internal.cuh"
+#include "qt_rank_model.h"
 
 namespace {
 
@@ -37,22 +41,25 @@ struct BatchArgs {
   float2* sites;
   const int64_t* site_off;   // per circuit: float2 offset of site 0
   const int* cap;            // per circuit: chi_max
+  const int* nsites;         // per circuit: qubits
   int* bonds;                // bond dims, bond_off[c] + i, i = 0..n
   const int* bond_off;
   const int* task_circ;
   const int* task_site;
   const double2* task_gate;  // 16 per task, column-major
+  const int* task_grank;     // per task: the gate's operator-Schmidt rank
   int task_begin, task_end;
   int* counter;
-  float2* slab;              // per CTA: 2 * slab_elems
+  float2* slab;              // per CTA: 4 * slab_elems float2 (FP32 X, T; or the FP64 X, T of a fallback)
   int slab_elems;
   double cutoff;
-  double floor_rel;
-  float tol;
+  double floor_rel;          // FP32 resolution relative to ||theta'||_F (<= 0: 4 sqrt(max(m, n)) u)
+  float tol;                 // FP32 Jacobi tolerance (relative off-diagonal)
   int max_sweeps;
   int* task_rank;
   int* task_sweeps;
   float* task_discarded;
+  int* task_cert;            // QT_CERT_* of the rank decision (QT_CERT_NONE: the FP64 split decided)
 };
 
 __device__ inline void tourney(int r, int q, int n, int& a, int& b) {
@@ -60,19 +67,170 @@ __device__ inline void tourney(int r, int q, int n, int& a, int& b) {
   else { a = (r + q) % (n - 1); b = (r - q + (n - 1)) % (n - 1); }
 }
 
-__device__ inline float warp_sum(float v) {
+template <typename R>
+__device__ inline R warp_sum(R v) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
 }
 
-__global__ void __launch_bounds__(BT) batch_layer_kernel(BatchArgs p) {
-  __shared__ int s_task, s_rot, s_k;
+// theta' = G (A B) into X and T (m x n, ld m), one thread per (a, b) owning
+// the four physical values; C = float2 (FP32 products) or double2 (FP64).
+template <int NT, typename C>
+__device__ void form_theta(const float2* A, const float2* B, int chil, int chim, int chir, const C* g, C* X, C* T) {
+  const int m = 2 * chil;
+  for (int idx = threadIdx.x; idx < chil * chir; idx += NT) {
+    const int a = idx % chil, b = idx / chil;
+    C acc[4] = {czero<C>(), czero<C>(), czero<C>(), czero<C>()};
+    for (int k = 0; k < chim; k++) {
+      const C a0 = ccast<C>(A[a + chil * (2 * k)]), a1 = ccast<C>(A[a + chil * (2 * k + 1)]);
+      const C b0 = ccast<C>(B[k + chim * (2 * b)]), b1 = ccast<C>(B[k + chim * (2 * b + 1)]);
+      cfma(acc[0], a0, b0);
+      cfma(acc[1], a1, b0);
+      cfma(acc[2], a0, b1);
+      cfma(acc[3], a1, b1);
+    }
+#pragma unroll
+    for (int o = 0; o < 4; o++) {
+      C v = czero<C>();
+#pragma unroll
+      for (int q = 0; q < 4; q++) cfma(v, g[o + 4 * q], acc[q]);
+      const int r = a + chil * (o & 1), col = (o >> 1) + 2 * b;
+      X[r + m * col] = v;
+      T[r + m * col] = v;
+    }
+  }
+}
+
+// ||X||_F^2 in FP64 over the CTA.
+template <int NT, typename C>
+__device__ double fro2_of(const C* X, int cnt, double* s_red) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  double part = 0;
+  for (int i = threadIdx.x; i < cnt; i += NT) part += (double)X[i].x * X[i].x + (double)X[i].y * X[i].y;
+  part = warp_sum(part);
+  __syncthreads();
+  if (lane == 0) s_red[warp] = part;
+  __syncthreads();
+  double fro2 = 0;
+  for (int i = 0; i < NT / 32; i++) fro2 += s_red[i];
+  return fro2;
+}
+
+// One-sided Jacobi on the n columns of X (m rows): warps on disjoint column
+// pairs of a round-robin round, rotation angles in FP64.  Columns with
+// |x|^2 <= nu2 are frozen.  Returns the sweeps run.
+template <int NT, typename C>
+__device__ int jacobi_columns(C* X, int m, int n, double tol, double nu2, int max_sweeps, int* s_rot) {
+  typedef typename real_of<C>::type R;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int sweeps = 0;
+  if (n < 2) return 0;
+  for (int sweep = 0; sweep < max_sweeps; sweep++) {
+    __syncthreads();  // every thread has read s_rot of the previous sweep
+    if (threadIdx.x == 0) *s_rot = 0;
+    __syncthreads();
+    for (int r = 0; r < n - 1; r++) {
+      for (int q = warp; q < n / 2; q += NT / 32) {
+        int pc, qc;
+        tourney(r, q, n, pc, qc);
+        C* xp = X + (size_t)m * pc;
+        C* xq = X + (size_t)m * qc;
+        R aa = 0, bb = 0, gr = 0, gi = 0;
+        for (int i = lane; i < m; i += 32) {
+          const C u = xp[i], v = xq[i];
+          aa = fma(u.x, u.x, fma(u.y, u.y, aa));
+          bb = fma(v.x, v.x, fma(v.y, v.y, bb));
+          gr = fma(u.x, v.x, fma(u.y, v.y, gr));
+          gi = fma(u.x, v.y, fma(-u.y, v.x, gi));
+        }
+        aa = warp_sum(aa);
+        bb = warp_sum(bb);
+        gr = warp_sum(gr);
+        gi = warp_sum(gi);
+        const double ag = sqrt((double)gr * gr + (double)gi * gi);
+        if ((double)aa > nu2 && (double)bb > nu2 && ag > tol * sqrt((double)aa * bb)) {
+          const double zeta = ((double)bb - aa) / (2.0 * ag);
+          const double t = copysign(1.0, zeta) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+          const double cs = 1.0 / sqrt(1.0 + t * t);
+          const R c = (R)cs, s = (R)(cs * t);
+          const R er = (R)(gr / ag), ei = (R)(gi / ag);
+          for (int i = lane; i < m; i += 32) {
+            const C u = xp[i], v = xq[i];
+            // x_p' = c x_p - s e^{-i phi} x_q ;  x_q' = s e^{i phi} x_p + c x_q
+            xp[i] = mk(c * u.x - s * (er * v.x + ei * v.y), c * u.y - s * (er * v.y - ei * v.x));
+            xq[i] = mk(s * (er * u.x - ei * u.y) + c * v.x, s * (er * u.y + ei * u.x) + c * v.y);
+          }
+          if (lane == 0) *s_rot = 1;
+        }
+      }
+      __syncthreads();
+    }
+    sweeps = sweep + 1;
+    const int again = *s_rot;  // read after the round's closing barrier
+    if (!again) break;
+  }
+  return sweeps;
+}
+
+// Column norms of X in FP64, sorted descending into s_sig / s_perm (bitonic).
+template <int NT, typename C>
+__device__ void sorted_norms(const C* X, int m, int n, double* s_sig, int* s_perm) {
+  int np2 = 1;
+  while (np2 < n) np2 <<= 1;
+  for (int j = threadIdx.x; j < np2; j += NT) {
+    double s = -1.0;
+    if (j < n) {
+      s = 0;
+      for (int i = 0; i < m; i++) {
+        const C v = X[i + (size_t)m * j];
+        s += (double)v.x * v.x + (double)v.y * v.y;
+      }
+      s = sqrt(s);
+    }
+    s_sig[j] = s;
+    s_perm[j] = j;
+  }
+  __syncthreads();
+  for (int k2 = 2; k2 <= np2; k2 <<= 1)
+    for (int j2 = k2 >> 1; j2 > 0; j2 >>= 1) {
+      for (int i = threadIdx.x; i < np2; i += NT) {
+        const int l = i ^ j2;
+        if (l > i) {
+          const bool desc = ((i & k2) == 0);
+          const double x = s_sig[i], y = s_sig[l];
+          const bool sw = desc ? (x < y || (x == y && s_perm[i] > s_perm[l]))
+                               : (x > y || (x == y && s_perm[i] < s_perm[l]));
+          if (sw) {
+            s_sig[i] = y; s_sig[l] = x;
+            const int tp = s_perm[i]; s_perm[i] = s_perm[l]; s_perm[l] = tp;
+          }
+        }
+      }
+      __syncthreads();
+    }
+}
+
+// The tail rule of src/svd.jl:29-33 (sequential from the smallest value,
+// strict >, k >= 1) on the n sorted values.
+__device__ int tail_rule(const double* s, int n, double cutoff) {
+  double acc = 0;
+  for (int i = n - 1; i >= 0; i--) {
+    acc += s[i] * s[i];
+    if (sqrt(acc) > cutoff) return i + 1;
+  }
+  return 1;
+}
+
+template <int NT>
+__global__ void __launch_bounds__(NT) batch_layer_kernel(BatchArgs p) {
+  __shared__ int s_task, s_rot, s_k, s_fb;
   __shared__ float2 g[16];
+  __shared__ double2 g64[16];
   __shared__ double s_sig[MAXN];
   __shared__ int s_perm[MAXN];
-  __shared__ double s_red[BWARPS];
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  float2* X = p.slab + (size_t)blockIdx.x * 2 * p.slab_elems;
+  __shared__ double s_red[NT / 32];
+  const int tid = threadIdx.x;
+  float2* X = p.slab + (size_t)blockIdx.x * 4 * p.slab_elems;
   float2* T = X + p.slab_elems;
 
   for (;;) {
@@ -83,7 +241,7 @@ __global__ void __launch_bounds__(BT) batch_layer_kernel(BatchArgs p) {
     const int c = p.task_circ[task], w = p.task_site[task];
     int* bond = p.bonds + p.bond_off[c];
     const int chil = bond[w], chim = bond[w + 1], chir = bond[w + 2];
-    const int cap = p.cap[c];
+    const int cap = p.cap[c], nq = p.nsites[c];
     const size_t slot = (size_t)cap * 2 * cap;
     float2* A = p.sites + p.site_off[c] + (size_t)w * slot;
     float2* B = A + slot;
@@ -91,165 +249,124 @@ __global__ void __launch_bounds__(BT) batch_layer_kernel(BatchArgs p) {
     if (tid < 16) {
       const double2 v = p.task_gate[(size_t)task * 16 + tid];
       g[tid] = make_float2((float)v.x, (float)v.y);
+      g64[tid] = v;
     }
     __syncthreads();
 
-    // 1. theta' = G (A B), one thread per (a, b) owning the four physical values
-    for (int idx = tid; idx < chil * chir; idx += BT) {
-      const int a = idx % chil, b = idx / chil;
-      float2 acc[4] = {make_float2(0, 0), make_float2(0, 0), make_float2(0, 0), make_float2(0, 0)};
-      for (int k = 0; k < chim; k++) {
-        const float2 a0 = A[a + chil * (2 * k)], a1 = A[a + chil * (2 * k + 1)];
-        const float2 b0 = B[k + chim * (2 * b)], b1 = B[k + chim * (2 * b + 1)];
-        cfma(acc[0], a0, b0);
-        cfma(acc[1], a1, b0);
-        cfma(acc[2], a0, b1);
-        cfma(acc[3], a1, b1);
-      }
-#pragma unroll
-      for (int o = 0; o < 4; o++) {
-        float2 v = make_float2(0, 0);
-#pragma unroll
-        for (int q = 0; q < 4; q++) cfma(v, g[o + 4 * q], acc[q]);
-        const int r = a + chil * (o & 1), col = (o >> 1) + 2 * b;
-        X[r + m * col] = v;
-        T[r + m * col] = v;
-      }
-    }
+    // 1. theta' = G (A B) in FP32
+    form_theta<NT, float2>(A, B, chil, chim, chir, g, X, T);
     __syncthreads();
-
-    // ||theta'||_F^2 in FP64 (sets the rounding floor)
-    double part = 0;
-    for (int i = tid; i < m * n; i += BT) part += (double)X[i].x * X[i].x + (double)X[i].y * X[i].y;
-    for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
-    if (lane == 0) s_red[warp] = part;
-    __syncthreads();
-    double fro2 = 0;
-    for (int i = 0; i < BWARPS; i++) fro2 += s_red[i];
+    const double fro2 = fro2_of<NT>(X, m * n, s_red);
     const double nu = 4.0 * sqrt((double)max(m, 16)) * 5.96e-8;
-    const float nu2 = (float)(nu * nu * fro2);
 
-    // 2. one-sided Jacobi on the n columns of X (m rows)
-    int sweeps = 0;
-    if (n > 1) {
-      for (int sweep = 0; sweep < p.max_sweeps; sweep++) {
-        __syncthreads();  // every thread has read s_rot of the previous sweep
-        if (tid == 0) s_rot = 0;
-        __syncthreads();
-        for (int r = 0; r < n - 1; r++) {
-          for (int q = warp; q < n / 2; q += BWARPS) {
-            int pc, qc;
-            tourney(r, q, n, pc, qc);
-            float2* xp = X + (size_t)m * pc;
-            float2* xq = X + (size_t)m * qc;
-            float aa = 0, bb = 0, gr = 0, gi = 0;
-            for (int i = lane; i < m; i += 32) {
-              const float2 u = xp[i], v = xq[i];
-              aa = fmaf(u.x, u.x, fmaf(u.y, u.y, aa));
-              bb = fmaf(v.x, v.x, fmaf(v.y, v.y, bb));
-              gr = fmaf(u.x, v.x, fmaf(u.y, v.y, gr));
-              gi = fmaf(u.x, v.y, fmaf(-u.y, v.x, gi));
-            }
-            aa = warp_sum(aa);
-            bb = warp_sum(bb);
-            gr = warp_sum(gr);
-            gi = warp_sum(gi);
-            const double ag = sqrt((double)gr * gr + (double)gi * gi);
-            if (aa > nu2 && bb > nu2 && ag > (double)p.tol * sqrt((double)aa * bb)) {
-              const double zeta = ((double)bb - aa) / (2.0 * ag);
-              const double t = copysign(1.0, zeta) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
-              const double cs = 1.0 / sqrt(1.0 + t * t);
-              const float c = (float)cs, s = (float)(cs * t);
-              const float er = (float)(gr / ag), ei = (float)(gi / ag);
-              for (int i = lane; i < m; i += 32) {
-                const float2 u = xp[i], v = xq[i];
-                // x_p' = c x_p - s e^{-i phi} x_q ;  x_q' = s e^{i phi} x_p + c x_q
-                xp[i] = make_float2(c * u.x - s * (er * v.x + ei * v.y), c * u.y - s * (er * v.y - ei * v.x));
-                xq[i] = make_float2(s * (er * u.x - ei * u.y) + c * v.x, s * (er * u.y + ei * u.x) + c * v.y);
-              }
-              if (lane == 0) s_rot = 1;
-            }
-          }
-          __syncthreads();
-        }
-        sweeps = sweep + 1;
-        const int again = s_rot;  // read after the round's closing barrier
-        if (!again) break;
-      }
-    }
+    // 2. one-sided Jacobi on the columns of X, 3. sorted FP64 norms
+    int sweeps = jacobi_columns<NT, float2>(X, m, n, (double)p.tol, nu * nu * fro2, p.max_sweeps, &s_rot);
+    sorted_norms<NT, float2>(X, m, n, s_sig, s_perm);
 
-    // 3. singular values (FP64 norms), sorted descending
-    int np2 = 1;
-    while (np2 < n) np2 <<= 1;
-    for (int j = tid; j < np2; j += BT) {
-      double s = -1.0;
-      if (j < n) {
-        s = 0;
-        for (int i = 0; i < m; i++) {
-          const float2 v = X[i + (size_t)m * j];
-          s += (double)v.x * v.x + (double)v.y * v.y;
-        }
-        s = sqrt(s);
-      }
-      s_sig[j] = s;
-      s_perm[j] = j;
-    }
-    __syncthreads();
-    for (int k2 = 2; k2 <= np2; k2 <<= 1)
-      for (int j2 = k2 >> 1; j2 > 0; j2 >>= 1) {
-        for (int i = tid; i < np2; i += BT) {
-          const int l = i ^ j2;
-          if (l > i) {
-            const bool desc = ((i & k2) == 0);
-            const double x = s_sig[i], y = s_sig[l];
-            const bool sw = desc ? (x < y || (x == y && s_perm[i] > s_perm[l]))
-                                 : (x > y || (x == y && s_perm[i] < s_perm[l]));
-            if (sw) {
-              s_sig[i] = y; s_sig[l] = x;
-              const int tp = s_perm[i]; s_perm[i] = s_perm[l]; s_perm[l] = tp;
-            }
-          }
-        }
-        __syncthreads();
-      }
-
-    // 4. the tail rule (sequential, from the smallest value), then the cap
+    // 4. the tail rule at the caller's cutoff, then the cap.  Below the FP32
+    // resolution eta the decision needs a certificate: the cap binding with
+    // margin, or exactly as many values above eta as the exact rank bound
+    // allows (the gate's operator-Schmidt rank times the inner bond, the
+    // Hilbert-space dimensions of the two sides).  Otherwise the FP64 split
+    // below decides.
+    const int kcap = min(cap, min(m, n));
     if (tid == 0) {
-      const double eff = fmax(p.cutoff, p.floor_rel * sqrt(fro2));
-      double acc = 0;
-      int k = 1;
-      for (int i = n - 1; i >= 0; i--) {
-        acc += s_sig[i] * s_sig[i];
-        if (sqrt(acc) > eff) { k = i + 1; break; }
+      const double eta = (p.floor_rel > 0 ? p.floor_rel : 4.0 * sqrt((double)max(m, n)) * 5.96e-8) * sqrt(fro2);
+      int kc = tail_rule(s_sig, n, p.cutoff);
+      int cert = QT_CERT_NONE;
+      if (p.cutoff >= eta) {
+        cert = QT_CERT_RESOLVED;
+      } else if (cap < min(m, n) && kc > cap) {
+        double t2 = 0;
+        for (int i = n - 1; i >= cap; i--) t2 += s_sig[i] * s_sig[i];
+        if (sqrt(t2) > p.cutoff + eta) cert = QT_CERT_CAP;
       }
-      k = min(k, min(cap, min(m, n)));
+      if (cert == QT_CERT_NONE) {
+        int srank = min(min(m, n), p.task_grank[task] * chim);
+        if (w + 1 < 30) srank = min(srank, 1 << (w + 1));
+        if (nq - w - 1 < 30) srank = min(srank, 1 << (nq - w - 1));
+        int kr = 0;
+        while (kr < n && s_sig[kr] > eta) kr++;
+        if (kr == srank) {
+          kc = srank;
+          cert = QT_CERT_STRUCT;
+        }
+      }
+      const int k = min(kc, kcap);
       double disc = 0;
       for (int i = k; i < n; i++) disc += s_sig[i] * s_sig[i];
       s_k = k;
+      s_fb = cert == QT_CERT_NONE;
       p.task_rank[task] = k;
       p.task_sweeps[task] = sweeps;
       p.task_discarded[task] = (float)disc;
+      p.task_cert[task] = cert;
     }
     __syncthreads();
-    const int k = s_k;
 
-    // 5. A' (chil, 2, k) = unit columns, into site slot w
-    for (int idx = tid; idx < m * k; idx += BT) {
-      const int r = idx % m, j = idx / m;
-      const double s = s_sig[j];
-      const float inv = s > 0 ? (float)(1.0 / s) : 0.f;
-      const float2 v = X[r + (size_t)m * s_perm[j]];
-      A[r + (size_t)m * j] = make_float2(v.x * inv, v.y * inv);
+    if (!s_fb) {
+      const int k = s_k;
+      // 5. A' (chil, 2, k) = unit columns, into site slot w
+      for (int idx = tid; idx < m * k; idx += NT) {
+        const int r = idx % m, j = idx / m;
+        const double s = s_sig[j];
+        const float inv = s > 0 ? (float)(1.0 / s) : 0.f;
+        const float2 v = X[r + (size_t)m * s_perm[j]];
+        A[r + (size_t)m * j] = make_float2(v.x * inv, v.y * inv);
+      }
+      __syncthreads();
+      // 6. B' (k, 2, chir) = A'^H theta', into site slot w+1
+      for (int idx = tid; idx < k * n; idx += NT) {
+        const int j = idx % k, col = idx / k;
+        float2 acc = make_float2(0, 0);
+        for (int r = 0; r < m; r++) cfma_conj(acc, A[r + (size_t)m * j], T[r + (size_t)m * col]);
+        B[j + (size_t)k * col] = acc;
+      }
+    } else {
+      // The exact FP64 split: theta' from the complex64 sites in FP64, FP64
+      // Jacobi (tolerance and freeze at FP64 rounding), the rule at the
+      // caller's cutoff; the FP64 X and T take the whole slab.
+      double2* X64 = reinterpret_cast<double2*>(X);
+      double2* T64 = X64 + p.slab_elems;
+      __syncthreads();
+      form_theta<NT, double2>(A, B, chil, chim, chir, g64, X64, T64);
+      __syncthreads();
+      const double f64 = fro2_of<NT>(X64, m * n, s_red);
+      const double nu64 = 4.0 * sqrt((double)max(m, 16)) * 1.11e-16;
+      sweeps += jacobi_columns<NT, double2>(X64, m, n, 16.0 * sqrt((double)max(m, 16)) * 1.11e-16,
+                                            nu64 * nu64 * f64, p.max_sweeps, &s_rot);
+      sorted_norms<NT, double2>(X64, m, n, s_sig, s_perm);
+      if (tid == 0) {
+        const int k = min(tail_rule(s_sig, n, p.cutoff), kcap);
+        double disc = 0;
+        for (int i = k; i < n; i++) disc += s_sig[i] * s_sig[i];
+        s_k = k;
+        p.task_rank[task] = k;
+        p.task_sweeps[task] = sweeps;
+        p.task_discarded[task] = (float)disc;
+      }
+      __syncthreads();
+      const int k = s_k;
+      // B' = A'^H theta' from the FP64 columns (before A is overwritten: B
+      // reads only X64 and T64), then A' = unit columns
+      for (int idx = tid; idx < k * n; idx += NT) {
+        const int j = idx % k, col = idx / k;
+        const double s = s_sig[j];
+        const double inv = s > 0 ? 1.0 / s : 0.0;
+        const double2* xj = X64 + (size_t)m * s_perm[j];
+        double2 acc = make_double2(0, 0);
+        for (int r = 0; r < m; r++) cfma_conj(acc, xj[r], T64[r + (size_t)m * col]);
+        B[j + (size_t)k * col] = make_float2((float)(acc.x * inv), (float)(acc.y * inv));
+      }
+      for (int idx = tid; idx < m * k; idx += NT) {
+        const int r = idx % m, j = idx / m;
+        const double s = s_sig[j];
+        const double inv = s > 0 ? 1.0 / s : 0.0;
+        const double2 v = X64[r + (size_t)m * s_perm[j]];
+        A[r + (size_t)m * j] = make_float2((float)(v.x * inv), (float)(v.y * inv));
+      }
     }
-    __syncthreads();
-    // 6. B' (k, 2, chir) = A'^H theta', into site slot w+1
-    for (int idx = tid; idx < k * n; idx += BT) {
-      const int j = idx % k, col = idx / k;
-      float2 acc = make_float2(0, 0);
-      for (int r = 0; r < m; r++) cfma_conj(acc, A[r + (size_t)m * j], T[r + (size_t)m * col]);
-      B[j + (size_t)k * col] = acc;
-    }
-    if (tid == 0) bond[w + 1] = k;
+    if (tid == 0) bond[w + 1] = s_k;
     __syncthreads();
   }
 }
@@ -347,17 +464,32 @@ struct qt_batch {
   double2* d_tg = nullptr;
   int* d_rank = nullptr;
   int* d_sweeps = nullptr;
+  int* d_grank = nullptr;
+  int* d_cert = nullptr;
   float* d_disc = nullptr;
   int ntask_cap = 0;
+  std::vector<int> order;    // device task index -> the caller's task index
   cudaGraphExec_t graph = nullptr;
+  // launch shape per bond-cap bucket (caps <= 16, 32, 64, 128): threads per
+  // CTA and CTAs per SM of the persistent layer kernel (qt_batch_set_launch)
+  int threads[4] = {256, 256, 256, 256};
+  int cps[4] = {1, 1, 1, 1};
+  int slab_ctas = 0;         // CTAs the slab holds
 };
+
+namespace {
+
+int bucket_of(int cap) { return cap <= 16 ? 0 : cap <= 32 ? 1 : cap <= 64 ? 2 : 3; }
+
+}  // namespace
 
 static void batch_free_program(qt_batch* b) {
   if (b->graph) cudaGraphExecDestroy(b->graph);
   b->graph = nullptr;
   cudaFree(b->d_tc); cudaFree(b->d_ts); cudaFree(b->d_tg);
-  cudaFree(b->d_rank); cudaFree(b->d_sweeps); cudaFree(b->d_disc);
+  cudaFree(b->d_rank); cudaFree(b->d_sweeps); cudaFree(b->d_disc); cudaFree(b->d_grank); cudaFree(b->d_cert);
   b->d_tc = b->d_ts = nullptr; b->d_tg = nullptr; b->d_rank = b->d_sweeps = nullptr; b->d_disc = nullptr;
+  b->d_grank = b->d_cert = nullptr;
   b->ntask_cap = 0;
 }
 
@@ -393,7 +525,8 @@ extern "C" int qt_batch_create(qt_handle* h, int ncirc, const int* nqubits, cons
             cudaMalloc(&b->d_nsites, sizeof(int) * ncirc) == cudaSuccess &&
             cudaMalloc(&b->d_bonds, sizeof(int) * boff) == cudaSuccess &&
             cudaMalloc(&b->d_bond_off, sizeof(int) * ncirc) == cudaSuccess &&
-            cudaMalloc(&b->d_slab, sizeof(float2) * 3 * (size_t)b->slab_elems * b->ctas) == cudaSuccess;
+            cudaMalloc(&b->d_slab, sizeof(float2) * 4 * (size_t)b->slab_elems * b->ctas) == cudaSuccess;
+  b->slab_ctas = b->ctas;
   if (!ok) {
     cudaGetLastError();
     qt_batch_free(h, b);
@@ -439,46 +572,99 @@ extern "C" int qt_batch_run(qt_handle* h, qt_batch* b, int nlayers, const int* l
       return qt_fail(h, QT_EBOUNDS, "batch_run: task site out of range");
   }
   batch_free_program(b);
+  // tasks of each layer grouped by the bucket of their circuit's cap (stable):
+  // one launch per (layer, bucket) with that bucket's launch shape
+  std::vector<int> order;
+  std::vector<int> seg_begin, seg_end, seg_bucket;
+  order.reserve(ntask);
+  for (int l = 0; l < nlayers; l++) {
+    for (int bk = 0; bk < 4; bk++) {
+      const int start = (int)order.size();
+      for (int t = layer_start[l]; t < layer_start[l + 1]; t++)
+        if (bucket_of(b->cap[circ[t]]) == bk) order.push_back(t);
+      if ((int)order.size() > start) {
+        seg_begin.push_back(start);
+        seg_end.push_back((int)order.size());
+        seg_bucket.push_back(bk);
+      }
+    }
+  }
+  const int nseg = (int)seg_begin.size();
+  std::vector<int> oc(ntask), os(ntask);
+  std::vector<double> og((size_t)32 * ntask);
+  for (int i = 0; i < ntask; i++) {
+    oc[i] = circ[order[i]];
+    os[i] = site[order[i]];
+    std::memcpy(&og[(size_t)32 * i], gates + (size_t)32 * order[i], sizeof(double) * 32);
+  }
+  b->order = order;
+  // the slab holds one 4-unit block per CTA of the widest launch
+  const int dev_sms = b->ctas;
+  int need = 0;
+  for (int bk = 0; bk < 4; bk++) need = std::max(need, dev_sms * b->cps[bk]);
+  if (need > b->slab_ctas) {
+    cudaFree(b->d_slab);
+    b->d_slab = nullptr;
+    if (cudaMalloc(&b->d_slab, sizeof(float2) * 4 * (size_t)b->slab_elems * need) != cudaSuccess) {
+      cudaGetLastError();
+      b->slab_ctas = 0;
+      return qt_fail(h, QT_ENOMEM, "batch_run: slab allocation failed");
+    }
+    b->slab_ctas = need;
+  }
   if (ntask > 0) {
     bool ok = cudaMalloc(&b->d_tc, sizeof(int) * ntask) == cudaSuccess &&
               cudaMalloc(&b->d_ts, sizeof(int) * ntask) == cudaSuccess &&
               cudaMalloc(&b->d_tg, sizeof(double2) * 16 * (size_t)ntask) == cudaSuccess &&
               cudaMalloc(&b->d_rank, sizeof(int) * ntask) == cudaSuccess &&
               cudaMalloc(&b->d_sweeps, sizeof(int) * ntask) == cudaSuccess &&
-              cudaMalloc(&b->d_disc, sizeof(float) * ntask) == cudaSuccess;
+              cudaMalloc(&b->d_disc, sizeof(float) * ntask) == cudaSuccess &&
+              cudaMalloc(&b->d_grank, sizeof(int) * ntask) == cudaSuccess &&
+              cudaMalloc(&b->d_cert, sizeof(int) * ntask) == cudaSuccess;
     if (!ok) {
       cudaGetLastError();
       return qt_fail(h, QT_ENOMEM, "batch_run: device allocation failed");
     }
     b->ntask_cap = ntask;
-    QT_CHECK_CUDA(h, cudaMemcpyAsync(b->d_tc, circ, sizeof(int) * ntask, cudaMemcpyHostToDevice, h->stream));
-    QT_CHECK_CUDA(h, cudaMemcpyAsync(b->d_ts, site, sizeof(int) * ntask, cudaMemcpyHostToDevice, h->stream));
-    QT_CHECK_CUDA(h, cudaMemcpyAsync(b->d_tg, gates, sizeof(double2) * 16 * ntask, cudaMemcpyHostToDevice, h->stream));
+    QT_CHECK_CUDA(h, cudaMemcpyAsync(b->d_tc, oc.data(), sizeof(int) * ntask, cudaMemcpyHostToDevice, h->stream));
+    QT_CHECK_CUDA(h, cudaMemcpyAsync(b->d_ts, os.data(), sizeof(int) * ntask, cudaMemcpyHostToDevice, h->stream));
+    QT_CHECK_CUDA(h, cudaMemcpyAsync(b->d_tg, og.data(), sizeof(double2) * 16 * ntask, cudaMemcpyHostToDevice,
+                                     h->stream));
+    std::vector<int> grank(ntask);
+    for (int t = 0; t < ntask; t++) grank[t] = qt_gate_schmidt_rank(og.data() + 32 * (size_t)t);
+    QT_CHECK_CUDA(h, cudaMemcpyAsync(b->d_grank, grank.data(), sizeof(int) * ntask, cudaMemcpyHostToDevice,
+                                     h->stream));
+    QT_CHECK_CUDA(h, cudaStreamSynchronize(h->stream));
   }
-  if (b->counter_cap < nlayers) {
+  if (b->counter_cap < nseg) {
     cudaFree(b->d_counter);
-    if (cudaMalloc(&b->d_counter, sizeof(int) * std::max(nlayers, 1)) != cudaSuccess)
+    if (cudaMalloc(&b->d_counter, sizeof(int) * std::max(nseg, 1)) != cudaSuccess)
       return qt_fail(h, QT_ENOMEM, "batch_run: counter allocation failed");
-    b->counter_cap = nlayers;
+    b->counter_cap = nseg;
   }
   BatchArgs a;
-  a.sites = b->d_sites; a.site_off = b->d_site_off; a.cap = b->d_cap; a.bonds = b->d_bonds;
+  a.sites = b->d_sites; a.site_off = b->d_site_off; a.cap = b->d_cap; a.nsites = b->d_nsites; a.bonds = b->d_bonds;
+  a.task_grank = b->d_grank; a.task_cert = b->d_cert;
   a.bond_off = b->d_bond_off; a.task_circ = b->d_tc; a.task_site = b->d_ts; a.task_gate = b->d_tg;
   a.slab = b->d_slab; a.slab_elems = b->slab_elems; a.cutoff = cutoff;
-  a.floor_rel = h->cfg.noise_floor > 0 ? h->cfg.noise_floor : 4.0 * std::sqrt(2.0 * b->capmax) * 5.96e-8;
+  a.floor_rel = h->cfg.noise_floor;  // <= 0: the default resolution of each task's shape
   a.tol = (float)(16.0 * std::sqrt(2.0 * b->capmax) * 5.96e-8);
   a.max_sweeps = std::max(4, h->cfg.max_sweeps);
   a.task_rank = b->d_rank; a.task_sweeps = b->d_sweeps; a.task_discarded = b->d_disc;
   auto launch_all = [&]() -> int {
-    QT_CHECK_CUDA(h, cudaMemsetAsync(b->d_counter, 0, sizeof(int) * std::max(nlayers, 1), h->stream));
-    for (int l = 0; l < nlayers; l++) {
-      if (layer_start[l + 1] <= layer_start[l]) continue;
+    QT_CHECK_CUDA(h, cudaMemsetAsync(b->d_counter, 0, sizeof(int) * std::max(nseg, 1), h->stream));
+    for (int sg = 0; sg < nseg; sg++) {
+      const int bk = seg_bucket[sg];
       BatchArgs al = a;
-      al.task_begin = layer_start[l];
-      al.task_end = layer_start[l + 1];
-      al.counter = b->d_counter + l;
-      const int grid = std::min(b->ctas, layer_start[l + 1] - layer_start[l]);
-      QT_LAUNCH(h, batch_layer_kernel, grid, BT, 0, al);
+      al.task_begin = seg_begin[sg];
+      al.task_end = seg_end[sg];
+      al.counter = b->d_counter + sg;
+      const int grid = std::min(dev_sms * b->cps[bk], seg_end[sg] - seg_begin[sg]);
+      switch (b->threads[bk]) {
+        case 128: QT_LAUNCH(h, batch_layer_kernel<128>, grid, 128, 0, al); break;
+        case 512: QT_LAUNCH(h, batch_layer_kernel<512>, grid, 512, 0, al); break;
+        default: QT_LAUNCH(h, batch_layer_kernel<256>, grid, 256, 0, al); break;
+      }
     }
     return QT_OK;
   };
@@ -526,9 +712,50 @@ extern "C" int qt_batch_task_stats(qt_handle* h, const qt_batch* b, int* rank, i
   if (!h || !b) return qt_fail(h, QT_EINVAL, "batch_task_stats: bad argument");
   const int n = b->ntask_cap;
   if (n == 0) return QT_OK;
-  if (rank) QT_CHECK_CUDA(h, cudaMemcpy(rank, b->d_rank, sizeof(int) * n, cudaMemcpyDeviceToHost));
-  if (sweeps) QT_CHECK_CUDA(h, cudaMemcpy(sweeps, b->d_sweeps, sizeof(int) * n, cudaMemcpyDeviceToHost));
-  if (discarded) QT_CHECK_CUDA(h, cudaMemcpy(discarded, b->d_disc, sizeof(float) * n, cudaMemcpyDeviceToHost));
+  // device order -> the caller's task order
+  std::vector<int> ri(n), si(n);
+  std::vector<float> di(n);
+  QT_CHECK_CUDA(h, cudaMemcpy(ri.data(), b->d_rank, sizeof(int) * n, cudaMemcpyDeviceToHost));
+  QT_CHECK_CUDA(h, cudaMemcpy(si.data(), b->d_sweeps, sizeof(int) * n, cudaMemcpyDeviceToHost));
+  QT_CHECK_CUDA(h, cudaMemcpy(di.data(), b->d_disc, sizeof(float) * n, cudaMemcpyDeviceToHost));
+  for (int i = 0; i < n; i++) {
+    const int t = b->order[i];
+    if (rank) rank[t] = ri[i];
+    if (sweeps) sweeps[t] = si[i];
+    if (discarded) discarded[t] = di[i];
+  }
+  return QT_OK;
+}
+
+extern "C" int qt_batch_set_launch(qt_handle* h, qt_batch* b, int bucket_cap, int threads, int ctas_per_sm) {
+  if (!h || !b) return qt_fail(h, QT_EINVAL, "batch_set_launch: bad argument");
+  if (bucket_cap != 16 && bucket_cap != 32 && bucket_cap != 64 && bucket_cap != 128)
+    return qt_fail(h, QT_EINVAL, "batch_set_launch: bucket_cap must be 16, 32, 64 or 128");
+  if (threads != 128 && threads != 256 && threads != 512)
+    return qt_fail(h, QT_EINVAL, "batch_set_launch: threads must be 128, 256 or 512");
+  if (ctas_per_sm < 1 || ctas_per_sm > 4) return qt_fail(h, QT_EINVAL, "batch_set_launch: ctas_per_sm must be 1..4");
+  const int bk = bucket_of(bucket_cap);
+  b->threads[bk] = threads;
+  b->cps[bk] = ctas_per_sm;
+  return QT_OK;
+}
+
+extern "C" int qt_batch_get_launch(const qt_batch* b, int bucket_cap, int* threads, int* ctas_per_sm) {
+  if (!b || !threads || !ctas_per_sm) return QT_EINVAL;
+  const int bk = bucket_of(bucket_cap);
+  *threads = b->threads[bk];
+  *ctas_per_sm = b->cps[bk];
+  return QT_OK;
+}
+
+extern "C" int qt_batch_cert_counts(qt_handle* h, const qt_batch* b, int64_t* out) {
+  if (!h || !b || !out) return qt_fail(h, QT_EINVAL, "batch_cert_counts: bad argument");
+  for (int i = 0; i < QT_CERT_SLOTS; i++) out[i] = 0;
+  const int n = b->ntask_cap;
+  if (n == 0) return QT_OK;
+  std::vector<int> cert(n);
+  QT_CHECK_CUDA(h, cudaMemcpy(cert.data(), b->d_cert, sizeof(int) * n, cudaMemcpyDeviceToHost));
+  for (int c : cert) out[(c >= 0 && c < QT_CERT_SLOTS) ? c : QT_CERT_NONE]++;
   return QT_OK;
 }
 
@@ -559,7 +786,7 @@ extern "C" int qt_batch_expect_z(qt_handle* h, qt_batch* b, int site, double* ou
   double* d_out;
   QT_CHECK_CUDA(h, cudaMalloc(&d_out, sizeof(double) * b->ncirc));
   const int grid = std::min(b->ncirc, b->ctas);
-  // the slab holds 2 * slab_elems per CTA for the update; the sweep needs 3 (cap^2 each fits in one)
+  // the slab holds 4 * slab_elems per CTA for the update; the sweep needs 3 (cap^2 each fits in one)
   batch_expect_kernel<<<grid, BT, 0, h->stream>>>(b->d_sites, b->d_site_off, b->d_cap, b->d_nsites, b->d_bonds,
                                                    b->d_bond_off, b->ncirc, site, b->d_slab, b->slab_elems / 4 + 1,
                                                    d_out);

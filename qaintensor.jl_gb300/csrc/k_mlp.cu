@@ -214,6 +214,24 @@ void qt_rank_features(const qt_mps* mps, int site, const double* G, double cutof
   f[15] = (float)(-std::log10(std::max(cutoff, 1e-300)) / 16.0);
 }
 
+int qt_gate_schmidt_rank(const double* G) {
+  double r[32];
+  for (int o1 = 0; o1 < 2; o1++)
+    for (int o2 = 0; o2 < 2; o2++)
+      for (int i1 = 0; i1 < 2; i1++)
+        for (int i2 = 0; i2 < 2; i2++) {
+          const int gi = (o1 + 2 * o2) + 4 * (i1 + 2 * i2);
+          const int row = o1 + 2 * i1, col = o2 + 2 * i2;
+          r[2 * (row + 4 * col)] = G[2 * gi];
+          r[2 * (row + 4 * col) + 1] = G[2 * gi + 1];
+        }
+  double sv[4];
+  singular_values_4x4(r, sv);
+  int k = 0;
+  for (int i = 0; i < 4; i++) k += (sv[i] > 1e-12 * sv[0]) ? 1 : 0;
+  return std::max(k, 1);
+}
+
 int qt_rank_model_predict(qt_handle* h, const float* feat, int kmax) {
   qt_rank_model* m = h->rank_model;
   if (!m || !m->trained || !h->cfg.use_rank_model || !m->d_params) return -1;

@@ -11,6 +11,7 @@
 //                   A''^H (exact isometry) and B''^H absorbed into the left one.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <vector>
 
@@ -85,7 +86,7 @@ int apply_mpo_t(qt_handle* h, qt_mps* mps, const double2* const* dW, const int* 
 
 // the truncated split used by the sweep (qt_engine.cu)
 int qt_split_device(qt_handle* h, int dtype, const void* M, int64_t m, int64_t n, double cutoff, int chi_max, int mode,
-                    void** A, void** B, int* k, double* discarded);
+                    void** A, void** B, int* k, double* discarded, int64_t struct_rank);
 
 extern "C" int qt_mps_apply_mpo(qt_handle* h, qt_mps* mps, const double* const* W, const int64_t* dims) {
   // W[i]: (bl, 2, 2, br) complex128 column-major interleaved; dims 4 per site
@@ -198,7 +199,12 @@ extern "C" int qt_mps_compress(qt_handle* h, qt_mps* mps, double cutoff, int chi
     void *Ah = nullptr, *Bh = nullptr;
     int k = 0;
     double disc = 0;
-    QT_TRY(qt_split_device(h, mps->dtype, Mh, 2 * cr, cl, cutoff, chi_max, mode, &Ah, &Bh, &k, &disc));
+    // exact rank bound: the Hilbert-space dimensions of the i qubits left of
+    // the bond and the n - i right of it
+    int64_t srank = std::min<int64_t>(2 * cr, cl);
+    if (i < 40) srank = std::min<int64_t>(srank, (int64_t)1 << i);
+    if (n - i < 40) srank = std::min<int64_t>(srank, (int64_t)1 << (n - i));
+    QT_TRY(qt_split_device(h, mps->dtype, Mh, 2 * cr, cl, cutoff, chi_max, mode, &Ah, &Bh, &k, &disc, srank));
     // new site = Ah^H (k x 2cr); left site (pl, 2, cl) <- left . Bh^H (cl x k)
     void *ns = nullptr, *nl = nullptr;
     QT_TRY(qt_dmalloc(h, &ns, es * k * 2 * cr));

@@ -50,6 +50,12 @@ static size_t elem_size(int dtype) { return dtype == QT_C64 ? sizeof(float2) : s
 
 extern "C" int qt_abi_version(void) { return QT_ABI_VERSION; }
 
+extern "C" int qt_cert_counters(const qt_handle* h, int64_t* out) {
+  if (!h || !out) return QT_EINVAL;
+  for (int i = 0; i < QT_CERT_SLOTS; i++) out[i] = h->cert_count[i];
+  return QT_OK;
+}
+
 extern "C" int qt_work_counters(const qt_handle* h, double* out) {
   if (!h || !out) return QT_EINVAL;
   out[0] = h->work_jacobi_bytes;
@@ -80,6 +86,7 @@ extern "C" int qt_config_default(qt_config* cfg) {
   cfg->seed = 0x5eed5eedull;
   cfg->tc_gemm = 0;
   cfg->jacobi_kernel = 0;
+  cfg->cap_sketch = 0.0;     // 0: 1.125 chi_max
   return QT_OK;
 }
 
@@ -424,6 +431,56 @@ int choose_rank(const qt_handle* h, const std::vector<double>& s, double cutoff,
   return QT_OK;
 }
 
+// Chosen-mode rank certification.  The FP32-level split resolves singular
+// values and tail norms only down to eta (a few units of FP32 rounding of
+// ||theta'||_F).  The tail rule of src/svd.jl:29-33 at a cutoff below eta is
+// still decided exactly when
+//   - the cutoff is at or above eta (resolved), or
+//   - the chi_max cap binds with margin: the computed tail beyond chi_max
+//     exceeds cutoff + eta, so the exact tail does too and k = chi_max, or
+//   - exactly struct_rank values lie above eta, where struct_rank bounds the
+//     rank in exact arithmetic (the gate's operator-Schmidt rank times the
+//     inner bond, the Hilbert-space dimensions of the two sides): the values
+//     below eta are then exact zeros, which the rule drops at any cutoff,
+//     while every value above eta exceeds the cutoff.
+// Any other decision is left to the exact FP64 split (fallback 4).
+struct RankCert {
+  double eta = -1.0;        // absolute resolution of the computed spectrum
+  int64_t struct_rank = 0;  // exact-arithmetic rank bound (0: unknown)
+  int how = 0;              // out: QT_CERT_*
+};
+
+bool certify_rank(const std::vector<double>& s, double extra_tail, double cutoff, int chi_max, RankCert* c,
+                  SvdOut* o) {
+  if (cutoff >= c->eta) {
+    c->how = QT_CERT_RESOLVED;
+    return true;
+  }
+  if (chi_max > 0 && o->k_cut > chi_max && (int64_t)s.size() >= chi_max) {
+    double t2 = extra_tail > 0 ? extra_tail * extra_tail : 0.0;
+    for (size_t i = s.size(); i-- > (size_t)chi_max;) t2 += s[i] * s[i];
+    if (std::sqrt(t2) > cutoff + c->eta) {
+      c->how = QT_CERT_CAP;
+      return true;
+    }
+  }
+  if (c->struct_rank > 0 && c->struct_rank <= (int64_t)s.size() && !(extra_tail > c->eta)) {
+    int64_t kr = 0;
+    while (kr < (int64_t)s.size() && s[kr] > c->eta) kr++;
+    if (kr == c->struct_rank) {
+      const int kc = (int)kr;
+      o->k_cut = kc;
+      o->k = chi_max > 0 ? std::min(kc, chi_max) : kc;
+      o->discarded = extra_tail > 0 ? extra_tail * extra_tail : 0.0;
+      for (size_t i = (size_t)o->k; i < s.size(); i++) o->discarded += s[i] * s[i];
+      c->how = QT_CERT_STRUCT;
+      return true;
+    }
+  }
+  c->how = QT_CERT_NONE;
+  return false;
+}
+
 double renorm_scale(const qt_handle* h, const SvdOut& o) {
   if (!h->cfg.renormalize) return 1.0;
   const double kept = o.norm2 - o.discarded;
@@ -638,7 +695,8 @@ int fp32_scale_exponent(double norm2) {
 template <typename TO>
 int svd_split_direct32(qt_handle* h, const float2* theta, int64_t m, int64_t n, double cutoff, int chi_max,
                        TO** Aout, TO** Bout, SvdOut* o, double extra_tail = -1.0, bool fast_freeze = false,
-                       int keep_hint = 0, const float2* proj = nullptr, int64_t proj_n = 0, double out_scale = 1.0) {
+                       int keep_hint = 0, const float2* proj = nullptr, int64_t proj_n = 0, double out_scale = 1.0,
+                       RankCert* cert = nullptr) {
   qt_scratch s(h);
   const bool wide = m < n;
   const int64_t rows = wide ? n : m, cols = wide ? m : n;
@@ -684,6 +742,9 @@ int svd_split_direct32(qt_handle* h, const float2* theta, int64_t m, int64_t n, 
   } else {
     QT_TRY(choose_rank(h, o->s, cutoff, chi_max, o));
   }
+  // a rank decision below the FP32 resolution that nothing certifies is
+  // left to the caller's exact FP64 split
+  if (cert && !certify_rank(o->s, extra_tail, cutoff, chi_max, cert, o)) return QT_UNCERTIFIED;
   const int k = o->k;
   const double sc = renorm_scale(h, *o) * out_scale;
   const float2 one = make_float2(1, 0), zero = make_float2(0, 0);
@@ -796,9 +857,13 @@ int svd_split_cusolver(qt_handle* h, double2* theta, int64_t m, int64_t n, doubl
 // more values than the sketch holds, when the sketch basis lost rank, or when
 // the Jacobi does not settle.  theta is m x n float2 (ld m); it is
 // overwritten by the sketch residual.
+// struct_rank bounds theta's rank in exact arithmetic (0: unknown); with it a
+// cutoff below the FP32 resolution is still decided exactly when theta has
+// no values between the cutoff and that resolution (certify_rank).
 template <typename TO>
 int svd_split_chosen(qt_handle* h, float2* theta, int64_t m, int64_t n, double cutoff, int chi_max, int kpred,
-                     TO** Aout, TO** Bout, SvdOut* o, int* sketch, int* fallback, double* residual) {
+                     TO** Aout, TO** Bout, SvdOut* o, int* sketch, int* fallback, double* residual,
+                     int64_t struct_rank = 0) {
   qt_scratch s(h);
   const int64_t kmin = std::min(m, n);
   double* dn;
@@ -807,7 +872,12 @@ int svd_split_chosen(qt_handle* h, float2* theta, int64_t m, int64_t n, double c
   double tn2 = 0;
   QT_CHECK_CUDA(h, cudaMemcpyAsync(&tn2, dn, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
   QT_CHECK_CUDA(h, cudaStreamSynchronize(h->stream));
-  const double eff_cut = std::max(cutoff, fp32_floor_rel(h, m, n) * std::sqrt(tn2));
+  // the rule runs at the caller's cutoff; eta is the FP32 resolution below
+  // which the decision needs a certificate or the exact split
+  const double eta = fp32_floor_rel(h, m, n) * std::sqrt(tn2);
+  RankCert cert;
+  cert.eta = eta;
+  cert.struct_rank = struct_rank;
   int64_t l = (kpred > 0 ? kpred : kmin) + std::max(0, h->cfg.oversample);
   // A rank predicted at the chi_max cap is pinned there by a spectrum that
   // is still decaying slowly at the cap; a sketch of cap + oversample then
@@ -819,8 +889,10 @@ int svd_split_chosen(qt_handle* h, float2* theta, int64_t m, int64_t n, double c
   // the FP32 noise columns of theta', settles in 5 sweeps instead of ~20 on
   // the whole theta'.
   const bool cap_bound = chi_max > 0 && chi_max < kmin && kpred > 0 && kpred + h->cfg.oversample >= 0.9 * chi_max;
-  // (QT_CAP_SKETCH overrides the factor; tuning)
-  static const double cap_mult = std::getenv("QT_CAP_SKETCH") ? std::atof(std::getenv("QT_CAP_SKETCH")) : 1.125;
+  // (cfg.cap_sketch sets the factor, as the autotuner chooses it; QT_CAP_SKETCH
+  // overrides the default when it is unset)
+  static const double cap_env = std::getenv("QT_CAP_SKETCH") ? std::atof(std::getenv("QT_CAP_SKETCH")) : 1.125;
+  const double cap_mult = h->cfg.cap_sketch > 0 ? h->cfg.cap_sketch : cap_env;
   // (and by at least 64 columns: at chi = 64 a sketch of 80 left 1.006 x)
   if (cap_bound) l = std::max<int64_t>(l, std::max<int64_t>((int64_t)(cap_mult * chi_max), chi_max + 64));
   l = ((l + 7) / 8) * 8;
@@ -829,16 +901,19 @@ int svd_split_chosen(qt_handle* h, float2* theta, int64_t m, int64_t n, double c
   // A sketch of three quarters of the matrix or more saves less in the small
   // SVD than its range finder and orthogonalisation cost: factor theta'
   // directly.
-  const bool fast = cap_bound || fast_freeze_ok(m, n, eff_cut, std::sqrt(tn2));
+  // freezing columns below sqrt(rows) u ||theta|| leaves every value above
+  // eta intact, which is all a certificate below eta looks at
+  const bool fast = cap_bound || cutoff < eta || fast_freeze_ok(m, n, cutoff, std::sqrt(tn2));
   if (4 * l >= 3 * kmin || kmin <= 32) {
     *sketch = 0;
-    const int rc = svd_split_direct32<TO>(h, theta, m, n, eff_cut, chi_max, Aout, Bout, o, -1.0, fast,
-                                          cap_bound ? chi_max : 0);
-    if (rc == QT_ENUMERIC) {  // the FP32-storage Jacobi did not settle: exact FP64 path
+    const int rc = svd_split_direct32<TO>(h, theta, m, n, cutoff, chi_max, Aout, Bout, o, -1.0, fast,
+                                          cap_bound ? chi_max : 0, nullptr, 0, 1.0, &cert);
+    h->cert_count[cert.how]++;
+    if (rc == QT_ENUMERIC || rc == QT_UNCERTIFIED) {  // no settled Jacobi / no certified rank: exact FP64 path
       qt_dfree(h, *Aout);
       qt_dfree(h, *Bout);
       *Aout = *Bout = nullptr;
-      *fallback = 2;
+      *fallback = rc == QT_ENUMERIC ? 2 : 4;
       return QT_OK;
     }
     return rc;
@@ -849,7 +924,8 @@ int svd_split_chosen(qt_handle* h, float2* theta, int64_t m, int64_t n, double c
   const int e = fp32_scale_exponent(tn2);
   const double up = std::ldexp(1.0, e);
   if (e) QT_LAUNCH(h, scale_pow2_kernel<float2>, 256, 256, 0, theta, m * n, 1.0 / up);
-  const double cut_s = e ? eff_cut / up : eff_cut;
+  const double cut_s = e ? cutoff / up : cutoff;
+  cert.eta = e ? eta / up : eta;
   const float2 one = make_float2(1, 0), zero = make_float2(0, 0), mone = make_float2(-1, 0);
   // The sketch spans theta's row space: Y (n x l) orthonormal, C = theta Y
   // (m x l) tall, so its one-sided Jacobi carries no V; A' comes from C and
@@ -894,12 +970,13 @@ int svd_split_chosen(qt_handle* h, float2* theta, int64_t m, int64_t n, double c
   // the split of the tall C (m x l): A' from its Jacobi, B' = A'^H theta
   {
     const int rc = svd_split_direct32<TO>(h, Cm, m, l, cut_s, chi_max, Aout, Bout, o, *residual, fast,
-                                          cap_bound ? chi_max : 0, theta, n, up);
-    if (rc == QT_ENUMERIC) {  // the small SVD did not settle: exact FP64 path
+                                          cap_bound ? chi_max : 0, theta, n, up, &cert);
+    h->cert_count[cert.how]++;
+    if (rc == QT_ENUMERIC || rc == QT_UNCERTIFIED) {  // no settled small SVD / no certified rank: exact FP64 path
       qt_dfree(h, *Aout);
       qt_dfree(h, *Bout);
       *Aout = *Bout = nullptr;
-      *fallback = 2;
+      *fallback = rc == QT_ENUMERIC ? 2 : 4;
       return QT_OK;
     }
     QT_TRY(rc);
@@ -928,7 +1005,7 @@ int svd_split_chosen(qt_handle* h, float2* theta, int64_t m, int64_t n, double c
 // Plain mode runs the exact FP64 path; chosen mode on complex64 keeps FP32
 // storage.
 int qt_split_device(qt_handle* h, int dtype, const void* M, int64_t m, int64_t n, double cutoff, int chi_max, int mode,
-                    void** A, void** B, int* k, double* discarded) {
+                    void** A, void** B, int* k, double* discarded, int64_t struct_rank) {
   SvdOut o;
   *A = *B = nullptr;
   int rc;
@@ -949,15 +1026,33 @@ int qt_split_device(qt_handle* h, int dtype, const void* M, int64_t m, int64_t n
     double n2 = 0;
     QT_CHECK_CUDA(h, cudaMemcpyAsync(&n2, dn, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     QT_CHECK_CUDA(h, cudaStreamSynchronize(h->stream));
-    const double cut = std::max(cutoff, fp32_floor_rel(h, m, n) * std::sqrt(n2));
-    rc = svd_split_direct32<float2>(h, (const float2*)M, m, n, cut, chi_max, (float2**)A, (float2**)B, &o, -1.0,
-                                    fast_freeze_ok(m, n, cut, std::sqrt(n2)));
+    RankCert cert;
+    cert.eta = fp32_floor_rel(h, m, n) * std::sqrt(n2);
+    cert.struct_rank = struct_rank;
+    rc = svd_split_direct32<float2>(h, (const float2*)M, m, n, cutoff, chi_max, (float2**)A, (float2**)B, &o, -1.0,
+                                    cutoff < cert.eta || fast_freeze_ok(m, n, cutoff, std::sqrt(n2)), 0, nullptr, 0,
+                                    1.0, &cert);
+    h->cert_count[cert.how]++;
+    if (rc == QT_UNCERTIFIED || rc == QT_ENUMERIC) {  // the exact FP64 split decides
+      qt_dfree(h, *A);
+      qt_dfree(h, *B);
+      *A = *B = nullptr;
+      double2* Mc;
+      QT_TRY(s.get(&Mc, (size_t)m * n));
+      QT_TRY(qt_convert(h, M, QT_C64, Mc, QT_C128, m * n));
+      o = SvdOut();
+      rc = svd_split_jacobi<double2, float2>(h, Mc, m, n, cutoff, chi_max, false, (float2**)A, (float2**)B, &o);
+      if (rc != QT_OK) rc = QT_EFALLBACK_FAILED;
+    }
   } else {
     qt_scratch s(h);
     double2* Mc;
     QT_TRY(s.get(&Mc, (size_t)m * n));
     QT_TRY(qt_convert(h, M, QT_C64, Mc, QT_C128, m * n));
-    rc = svd_split_jacobi<double2, float2>(h, Mc, m, n, cutoff, chi_max, false, (float2**)A, (float2**)B, &o);
+    if (mode == QT_MODE_CUSOLVER)
+      rc = svd_split_cusolver<float2>(h, Mc, m, n, cutoff, chi_max, (float2**)A, (float2**)B, &o);
+    else
+      rc = svd_split_jacobi<double2, float2>(h, Mc, m, n, cutoff, chi_max, false, (float2**)A, (float2**)B, &o);
   }
   if (rc == QT_OK) rc = qt_check_status(h);
   if (rc != QT_OK) {
@@ -1009,7 +1104,14 @@ static int update_impl(qt_handle* h, qt_mps* mps, int site, const double* G, dou
         QT_TRY(qt_theta_gate(h, mps->dtype, mps->site[site], mps->site[site + 1], cl, cm, cr, G, 1, th));
       }
       kpred = qt_rank_model_predict(h, feat, kmax);
-      rc = svd_split_chosen<TO>(h, th, m, n, cutoff, chi_max, kpred, &An, &Bn, &o, &sketch, &fallback, &residual);
+      // exact-arithmetic rank bound of theta' = G (A B): the gate's
+      // operator-Schmidt rank times the inner bond, and the Hilbert-space
+      // dimensions of the qubits left and right of the bond
+      int64_t srank = std::min<int64_t>(std::min(m, n), (int64_t)qt_gate_schmidt_rank(G) * cm);
+      if (site + 1 < 40) srank = std::min<int64_t>(srank, (int64_t)1 << (site + 1));
+      if (mps->nsites - site - 1 < 40) srank = std::min<int64_t>(srank, (int64_t)1 << (mps->nsites - site - 1));
+      rc = svd_split_chosen<TO>(h, th, m, n, cutoff, chi_max, kpred, &An, &Bn, &o, &sketch, &fallback, &residual,
+                                srank);
       if (rc == QT_OK && fallback) {
         qt_dfree(h, An);
         qt_dfree(h, Bn);
@@ -1237,11 +1339,11 @@ extern "C" int qt_contract_pair(qt_handle* h, int dtype, int ndA, const int64_t*
 
 namespace {
 
-// Exact truncated SVD of a host matrix in FP64 (any dtype), results in FP64.
-// Host-facing truncated SVD.  M64 (FP64 copy of the input) feeds the exact
-// paths; M32 (the complex64 input itself, chosen mode) feeds the FP32-storage
-// QR-preconditioned Jacobi, whose cutoff is floored at the FP32 noise level
-// 4 sqrt(max(m, n)) u_fp32 ||M||_F (the chosen-mode precision contract).
+// Host-facing truncated SVD, results in FP64.  M64 (FP64 copy of the input)
+// feeds the exact paths; M32 (the complex64 input itself, chosen mode) feeds
+// the FP32-storage Jacobi, whose rank decision at a cutoff below its
+// resolution 4 sqrt(max(m, n)) u_fp32 ||M||_F is certified by the chi_max cap
+// or left to the exact FP64 split of M64.
 int host_truncated_svd64(qt_handle* h, const double2* M64, const float2* M32, int64_t m, int64_t n, double cutoff,
                          int chi_max, int mode, std::vector<double2>* U, std::vector<double>* S,
                          std::vector<double2>* Vh, int* k, double* disc) {
@@ -1259,9 +1361,23 @@ int host_truncated_svd64(qt_handle* h, const double2* M64, const float2* M32, in
     double n2 = 0;
     QT_CHECK_CUDA(h, cudaMemcpyAsync(&n2, dn, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     QT_CHECK_CUDA(h, cudaStreamSynchronize(h->stream));
-    const double cut = std::max(cutoff, fp32_floor_rel(h, m, n) * std::sqrt(n2));
-    rc = svd_split_direct32<double2>(h, dM, m, n, cut, chi_max, &A, &B, &o, -1.0,
-                                     fast_freeze_ok(m, n, cut, std::sqrt(n2)));
+    RankCert cert;
+    cert.eta = fp32_floor_rel(h, m, n) * std::sqrt(n2);
+    rc = svd_split_direct32<double2>(h, dM, m, n, cutoff, chi_max, &A, &B, &o, -1.0,
+                                     cutoff < cert.eta || fast_freeze_ok(m, n, cutoff, std::sqrt(n2)), 0, nullptr, 0,
+                                     1.0, &cert);
+    h->cert_count[cert.how]++;
+    if (rc == QT_UNCERTIFIED || rc == QT_ENUMERIC) {  // the exact FP64 split decides
+      qt_dfree(h, A);
+      qt_dfree(h, B);
+      A = B = nullptr;
+      double2* dM64;
+      QT_TRY(s.get(&dM64, (size_t)m * n));
+      QT_CHECK_CUDA(h, cudaMemcpyAsync(dM64, M64, sizeof(double2) * m * n, cudaMemcpyHostToDevice, h->stream));
+      o = SvdOut();
+      rc = svd_split_jacobi<double2, double2>(h, dM64, m, n, cutoff, chi_max, false, &A, &B, &o);
+      if (rc != QT_OK) rc = QT_EFALLBACK_FAILED;
+    }
   } else {
     double2* dM;
     QT_TRY(s.get(&dM, (size_t)m * n));

@@ -22,6 +22,13 @@ struct qt_profile_rec {
   cudaEvent_t start, stop;
 };
 
+// Internal return code (never crosses the ABI): a chosen-mode rank decision
+// that the FP32-level split cannot certify; the caller takes the exact FP64
+// split instead.
+constexpr int QT_UNCERTIFIED = 1;
+// How a chosen-mode rank decision was certified (qt_cert_counters slots).
+enum { QT_CERT_NONE = 0, QT_CERT_RESOLVED = 1, QT_CERT_CAP = 2, QT_CERT_STRUCT = 3, QT_CERT_SLOTS = 4 };
+
 struct qt_handle {
   qt_config cfg;
   int device = 0;
@@ -41,6 +48,7 @@ struct qt_handle {
   double work_jacobi_bytes = 0, work_jacobi_rounds = 0, work_tc_flops = 0, work_tc_launches = 0;
   double work_jacobi_pairs = 0, work_jacobi_inner = 0;  // rotated pairs, pair-solver inner sweeps
   double work_jacobi_gram_bytes = 0, work_jacobi_rot_bytes = 0;  // X read by the Gram products; X, V rewritten
+  int64_t cert_count[QT_CERT_SLOTS] = {};  // chosen-mode rank decisions by QT_CERT_* (NONE: fell back)
   bool prof = false;
   std::vector<qt_profile_rec> prof_recs;
   std::vector<cudaEvent_t> event_pool;

@@ -35,6 +35,10 @@ void qt_rank_model_destroy(qt_rank_model* m);
 // 16 features of the update on bond (site, site+1) of mps with gate G.
 void qt_rank_features(const qt_mps* mps, int site, const double* G, double cutoff, int chi_max, float* f);
 int qt_rank_kmax(const qt_mps* mps, int site, int chi_max);
+// Operator-Schmidt rank of a 4x4 gate (complex128, column-major): the number
+// of its operator-Schmidt values above 1e-12 of the largest (1 for a product
+// of one-qubit gates, 2 for CNOT, 4 for SWAP and generic gates).
+int qt_gate_schmidt_rank(const double* G);
 
 // Predicted kept rank (>= 1), or -1 when no trained model is active.
 int qt_rank_model_predict(qt_handle* h, const float* feat, int kmax);
