@@ -151,7 +151,9 @@ int qt_host_free(void* p);
 /* Pairwise contraction with ncon semantics: contract legs axesA[i] of A with
  * axesB[i] of B (0-based); the result's legs are A's free legs in order, then
  * B's.  Replaces the TensorOperations.ncon pairwise step called at
- * src/contract.jl:257,263 (and the products of src/svd.jl:35). */
+ * src/contract.jl:257,263 (and the products of src/svd.jl:35).  The operands
+ * are uploaded and contracted by qt_tensor_contract (permutes folded into the
+ * GEMM operand gathers on the device). */
 int qt_contract_pair(qt_handle* h, int dtype,
                      int ndA, const int64_t* dimsA, const void* A,
                      int ndB, const int64_t* dimsB, const void* B,
@@ -203,6 +205,34 @@ int qt_contract_svd(qt_handle* h, int dtype,
                     int nd1, const int64_t* dims1, const void* T1,
                     int nd2, const int64_t* dims2, const void* T2,
                     int i1, int i2, double er, void* out);
+
+/* ---- device-resident tensors (the operands of ncon's pairwise steps) ----
+ * A qt_tensor is a column-major complex64/complex128 tensor in HBM.  A
+ * network is contracted by uploading its tensors once and chaining
+ * qt_tensor_contract / qt_tensor_trace steps in ncon's order (the schedule
+ * of TensorOperations.ncon under src/contract.jl:257,263), downloading only
+ * the result: no intermediate leaves the device and no permute runs on the
+ * host. */
+typedef struct qt_tensor qt_tensor;
+/* host may be NULL (a zero tensor); the library copies the data. */
+int qt_tensor_create(qt_handle* h, int dtype, int nd, const int64_t* dims, const void* host, qt_tensor** out);
+int qt_tensor_free(qt_handle* h, qt_tensor* t);
+int qt_tensor_ndims(const qt_tensor* t);
+int qt_tensor_dims(const qt_tensor* t, int64_t* dims);
+int qt_tensor_download(qt_handle* h, const qt_tensor* t, void* host);
+/* *out = A contracted with B over legs axesA[i] <-> axesB[i] (0-based); its
+ * legs are A's free legs then B's, reordered by out_perm when not NULL
+ * (out leg i = natural leg out_perm[i]).  ncontract = 0 is the outer product.
+ * complex64 with cfg.tc_gemm runs the tcgen05 split-TF32x3 GEMM, its operand
+ * planes gathered straight from A and B through offset tables; otherwise a
+ * tiled gather writes the operand matrices for the SIMT GEMM. */
+int qt_tensor_contract(qt_handle* h, const qt_tensor* A, const qt_tensor* B, int ncontract, const int* axesA,
+                       const int* axesB, const int* out_perm, qt_tensor** out);
+/* *out = the legs of A in the order perm (out leg i = leg perm[i] of A):
+ * permutedims of src/contract.jl:243-245 and ncon's final leg order. */
+int qt_tensor_permute(qt_handle* h, const qt_tensor* A, const int* perm, qt_tensor** out);
+/* *out = A traced over legs ax1 and ax2 (a label repeated on one tensor). */
+int qt_tensor_trace(qt_handle* h, const qt_tensor* A, int ax1, int ax2, qt_tensor** out);
 
 /* ---- device-resident MPS ------------------------------------------------ */
 

@@ -101,6 +101,14 @@ def library() -> C.CDLL:
         "qt_cert_counters": (I, [P, C.POINTER(L)]),
         "qt_gemm": (I, [P, I, I, I, L, L, L, C.POINTER(D), P, L, P, L, C.POINTER(D), P, L]),
         "qt_contract_pair": (I, [P, I, I, C.POINTER(L), P, I, C.POINTER(L), P, I, C.POINTER(I), C.POINTER(I), P]),
+        "qt_tensor_create": (I, [P, I, I, C.POINTER(L), P, C.POINTER(P)]),
+        "qt_tensor_free": (I, [P, P]),
+        "qt_tensor_ndims": (I, [P]),
+        "qt_tensor_dims": (I, [P, C.POINTER(L)]),
+        "qt_tensor_download": (I, [P, P, P]),
+        "qt_tensor_contract": (I, [P, P, P, I, C.POINTER(I), C.POINTER(I), C.POINTER(I), C.POINTER(P)]),
+        "qt_tensor_permute": (I, [P, P, C.POINTER(I), C.POINTER(P)]),
+        "qt_tensor_trace": (I, [P, P, I, I, C.POINTER(P)]),
         "qt_truncated_svd": (I, [P, I, L, L, P, D, I, I, P, C.POINTER(D), P, C.POINTER(I), C.POINTER(D)]),
         "qt_contract_svd": (I, [P, I, I, C.POINTER(L), P, I, C.POINTER(L), P, I, I, D, P]),
         "qt_mps_create": (I, [P, I, C.POINTER(L), C.POINTER(P), I, C.POINTER(P)]),
@@ -349,6 +357,10 @@ class Engine:
         self._check(self._lib.qt_contract_pair(self._h, _dtype_code(dt), A.ndim, dA, _ptr(A), B.ndim, dB, _ptr(B), nc,
                                                (C.c_int * nc)(*axesA), (C.c_int * nc)(*axesB), _ptr(out)))
         return out
+
+    def tensor(self, data, dtype=None) -> "DeviceTensor":
+        """A device-resident copy of a host tensor (column-major)."""
+        return DeviceTensor(self, data, dtype)
 
     def gemm(self, A: np.ndarray, B: np.ndarray, opA: str = "N", opB: str = "N", alpha=1.0, beta=0.0, out=None):
         """alpha op(A) op(B) + beta out on the device (op "N" or "C"); complex64 or complex128."""
@@ -630,6 +642,71 @@ class DeviceMPS:
             pass
 
 
+class DeviceTensor:
+    """A column-major complex tensor resident in the engine's device memory
+    (``qt_tensor``): the operand of ncon's pairwise steps on the GPU."""
+
+    def __init__(self, eng: "Engine", data=None, dtype=None, _handle=None):
+        self.eng = eng
+        if _handle is not None:
+            self._p = _handle
+        else:
+            a = np.asarray(data)
+            dt = np.dtype(dtype) if dtype is not None else np.result_type(a.dtype, np.complex64)
+            a = np.asfortranarray(a.astype(dt))
+            dims = (C.c_int64 * max(a.ndim, 1))(*a.shape)
+            self._p = C.c_void_p()
+            eng._check(eng._lib.qt_tensor_create(eng._h, _dtype_code(dt), a.ndim, dims, _ptr(a), C.byref(self._p)))
+        nd = eng._lib.qt_tensor_ndims(self._p)
+        dims = (C.c_int64 * max(nd, 1))()
+        eng._lib.qt_tensor_dims(self._p, dims)
+        self.shape = tuple(int(dims[i]) for i in range(nd))
+
+    @property
+    def ndim(self) -> int:
+        return len(self.shape)
+
+    def contract(self, other: "DeviceTensor", axes_self: Sequence[int], axes_other: Sequence[int],
+                 out_perm: Optional[Sequence[int]] = None) -> "DeviceTensor":
+        """The ncon pairwise step on the device: legs axes_self of this
+        tensor with axes_other of ``other`` (0-based); result legs: this
+        tensor's free legs then ``other``'s, reordered by ``out_perm``."""
+        nc = len(axes_self)
+        p = C.c_void_p()
+        perm = None if out_perm is None else (C.c_int * max(len(out_perm), 1))(*out_perm)
+        self.eng._check(self.eng._lib.qt_tensor_contract(self.eng._h, self._p, other._p, nc,
+                                                         (C.c_int * max(nc, 1))(*axes_self),
+                                                         (C.c_int * max(nc, 1))(*axes_other), perm, C.byref(p)))
+        return DeviceTensor(self.eng, _handle=p)
+
+    def trace(self, ax1: int, ax2: int) -> "DeviceTensor":
+        p = C.c_void_p()
+        self.eng._check(self.eng._lib.qt_tensor_trace(self.eng._h, self._p, ax1, ax2, C.byref(p)))
+        return DeviceTensor(self.eng, _handle=p)
+
+    def permute(self, perm: Sequence[int]) -> "DeviceTensor":
+        p = C.c_void_p()
+        self.eng._check(self.eng._lib.qt_tensor_permute(self.eng._h, self._p,
+                                                        (C.c_int * max(len(perm), 1))(*perm), C.byref(p)))
+        return DeviceTensor(self.eng, _handle=p)
+
+    def numpy(self, dtype) -> np.ndarray:
+        out = np.zeros(self.shape if self.shape else (1,), dtype=dtype, order="F")
+        self.eng._check(self.eng._lib.qt_tensor_download(self.eng._h, self._p, _ptr(out)))
+        return out if self.shape else out.reshape(())
+
+    def free(self):
+        if self._p and self.eng._h:
+            self.eng._lib.qt_tensor_free(self.eng._h, self._p)
+        self._p = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
 class Batch:
     """Many independent circuits' MPS (complex64) updated layer by layer by
     one persistent kernel per layer (optionally replayed from a CUDA graph)."""
@@ -841,18 +918,25 @@ def contract_order(shapes, labels):
 
 
 def contract(engine: "Engine", tensors, contractions, openidx, optimize: bool = False, order=None) -> np.ndarray:
-    """``contract(net, optimize)`` of src/contract.jl:242-264 with every
-    pairwise product on the GPU (``qt_contract_pair``).  The schedule is
-    TensorOperations.ncon's: positive labels in ascending order (or in
-    ``order``), each step contracting every label the two operands share; a
-    label repeated on one tensor is traced (a product with the identity);
-    disconnected parts are joined by outer products; the result's axes run
-    -1, -2, ...  With ``optimize`` the labels are renumbered by their position
-    in ``contract_order``'s sequence and contracted with ``order=sequence``,
-    as the reference does.  The final axis order is a host-side transpose of
-    the result (layout only)."""
-    if len(tensors) == 1:
-        return np.transpose(np.asarray(tensors[0]), [leg - 1 for (_, leg) in openidx])
+    """``contract(net, optimize)`` of src/contract.jl:242-264 on the GPU.  The
+    network's tensors are uploaded once and stay in device memory; every
+    pairwise product, trace and the final leg order run on the device
+    (``qt_tensor_contract``, ``qt_tensor_trace``, ``qt_tensor_permute``) and
+    only the result is downloaded.  The schedule is TensorOperations.ncon's:
+    positive labels in ascending order (or in ``order``), each step
+    contracting every label the two operands share; a label repeated on one
+    tensor is traced; disconnected parts are joined by outer products; the
+    result's axes run -1, -2, ...  With ``optimize`` the labels are
+    renumbered by their position in ``contract_order``'s sequence and
+    contracted with ``order=sequence``, as the reference does."""
+    dt = np.result_type(*[np.asarray(t).dtype for t in tensors], np.complex64)
+    if len(tensors) == 1:  # src/contract.jl:243-245: permutedims only
+        t = engine.tensor(tensors[0], dt)
+        out = t.permute([leg - 1 for (_, leg) in openidx]) if t.ndim else t
+        res = out.numpy(dt)
+        t.free()
+        out.free()
+        return res
     labels = contract_rep(tensors, contractions, openidx)
     if optimize and order is None:
         if any(len({v for v in l if v > 0}) != sum(1 for v in l if v > 0) for l in labels):
@@ -861,7 +945,7 @@ def contract(engine: "Engine", tensors, contractions, openidx, optimize: bool = 
         pos = {lab: k for k, lab in enumerate(sequence, 1)}
         labels = [[pos[v] if v > 0 else v for v in l] for l in labels]
         order = list(sequence)
-    work = [(np.asarray(t), list(l)) for t, l in zip(tensors, labels)]
+    work = [(engine.tensor(t, dt), list(l)) for t, l in zip(tensors, labels)]
     for lab in (order if order is not None else sorted({v for l in labels for v in l if v > 0})):
         holders = [k for k, (_, l) in enumerate(work) if lab in l]
         if not holders:
@@ -869,21 +953,30 @@ def contract(engine: "Engine", tensors, contractions, openidx, optimize: bool = 
         if len(holders) == 1:
             t, l = work[holders[0]]
             a, b = [i for i, v in enumerate(l) if v == lab]
-            eye = np.eye(t.shape[a], dtype=np.result_type(t.dtype, np.complex64))
-            t = engine.contract_pair(t, eye, [a, b], [0, 1])
-            work[holders[0]] = (t, [v for i, v in enumerate(l) if i not in (a, b)])
+            work[holders[0]] = (t.trace(a, b), [v for i, v in enumerate(l) if i not in (a, b)])
+            t.free()
             continue
         ka, kb = holders
         (ta, la), (tb, lb) = work[ka], work[kb]
         common = [v for v in la if v > 0 and v in lb]
-        t = engine.contract_pair(ta, tb, [la.index(v) for v in common], [lb.index(v) for v in common])
+        t = ta.contract(tb, [la.index(v) for v in common], [lb.index(v) for v in common])
+        ta.free()
+        tb.free()
         l = [v for v in la if v not in common] + [v for v in lb if v not in common]
         work = [w for k, w in enumerate(work) if k not in (ka, kb)] + [(t, l)]
     t, l = work[0]
     for tb, lb in work[1:]:
-        t = engine.contract_pair(t, tb, [], [])
-        l = l + lb
-    return np.transpose(t, sorted(range(len(l)), key=lambda i: -l[i])) if l else t
+        t2 = t.contract(tb, [], [])
+        t.free()
+        tb.free()
+        t, l = t2, l + lb
+    if l:
+        out = t.permute(sorted(range(len(l)), key=lambda i: -l[i]))
+        t.free()
+        t = out
+    res = t.numpy(dt)
+    t.free()
+    return res
 
 
 def contract_svd_mps(engine: "Engine", tensors, contractions=(), er: float = 0.0) -> np.ndarray:

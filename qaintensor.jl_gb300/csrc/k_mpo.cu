@@ -84,9 +84,6 @@ int apply_mpo_t(qt_handle* h, qt_mps* mps, const double2* const* dW, const int* 
 
 }  // namespace
 
-// the truncated split used by the sweep (qt_engine.cu)
-int qt_split_device(qt_handle* h, int dtype, const void* M, int64_t m, int64_t n, double cutoff, int chi_max, int mode,
-                    void** A, void** B, int* k, double* discarded, int64_t struct_rank);
 
 extern "C" int qt_mps_apply_mpo(qt_handle* h, qt_mps* mps, const double* const* W, const int64_t* dims) {
   // W[i]: (bl, 2, 2, br) complex128 column-major interleaved; dims 4 per site

@@ -350,6 +350,73 @@ __global__ void gather_b_kernel(const float2* __restrict__ src, int64_t ldb, int
   }
 }
 
+// The same planes from a permuted view of an N-d tensor: op(A)(m, k) =
+// src[rowoff[m] + coloff[k]] (rowoff over A's free legs, coloff over its
+// contracted legs, both in element strides of the source).  This is the ncon
+// permute folded into the operand gather: no permuted copy of A is written.
+// rows_fast: the source's unit-stride leg is a row leg (threads load along
+// m), otherwise a column leg (threads load along k).
+__global__ void gather_a_map_kernel(const float2* __restrict__ src, const int64_t* __restrict__ rowoff,
+                                    const int64_t* __restrict__ coloff, int rows_fast, int M, int K, int Mp, int Kp,
+                                    float* __restrict__ planes) {
+  __shared__ float2 tile[32][33];
+  const int m0 = blockIdx.y * 32, k0 = blockIdx.x * 32;
+  for (int r = threadIdx.y; r < 32; r += 8) {
+    if (rows_fast) {
+      const int m = m0 + threadIdx.x, k = k0 + r;
+      tile[threadIdx.x][r] = (m < M && k < K) ? src[rowoff[m] + coloff[k]] : make_float2(0.f, 0.f);
+    } else {
+      const int m = m0 + r, k = k0 + threadIdx.x;
+      tile[r][threadIdx.x] = (m < M && k < K) ? src[rowoff[m] + coloff[k]] : make_float2(0.f, 0.f);
+    }
+  }
+  __syncthreads();
+  const size_t plane = (size_t)Mp * Kp;
+  for (int r = threadIdx.y; r < 32; r += 8) {
+    const int m = m0 + r, k = k0 + threadIdx.x;
+    if (m >= Mp || k >= Kp) continue;
+    const float2 v = tile[r][threadIdx.x];
+    const float hr = tf32_rna(v.x), hi = tf32_rna(v.y);
+    const size_t o = (size_t)m * Kp + k;
+    planes[o] = hr;
+    planes[o + plane] = hi;
+    planes[o + 2 * plane] = tf32_rna(v.x - hr);
+    planes[o + 3 * plane] = tf32_rna(v.y - hi);
+  }
+}
+
+// B planes from op(B)(k, n) = src[rowoff[k] + coloff[n]] (rowoff over B's
+// contracted legs, coloff over its free legs); rows_fast: unit stride in k.
+__global__ void gather_b_map_kernel(const float2* __restrict__ src, const int64_t* __restrict__ rowoff,
+                                    const int64_t* __restrict__ coloff, int rows_fast, int K, int N, int N2p, int Kp,
+                                    float* __restrict__ planes) {
+  __shared__ float2 tile[32][33];  // [n][k]
+  const int n0 = blockIdx.y * 32, k0 = blockIdx.x * 32;
+  for (int r = threadIdx.y; r < 32; r += 8) {
+    if (rows_fast) {
+      const int n = n0 + r, k = k0 + threadIdx.x;
+      tile[r][threadIdx.x] = (n < N && k < K) ? src[rowoff[k] + coloff[n]] : make_float2(0.f, 0.f);
+    } else {
+      const int n = n0 + threadIdx.x, k = k0 + r;
+      tile[threadIdx.x][r] = (n < N && k < K) ? src[rowoff[k] + coloff[n]] : make_float2(0.f, 0.f);
+    }
+  }
+  __syncthreads();
+  const size_t plane = (size_t)N2p * Kp;
+  for (int r = threadIdx.y; r < 32; r += 8) {
+    const int n = n0 + r, k = k0 + threadIdx.x;
+    if (2 * n >= N2p || k >= Kp) continue;
+    const float2 v = tile[r][threadIdx.x];
+    const float hr = tf32_rna(v.x), hi = tf32_rna(v.y);
+    const float lr = tf32_rna(v.x - hr), li = tf32_rna(v.y - hi);
+    const size_t o0 = (size_t)(2 * n) * Kp + k, o1 = o0 + Kp;
+    planes[o0] = hr;               planes[o1] = hi;
+    planes[o0 + plane] = lr;       planes[o1 + plane] = li;
+    planes[o0 + 2 * plane] = -hi;  planes[o1 + 2 * plane] = hr;
+    planes[o0 + 3 * plane] = -li;  planes[o1 + 3 * plane] = lr;
+  }
+}
+
 PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
 std::once_flag g_encode_once;
 
@@ -385,6 +452,38 @@ int qt_cgemm_c64(qt_handle* h, int opA, int opB, int64_t M, int64_t N, int64_t K
   return qt_cgemm<float2>(h, opA, opB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc);
 }
 
+namespace {
+
+// The tensor-core GEMM on planes already gathered (pa: 4 x Mp x Kp, pb: 4 x
+// N2p x Kp); C (M x N) = alpha A B + beta C.
+int tc_gemm_planes(qt_handle* h, float* pa, float* pb, int64_t M, int64_t N, int64_t K, int64_t Mp, int64_t N2p,
+                   int64_t Kp, float2 alpha, float2 beta, float2* C, int64_t ldc, int* status) {
+  CUtensorMap ma, mb;
+  if (!make_map(&ma, pa, (int)Kp, (int)Mp, BM) || !make_map(&mb, pb, (int)Kp, (int)N2p, BN))
+    return qt_fail(h, QT_ECUDA, "tc gemm: tensor map encoding failed");
+  static bool attr_set = false;
+  if (!attr_set) {
+    QT_CHECK_CUDA(h, cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
+    attr_set = true;
+  }
+  TcParams p;
+  p.M = (int)M; p.N = (int)N; p.Kp = (int)Kp; p.Mp = (int)Mp; p.N2p = (int)N2p;
+  p.alpha = alpha; p.beta = beta; p.C = C; p.ldc = ldc; p.status = status;
+  dim3 grid((unsigned)(Mp / BM), (unsigned)(N2p / BN));
+  QT_LAUNCH(h, tc_gemm_kernel, grid, NTHREADS, SMEM_BYTES, ma, mb, p);
+  h->work_tc_flops += 24.0 * (double)M * (double)N * (double)K;
+  h->work_tc_launches += 1;
+  if (status != h->d_status) {  // a handle without a status word: check here
+    int hs = 0;
+    QT_CHECK_CUDA(h, cudaMemcpyAsync(&hs, status, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    QT_CHECK_CUDA(h, cudaStreamSynchronize(h->stream));
+    if (hs) return qt_fail(h, QT_ETIMEOUT, "tc gemm: a pipeline wait timed out");
+  }
+  return QT_OK;
+}
+
+}  // namespace
+
 // C (M x N) = alpha op(A) op(B) + beta C on the tensor cores; op in {N, C}.
 int qt_cgemm_tc(qt_handle* h, int opA, int opB, int64_t M, int64_t N, int64_t K, float2 alpha, const float2* A,
                 int64_t lda, const float2* B, int64_t ldb, float2 beta, float2* C, int64_t ldc) {
@@ -411,26 +510,38 @@ int qt_cgemm_tc(qt_handle* h, int opA, int opB, int64_t M, int64_t N, int64_t K,
     QT_LAUNCH(h, gather_b_kernel, grid, dim3(32, 8), 0, B, ldb, opB == QT_OP_C ? 1 : 0, (int)K, (int)N, (int)N2p,
               (int)Kp, pb);
   }
-  CUtensorMap ma, mb;
-  if (!make_map(&ma, pa, (int)Kp, (int)Mp, BM) || !make_map(&mb, pb, (int)Kp, (int)N2p, BN))
-    return qt_fail(h, QT_ECUDA, "tc gemm: tensor map encoding failed");
-  static bool attr_set = false;
-  if (!attr_set) {
-    QT_CHECK_CUDA(h, cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
-    attr_set = true;
+  return tc_gemm_planes(h, pa, pb, M, N, K, Mp, N2p, Kp, alpha, beta, C, ldc, status);
+}
+
+// C (M x N, ld M) = A_view B_view on the tensor cores, the operands read
+// through offset tables (device arrays): A_view(m, k) = A[a_row[m] +
+// a_col[k]], B_view(k, n) = B[b_row[k] + b_col[n]] -- the pairwise ncon
+// contraction with its permutes folded into the operand gathers.
+int qt_cgemm_tc_mapped(qt_handle* h, int64_t M, int64_t N, int64_t K, const float2* A, const int64_t* a_row,
+                       const int64_t* a_col, int a_rows_fast, const float2* B, const int64_t* b_row,
+                       const int64_t* b_col, int b_rows_fast, float2* C) {
+  if (M <= 0 || N <= 0) return QT_OK;
+  if (!encode_fn()) return qt_fail(h, QT_ENOTSUP, "tc gemm: cuTensorMapEncodeTiled unavailable");
+  const int64_t Mp = round_up(M, BM), N2p = round_up(2 * N, BN), Kp = round_up(std::max<int64_t>(K, 1), BK);
+  qt_scratch s(h);
+  float *pa, *pb;
+  int* status = h->d_status;
+  QT_TRY(s.get(&pa, (size_t)4 * Mp * Kp));
+  QT_TRY(s.get(&pb, (size_t)4 * N2p * Kp));
+  if (!status) {
+    QT_TRY(s.get(&status, 1));
+    QT_CHECK_CUDA(h, cudaMemsetAsync(status, 0, sizeof(int), h->stream));
   }
-  TcParams p;
-  p.M = (int)M; p.N = (int)N; p.Kp = (int)Kp; p.Mp = (int)Mp; p.N2p = (int)N2p;
-  p.alpha = alpha; p.beta = beta; p.C = C; p.ldc = ldc; p.status = status;
-  dim3 grid((unsigned)(Mp / BM), (unsigned)(N2p / BN));
-  QT_LAUNCH(h, tc_gemm_kernel, grid, NTHREADS, SMEM_BYTES, ma, mb, p);
-  h->work_tc_flops += 24.0 * (double)M * (double)N * (double)K;
-  h->work_tc_launches += 1;
-  if (status != h->d_status) {  // a handle without a status word: check here
-    int hs = 0;
-    QT_CHECK_CUDA(h, cudaMemcpyAsync(&hs, status, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
-    QT_CHECK_CUDA(h, cudaStreamSynchronize(h->stream));
-    if (hs) return qt_fail(h, QT_ETIMEOUT, "tc gemm: a pipeline wait timed out");
+  {
+    dim3 grid((unsigned)(Kp / 32), (unsigned)(Mp / 32));
+    QT_LAUNCH(h, gather_a_map_kernel, grid, dim3(32, 8), 0, A, a_row, a_col, a_rows_fast, (int)M, (int)K, (int)Mp,
+              (int)Kp, pa);
   }
-  return QT_OK;
+  {
+    dim3 grid((unsigned)(Kp / 32), (unsigned)(N2p / 2 / 32 + ((N2p / 2) % 32 ? 1 : 0)));
+    QT_LAUNCH(h, gather_b_map_kernel, grid, dim3(32, 8), 0, B, b_row, b_col, b_rows_fast, (int)K, (int)N,
+              (int)N2p, (int)Kp, pb);
+  }
+  return tc_gemm_planes(h, pa, pb, M, N, K, Mp, N2p, Kp, make_float2(1.f, 0.f), make_float2(0.f, 0.f), C, M,
+                        status);
 }

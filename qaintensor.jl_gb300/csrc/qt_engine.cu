@@ -1218,75 +1218,8 @@ extern "C" int qt_mps_norm2(qt_handle* h, const qt_mps* mps, double* out) {
 // dense primitives on host buffers
 // ---------------------------------------------------------------------------
 
-namespace {
-
-// Column-major permutation of a host tensor: out[new index] = in[old], where
-// new leg i is old leg perm[i].
-template <typename T>
-void permute_host(const T* in, const std::vector<int64_t>& dims, const std::vector<int>& perm, T* out) {
-  const int nd = (int)dims.size();
-  int64_t total = 1;
-  for (auto d : dims) total *= d;
-  std::vector<int64_t> stride(nd, 1);
-  for (int i = 1; i < nd; i++) stride[i] = stride[i - 1] * dims[i - 1];
-  std::vector<int64_t> nd_dims(nd), idx(nd, 0);
-  for (int i = 0; i < nd; i++) nd_dims[i] = dims[perm[i]];
-  for (int64_t lin = 0; lin < total; lin++) {
-    int64_t src = 0;
-    for (int i = 0; i < nd; i++) src += idx[i] * stride[perm[i]];
-    out[lin] = in[src];
-    for (int i = 0; i < nd; i++) {
-      if (++idx[i] < nd_dims[i]) break;
-      idx[i] = 0;
-    }
-  }
-}
-
-template <typename C>
-int dense_matmul(qt_handle* h, const C* A, int64_t M, int64_t K, const C* B, int64_t N, C* Cout) {
-  qt_scratch s(h);
-  C *dA, *dB, *dC;
-  QT_TRY(s.get(&dA, (size_t)M * K));
-  QT_TRY(s.get(&dB, (size_t)K * N));
-  QT_TRY(s.get(&dC, (size_t)M * N));
-  QT_CHECK_CUDA(h, cudaMemcpyAsync(dA, A, sizeof(C) * M * K, cudaMemcpyHostToDevice, h->stream));
-  QT_CHECK_CUDA(h, cudaMemcpyAsync(dB, B, sizeof(C) * K * N, cudaMemcpyHostToDevice, h->stream));
-  C one, zero;
-  one.x = 1; one.y = 0; zero.x = 0; zero.y = 0;
-  QT_TRY(qt_gemm_any(h, QT_OP_N, QT_OP_N, M, N, K, one, dA, M, dB, K, zero, dC, M));
-  QT_CHECK_CUDA(h, cudaMemcpyAsync(Cout, dC, sizeof(C) * M * N, cudaMemcpyDeviceToHost, h->stream));
-  QT_CHECK_CUDA(h, cudaStreamSynchronize(h->stream));
-  return QT_OK;
-}
-
-template <typename C>
-int contract_pair_t(qt_handle* h, int ndA, const int64_t* dA, const C* A, int ndB, const int64_t* dB, const C* B,
-                    int nc, const int* axA, const int* axB, C* out) {
-  std::vector<int64_t> da(dA, dA + ndA), db(dB, dB + ndB);
-  std::vector<char> ca(ndA, 0), cb(ndB, 0);
-  int64_t K = 1;
-  for (int i = 0; i < nc; i++) {
-    if (axA[i] < 0 || axA[i] >= ndA || axB[i] < 0 || axB[i] >= ndB || ca[axA[i]] || cb[axB[i]])
-      return qt_fail(h, QT_EINVAL, "contract_pair: bad axis");
-    if (da[axA[i]] != db[axB[i]]) return qt_fail(h, QT_EDIM_MISMATCH, "Dimensions of contraction legs do not match");
-    ca[axA[i]] = 1;
-    cb[axB[i]] = 1;
-    K *= da[axA[i]];
-  }
-  // A -> [free..., contracted (in axesA order)], B -> [contracted (axesB order), free...]
-  std::vector<int> pa, pb;
-  int64_t M = 1, N = 1;
-  for (int i = 0; i < ndA; i++) if (!ca[i]) { pa.push_back(i); M *= da[i]; }
-  for (int i = 0; i < nc; i++) pa.push_back(axA[i]);
-  for (int i = 0; i < nc; i++) pb.push_back(axB[i]);
-  for (int i = 0; i < ndB; i++) if (!cb[i]) { pb.push_back(i); N *= db[i]; }
-  std::vector<C> Ap((size_t)M * K), Bp((size_t)K * N);
-  permute_host(A, da, pa, Ap.data());
-  permute_host(B, db, pb, Bp.data());
-  return dense_matmul<C>(h, Ap.data(), M, K, Bp.data(), N, out);
-}
-
-}  // namespace
+// (qt_contract_pair, the ncon pairwise step on host buffers, is in k_ncon.cu
+// with the device-resident tensors it runs on.)
 
 extern "C" int qt_gemm(qt_handle* h, int dtype, int opA, int opB, int64_t M, int64_t N, int64_t K,
                        const double* alpha, const void* A, int64_t lda, const void* B, int64_t ldb,
@@ -1322,20 +1255,6 @@ extern "C" int qt_gemm(qt_handle* h, int dtype, int opA, int opB, int64_t M, int
   return QT_OK;
 }
 
-extern "C" int qt_contract_pair(qt_handle* h, int dtype, int ndA, const int64_t* dimsA, const void* A, int ndB,
-                                const int64_t* dimsB, const void* B, int ncontract, const int* axesA, const int* axesB,
-                                void* C) {
-  if (!h || !dimsA || !dimsB || !A || !B || !C || (ncontract > 0 && (!axesA || !axesB)))
-    return qt_fail(h, QT_EINVAL, "contract_pair: null argument");
-  cudaSetDevice(h->device);
-  if (dtype == QT_C128)
-    return contract_pair_t<double2>(h, ndA, dimsA, (const double2*)A, ndB, dimsB, (const double2*)B, ncontract, axesA,
-                                    axesB, (double2*)C);
-  if (dtype == QT_C64)
-    return contract_pair_t<float2>(h, ndA, dimsA, (const float2*)A, ndB, dimsB, (const float2*)B, ncontract, axesA,
-                                   axesB, (float2*)C);
-  return qt_fail(h, QT_EINVAL, "contract_pair: bad dtype");
-}
 
 namespace {
 
@@ -1460,42 +1379,66 @@ extern "C" int qt_contract_svd(qt_handle* h, int dtype, int nd1, const int64_t* 
   if (i1 > nd1 || i2 > nd2) return qt_fail(h, QT_ENOTSUP, "contract_svd: trailing singleton legs");
   if (dtype != QT_C64 && dtype != QT_C128) return qt_fail(h, QT_EINVAL, "contract_svd: bad dtype");
   cudaSetDevice(h->device);
-  std::vector<int64_t> d1(dims1, dims1 + nd1), d2(dims2, dims2 + nd2);
+  // the operands on the device in FP64 (the plain path of the reference's svd)
   int64_t n1 = 1, n2 = 1;
-  for (auto d : d1) n1 *= d;
-  for (auto d : d2) n2 *= d;
+  for (int i = 0; i < nd1; i++) n1 *= dims1[i];
+  for (int i = 0; i < nd2; i++) n2 *= dims2[i];
   std::vector<double2> t1((size_t)n1), t2((size_t)n2);
   for (int64_t i = 0; i < n1; i++)
     t1[i] = (dtype == QT_C64) ? make_double2(((const float2*)T1)[i].x, ((const float2*)T1)[i].y) : ((const double2*)T1)[i];
   for (int64_t i = 0; i < n2; i++)
     t2[i] = (dtype == QT_C64) ? make_double2(((const float2*)T2)[i].x, ((const float2*)T2)[i].y) : ((const double2*)T2)[i];
-  // T1p = permutedims(T1, [rest..., i1]) reshaped (:, D1); T2p = permutedims(T2, [i2, rest...]) reshaped (D1, :)
+  // T1p = permutedims(T1, [rest..., i1]) as (:, D1); T2p = permutedims(T2, [i2, rest...]) as (D1, :)
+  // (src/svd.jl:20-24), permuted on the device
   std::vector<int> p1, p2;
   for (int i = 0; i < nd1; i++) if (i != i1 - 1) p1.push_back(i);
   p1.push_back(i1 - 1);
   p2.push_back(i2 - 1);
   for (int i = 0; i < nd2; i++) if (i != i2 - 1) p2.push_back(i);
-  std::vector<double2> a((size_t)n1), b((size_t)n2);
-  permute_host(t1.data(), d1, p1, a.data());
-  permute_host(t2.data(), d2, p2, b.data());
+  qt_tensor *a0 = nullptr, *b0 = nullptr, *a = nullptr, *b = nullptr;
+  int rc = qt_tensor_create(h, QT_C128, nd1, dims1, t1.data(), &a0);
+  if (rc == QT_OK) rc = qt_tensor_create(h, QT_C128, nd2, dims2, t2.data(), &b0);
+  if (rc == QT_OK) rc = qt_tensor_permute(h, a0, p1.data(), &a);
+  if (rc == QT_OK) rc = qt_tensor_permute(h, b0, p2.data(), &b);
+  qt_tensor_free(h, a0);
+  qt_tensor_free(h, b0);
   const int64_t m1 = n1 / D1, m2 = n2 / D1;
-  // two truncated SVDs (src/svd.jl:26-33), then the product chain of :35
-  std::vector<double2> u1, v1, u2, v2;
-  std::vector<double> s1, s2;
+  // two truncated splits (src/svd.jl:26-33): T1p ~ A1 (diag(S1) V1'), T2p ~ A2 (diag(S2) V2'),
+  // then the product chain of :35, U1 S1 V1' U2 S2 V2', as ((A1 B1) A2) B2
+  void *A1 = nullptr, *B1 = nullptr, *A2 = nullptr, *B2 = nullptr;
   int k1 = 0, k2 = 0;
   double dd = 0;
-  QT_TRY(host_truncated_svd64(h, a.data(), nullptr, m1, D1, er, 0, QT_MODE_PLAIN, &u1, &s1, &v1, &k1, &dd));
-  QT_TRY(host_truncated_svd64(h, b.data(), nullptr, D1, m2, er, 0, QT_MODE_PLAIN, &u2, &s2, &v2, &k2, &dd));
-  // L = U1 diag(S1) V1h (m1 x D1) ; R = U2 diag(S2) V2h (D1 x m2) ; out = L R
-  std::vector<double2> us1((size_t)m1 * k1), us2((size_t)D1 * k2), L((size_t)m1 * D1), R((size_t)D1 * m2);
-  for (int j = 0; j < k1; j++)
-    for (int64_t i = 0; i < m1; i++) us1[i + m1 * j] = cscale(u1[i + m1 * j], s1[j]);
-  for (int j = 0; j < k2; j++)
-    for (int64_t i = 0; i < D1; i++) us2[i + D1 * j] = cscale(u2[i + D1 * j], s2[j]);
-  QT_TRY(dense_matmul<double2>(h, us1.data(), m1, k1, v1.data(), D1, L.data()));
-  QT_TRY(dense_matmul<double2>(h, us2.data(), D1, k2, v2.data(), m2, R.data()));
+  if (rc == QT_OK)
+    rc = qt_split_device(h, QT_C128, qt_tensor_data(a), m1, D1, er, 0, QT_MODE_PLAIN, &A1, &B1, &k1, &dd, 0);
+  if (rc == QT_OK)
+    rc = qt_split_device(h, QT_C128, qt_tensor_data(b), D1, m2, er, 0, QT_MODE_PLAIN, &A2, &B2, &k2, &dd, 0);
+  qt_tensor_free(h, a);
+  qt_tensor_free(h, b);
   std::vector<double2> res((size_t)m1 * m2);
-  QT_TRY(dense_matmul<double2>(h, L.data(), m1, D1, R.data(), m2, res.data()));
+  if (rc == QT_OK) {
+    qt_scratch s(h);
+    double2 *L = nullptr, *LA = nullptr, *T = nullptr;
+    const double2 one = make_double2(1, 0), zero = make_double2(0, 0);
+    rc = s.get(&L, (size_t)m1 * D1);
+    if (rc == QT_OK) rc = s.get(&LA, (size_t)m1 * k2);
+    if (rc == QT_OK) rc = s.get(&T, (size_t)m1 * m2);
+    if (rc == QT_OK)
+      rc = qt_cgemm<double2>(h, QT_OP_N, QT_OP_N, m1, D1, k1, one, (const double2*)A1, m1, (const double2*)B1, k1,
+                             zero, L, m1);
+    if (rc == QT_OK)
+      rc = qt_cgemm<double2>(h, QT_OP_N, QT_OP_N, m1, k2, D1, one, L, m1, (const double2*)A2, D1, zero, LA, m1);
+    if (rc == QT_OK)
+      rc = qt_cgemm<double2>(h, QT_OP_N, QT_OP_N, m1, m2, k2, one, LA, m1, (const double2*)B2, k2, zero, T, m1);
+    if (rc == QT_OK && (cudaMemcpyAsync(res.data(), T, sizeof(double2) * m1 * m2, cudaMemcpyDeviceToHost,
+                                        h->stream) != cudaSuccess ||
+                        cudaStreamSynchronize(h->stream) != cudaSuccess))
+      rc = qt_fail(h, QT_ECUDA, "contract_svd: download failed");
+  }
+  qt_dfree(h, A1);
+  qt_dfree(h, B1);
+  qt_dfree(h, A2);
+  qt_dfree(h, B2);
+  QT_TRY(rc);
   for (int64_t i = 0; i < m1 * m2; i++) {
     if (dtype == QT_C64) ((float2*)out)[i] = make_float2((float)res[i].x, (float)res[i].y);
     else ((double2*)out)[i] = res[i];

@@ -199,6 +199,13 @@ int qt_cgemm(qt_handle* h, int opA, int opB, int64_t M, int64_t N, int64_t K, C 
 // k_tcgemm.cu: complex64 GEMM on the tcgen05 tensor cores (split-TF32x3), op in {N, C}
 int qt_cgemm_tc(qt_handle* h, int opA, int opB, int64_t M, int64_t N, int64_t K, float2 alpha, const float2* A,
                 int64_t lda, const float2* B, int64_t ldb, float2 beta, float2* C, int64_t ldc);
+// C (M x N, ld M) = A_view B_view on the tensor cores with the operands read
+// through device offset tables: A_view(m, k) = A[a_row[m] + a_col[k]],
+// B_view(k, n) = B[b_row[k] + b_col[n]] (the ncon permutes folded into the
+// operand gathers); *_rows_fast: the source's unit-stride leg is a row leg.
+int qt_cgemm_tc_mapped(qt_handle* h, int64_t M, int64_t N, int64_t K, const float2* A, const int64_t* a_row,
+                       const int64_t* a_col, int a_rows_fast, const float2* B, const int64_t* b_row,
+                       const int64_t* b_col, int b_rows_fast, float2* C);
 // complex64 GEMM dispatch: tensor cores when cfg.tc_gemm is set and the
 // problem fills a tile, the SIMT kernel otherwise.
 int qt_cgemm_c64(qt_handle* h, int opA, int opB, int64_t M, int64_t N, int64_t K, float2 alpha, const float2* A,
@@ -267,6 +274,13 @@ int qt_gaussian(qt_handle* h, C* out, int64_t rows, int64_t cols, int64_t ld, ui
 // CholeskyQR2 (FP64 Gram / Cholesky): Y (m x l, ld m) -> orthonormal columns.
 template <typename C>
 int qt_orthonormalize(qt_handle* h, C* Y, int64_t m, int64_t l);
+
+// k_ncon.cu ------------------------------------------------------------------
+// device buffer of a qt_tensor (column-major, its dtype's element)
+void* qt_tensor_data(const qt_tensor* t);
+// the truncated split of a device matrix (qt_engine.cu): M ~ A (m x k) B (k x n)
+int qt_split_device(qt_handle* h, int dtype, const void* M, int64_t m, int64_t n, double cutoff, int chi_max, int mode,
+                    void** A, void** B, int* k, double* discarded, int64_t struct_rank);
 
 // k_obs.cu -------------------------------------------------------------------
 int qt_mps_expect(qt_handle* h, const qt_mps* mps, int site, int nops, double* out);
