@@ -384,9 +384,10 @@ def load_peaks():
 
 def profiled_traffic(kernel):
     """DRAM bytes per launch of `kernel` from its committed ncu summary
-    (profiles/<kernel>_chi1024.md, line `traffic_per_launch_bytes: N`), or None."""
+    (profiles/<kernel>_chi1024_bench.md, line `traffic_per_launch_bytes: N`,
+    captured on this bench's workload), or None."""
     base = kernel.split("<")[0].split("(")[-1].strip()
-    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "profiles", f"{base}_chi1024.md")
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "profiles", f"{base}_chi1024_bench.md")
     try:
         with open(path) as f:
             for line in f:
@@ -400,13 +401,16 @@ def profiled_traffic(kernel):
 def roofline(prof, work, n_prof, sm_mhz=2070.0):
     """Roofline of the dominant kernel (largest total device time in the
     profiled updates), from the engine's algorithmic work counters:
-      Jacobi round kernels: HBM-class bound.  Algorithmic bytes of a round are
-        every column of X read once (the Gram products) plus the rotated
-        pairs' columns written once (and their V rows read and written).  Per
-        kernel: the Gram + pair-solver kernel (pair_eig32_kernel) is charged
-        the reads, the rotation kernel (pair_apply32_kernel) reads and writes
-        the rotated columns, a one-launch round (pair_round_kernel) or sweep
-        (jacobi_sweep32_kernel) is charged all its rounds;
+      Jacobi round kernels (FP32 storage): bound by the FP32 FMA pipe they run
+        on.  Algorithmic FMAs of a round: per row of a rotated pair, 1024
+        complex-as-real FMAs of the rebuild (16 columns x a 16 x 8 block of
+        the pair unitary, twice) and 544 of the pair Gram (its upper 4 x 4
+        tiles of the 16 x 16 complex Gram); the counters give them as
+        8 x rot_bytes and 4.25 x gram_bytes.  Peak = 152 SMs x 128 FP32
+        FMA/clock x 2 flops at the SM clock sampled during the run (the
+        measured peaks hold no FP32 figure).  Their bytes stay in L2 (the
+        ping-pong columns of a 2048 x 1152 complex64 matrix are 19 MB), so
+        the DRAM traffic of the ncu capture is reported beside it;
       tc_gemm_kernel: tensor bound; 24 M N K TF32 flops per complex product,
         peak = half the measured dense bf16 rate (TF32 runs at half the bf16
         tensor rate)."""
@@ -415,44 +419,33 @@ def roofline(prof, work, n_prof, sm_mhz=2070.0):
     peaks, src = load_peaks()
     name, launches, ms = prof[0]
     per_launch_s = ms / 1e3 / launches
-    jacobi = {"pair_round_kernel": work["jacobi_bytes"], "jacobi_sweep32_kernel": work["jacobi_bytes"],
-              "(gram_kernel": work["jacobi_gram_bytes"], "pair_eig32_kernel": work["jacobi_gram_bytes"],
-              "apply_kernel": 2.0 * work["jacobi_rot_bytes"], "pair_apply32_kernel": 2.0 * work["jacobi_rot_bytes"]}
-    for prefix, nbytes in jacobi.items():
-        if not name.startswith(prefix):
-            continue
+    fp32_kernels = ("pair_round_kernel", "jacobi_sweep32_kernel", "(gram_kernel", "pair_eig32_kernel",
+                    "apply_kernel", "pair_apply32_kernel")
+    if name.startswith(fp32_kernels):
         if work["jacobi_rounds"] <= 0:
             return {"kernel": name, "note": "no Jacobi work recorded"}
-        # work counters are per update; the profile covers n_prof updates
-        bytes_per_launch = nbytes * n_prof / launches
-        achieved = bytes_per_launch / per_launch_s / 1e9
-        peak = peaks["hbm_gbs"]
-        out = {"kernel": name, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-               "frac": achieved / peak, "traffic": profiled_traffic(name), "bytes_per_launch": bytes_per_launch,
-               "peak_source": f"{src} hbm_gbs",
-               "note": "X and V of the round are L2-resident (<= 67 MB at 2048^2); traffic = DRAM bytes per launch "
-                       "of the committed ncu capture (cold L2)"}
-        # the FP32 pipe: the rebuild/rotation costs 1024 FMA per row per
-        # rotated pair (rot_bytes / 128 rows of 16 columns), the Gram 544 per
-        # row per pair (gram_bytes / 128); peak = 152 SMs x 128 FMA/clock at
-        # the SM clock sampled during the run
         fma = 8.0 * work["jacobi_rot_bytes"] + 4.25 * work["jacobi_gram_bytes"]
         if name.startswith("pair_eig32_kernel") or name.startswith("(gram_kernel"):
             fma = 4.25 * work["jacobi_gram_bytes"]
         elif name.startswith("pair_apply32_kernel") or name.startswith("apply_kernel"):
             fma = 8.0 * work["jacobi_rot_bytes"]
-        tflops = 2.0 * fma * n_prof / (ms / 1e3) / 1e12
-        out["fp32_pipe"] = {"achieved_tflops": tflops, "sm_mhz": sm_mhz,
-                            "peak_tflops": 2.0 * 152 * 128 * sm_mhz * 1e6 / 1e12,
-                            "frac": tflops / (2.0 * 152 * 128 * sm_mhz * 1e6 / 1e12)}
-        return out
+        # work counters are per update; the profile covers n_prof updates
+        flops_per_launch = 2.0 * fma * n_prof / launches
+        achieved = flops_per_launch / per_launch_s / 1e12
+        peak = 2.0 * 152 * 128 * sm_mhz * 1e6 / 1e12
+        return {"kernel": name, "bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                "frac": achieved / peak, "traffic": profiled_traffic(name), "flops_per_launch": flops_per_launch,
+                "l2_bytes_per_launch": work["jacobi_bytes"] * n_prof / launches,
+                "peak_source": f"152 SMs x 128 FMA/clock x 2 at the sampled SM clock {sm_mhz:.0f} MHz",
+                "note": "traffic = DRAM bytes per launch of the committed ncu capture of this workload"}
     if name.startswith("tc_gemm_kernel"):
         n_launch = work["tc_launches"]
         flops_per_launch = work["tc_flops"] / max(n_launch, 1)
         achieved = flops_per_launch / per_launch_s / 1e12
         peak = peaks["bf16_tflops"] / 2
         return {"kernel": name, "bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                "frac": achieved / peak, "traffic": None, "peak_source": f"{src} bf16_tflops / 2 (TF32)"}
+                "frac": achieved / peak, "traffic": profiled_traffic(name),
+                "peak_source": f"{src} bf16_tflops / 2 (TF32)"}
     return {"kernel": name, "note": "no work model for this kernel"}
 
 
@@ -467,11 +460,15 @@ def bench_reference(args, dist: Dist):
     chi = args.chi
     pair = decay_pair(chi, 1001)
     rng = np.random.default_rng(77)
-    gates = [haar(rng) for _ in range(8)]
-    steps = max(1, min(args.steps, 2))
-    warm = min(args.warmup, 1)
+    # the same K and W as the engine's arm, unless the steps would take more
+    # than about three minutes of host time (then as many as fit)
+    gates = [haar(rng) for _ in range(args.steps + args.warmup + 8)]
+    warm = args.warmup
+    t0 = time.perf_counter()
     for i in range(warm):
         oracle.apply_2q([pair[0].copy(), pair[1].copy()], gates[i], 1, CUTOFF, chi)
+    per = (time.perf_counter() - t0) / max(warm, 1)
+    steps = max(1, min(args.steps, int(180.0 / max(per, 1e-9)))) if warm else max(1, args.steps)
     t0 = time.perf_counter()
     for i in range(steps):
         oracle.apply_2q([pair[0].copy(), pair[1].copy()], gates[warm + i], 1, CUTOFF, chi)
@@ -482,13 +479,47 @@ def bench_reference(args, dist: Dist):
             "impl": "reference", "dtype": "c128", "data": "synthetic",
             "config": workload_config(chi, 1),
             "cpu_baseline": {"value": v, "unit": "updates/s", "cores": os.cpu_count(), "kind": "port",
-                             "sample": f"{steps} timed update(s) at chi={chi} (steps capped at 2 to bound the run)"},
+                             "sample": f"{steps} timed update(s) of the chi={chi} workload after {warm} warm-up "
+                                       f"(numpy gesdd, OpenBLAS on all host threads)"},
             "e2e": {"value": v, "unit": "updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "vs_baseline": None}
 
 
+def free_port() -> int:
+    import socket
+    with socket.socket(socket.AF_INET, socket.SOCK_STREAM) as sk:
+        sk.bind(("127.0.0.1", 0))
+        return sk.getsockname()[1]
+
+
+def launch_command(argv, gpus: int, port: int):
+    """The one-process-per-GPU launch of this script on `gpus` local GPUs."""
+    return [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={gpus}",
+            "--master-addr", "127.0.0.1", f"--master-port={port}", os.path.abspath(__file__)] + list(argv)
+
+
+def check_world(args, env):
+    """None when this process should run the bench itself; otherwise the exit
+    status of the launch it made.  `--gpus N` without a launcher (WORLD_SIZE
+    unset) starts N local ranks through torch.distributed.run; under a
+    launcher, a WORLD_SIZE other than N is refused."""
+    world = env.get("WORLD_SIZE")
+    if world is None:
+        if args.gpus > 1:
+            return subprocess.call(launch_command(sys.argv[1:], args.gpus, free_port()))
+        return None
+    if int(world) != args.gpus:
+        print(json.dumps({"error": f"--gpus {args.gpus} but WORLD_SIZE={world}: launch one rank per GPU"}),
+              file=sys.stderr)
+        return 2
+    return None
+
+
 def main():
     args = parse()
+    rc = check_world(args, os.environ)
+    if rc is not None:
+        sys.exit(rc)
     dist = Dist()
     if args.impl == "reference":
         line = bench_reference(args, dist)

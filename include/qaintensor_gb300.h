@@ -255,7 +255,7 @@ int qt_mps_upload_site(qt_handle* h, qt_mps* mps, int site, const int64_t* dims3
 int qt_apply_2q(qt_handle* h, qt_mps* mps, int site, const double* G,
                 double cutoff, int chi_max, int mode, qt_update_stats* stats);
 
-/* switch!(mps, i) of src/switch.jl (function at file lines 56-94): swap the
+/* switch!(mps, i) of src/switch.jl:18-56: swap the
  * physical legs of sites (site, site+1) with an untruncated SVD split. */
 int qt_switch(qt_handle* h, qt_mps* mps, int site);
 

@@ -9,7 +9,7 @@ that the CUDA engine replaces:
 * ``contract_rep`` / ``ncon`` pairwise contraction   (src/contract.jl:39-60, 242-264)
 * ``contract_order`` contraction-order search        (src/contract.jl:8-32, 65-235)
 * ``contract_svd`` and its absolute tail-norm rule    (src/svd.jl:7-38, rule at :29-33)
-* ``switch!`` / ``permute!``                          (src/switch.jl:18-144 of the file)
+* ``switch!`` / ``permute!``                          (src/switch.jl:6-106)
 * ``MPS(psi)`` sequential SVD                         (src/mps.jl:55-89)
 * ``MPO(m)`` / ``decompose!``                         (src/mpo.jl:27-90, src/decompose.jl:6-52)
 * ``extend_MPO`` / ``apply_MPO`` wiring               (src/mpo.jl:122-252)

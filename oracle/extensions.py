@@ -3,11 +3,11 @@
 The reference has no eager two-qubit gate + truncated-SVD update; it is
 composed here from reference pieces, each cited:
 
-* two-site contraction   -- src/switch.jl (contract_svd call, file line 64) / src/svd.jl:35
+* two-site contraction   -- src/switch.jl:26 (the contract_svd call) / src/svd.jl:35
 * gate acts as U on the input legs, iwire[k] = bit k-1 -- src/decompose.jl:16-31, src/mpo.jl:41-57
-* matrix view (2*chiL, 2*chiR), rows (a,s1), columns (s2,b) -- src/switch.jl (file lines 73-77)
+* matrix view (2*chiL, 2*chiR), rows (a,s1), columns (s2,b) -- src/switch.jl:35-36
 * rank by the absolute tail rule              -- src/svd.jl:29-33
-* split U -> left site, diag(S)V' -> right     -- src/switch.jl (file lines 88-91)
+* split U -> left site, diag(S)V' -> right     -- src/switch.jl:50-52
 
 Sites use a uniform 3-leg layout (chiL, 2, chiR); the first site has chiL=1
 and the last chiR=1 (the same memory as the reference's 2-leg end tensors).

@@ -387,7 +387,7 @@ def mps_from_state(psi: np.ndarray) -> Network:
 def switch_adjacent(mps: Network, i: int) -> None:
     """``switch!(mps, i)``: swap the physical legs of sites i and i+1 (1-based).
 
-    Follows src/switch.jl (function at file lines 56-94): the two sites are
+    Follows src/switch.jl:18-56: the two sites are
     contracted with ``contract_svd(..., er=0)``, the physical legs swapped,
     then one untruncated SVD split with U to the left and diag(S)V' to the right.
     """
@@ -418,7 +418,7 @@ def switch_adjacent(mps: Network, i: int) -> None:
 
 
 def switch_wires(mps: Network, i: int, j: int) -> None:
-    """``switch!(mps, i, j)`` (src/switch.jl, file lines 101-124): wire numbers
+    """``switch!(mps, i, j)`` (src/switch.jl:63-86): wire numbers
     count from the far end (``i -> L - i + 1``) and the swap runs as a ladder of
     adjacent swaps up then down."""
     check_mps(mps)
@@ -438,14 +438,14 @@ def switch_wires(mps: Network, i: int, j: int) -> None:
 
 
 def switch_pairs(mps: Network, pairs) -> None:
-    """``switch!(mps, indices::Vector{Tuple})`` (src/switch.jl, file lines 44-49)."""
+    """``switch!(mps, indices::Vector{Tuple})`` (src/switch.jl:6-11)."""
     check_mps(mps)
     for a, b in pairs:
         switch_wires(mps, a, b)
 
 
 def permute_mps(mps: Network, order: Sequence[int]) -> None:
-    """``Base.permute!(mps, order)`` (src/switch.jl, file lines 132-144)."""
+    """``Base.permute!(mps, order)`` (src/switch.jl:94-106)."""
     check_mps(mps)
     order = list(order)
     n = len(mps.tensors)

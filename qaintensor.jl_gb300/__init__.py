@@ -533,11 +533,11 @@ class DeviceMPS:
         return st.as_dict()
 
     def switch(self, i: int):
-        """``switch!(mps, i)`` (src/switch.jl): swap the physical legs of sites i, i+1."""
+        """``switch!(mps, i)`` (src/switch.jl:18-56): swap the physical legs of sites i, i+1."""
         self.eng._check(self.eng._lib.qt_switch(self.eng._h, self._p, i - 1))
 
     def switch_wires(self, i: int, j: int):
-        """``switch!(mps, i, j)`` (src/switch.jl, file lines 101-124): wire
+        """``switch!(mps, i, j)`` (src/switch.jl:63-86): wire
         numbers count from the far end (i -> L - i + 1) and the swap runs as a
         ladder of adjacent swaps up, then down."""
         if not (i > 0 and j > 0):
@@ -556,7 +556,7 @@ class DeviceMPS:
             self.switch(s)
 
     def permute(self, order):
-        """``Base.permute!(mps, order)`` (src/switch.jl, file lines 132-144)."""
+        """``Base.permute!(mps, order)`` (src/switch.jl:94-106)."""
         order = list(order)
         n = self.nsites
         if len(order) != n:

@@ -3,7 +3,7 @@
 //
 // theta = A_mat (2chiL x chiM) . B_mat (chiM x 2chiR) is the pairwise ncon
 // step of src/contract.jl:257,263 for two neighbouring MPS sites (the two-site
-// contraction of src/switch.jl, file line 64).  The gate acts on the input
+// contraction of src/switch.jl:26).  The gate acts on the input
 // legs, G[o1 + 2 o2, i1 + 2 i2] (src/decompose.jl:16-31, src/mpo.jl:41-57).
 #include <cuda_runtime.h>
 

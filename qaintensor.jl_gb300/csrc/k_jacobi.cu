@@ -1,7 +1,7 @@
 // One-sided block Jacobi SVD (Hestenes).
 //
 // Replaces the dense LAPACK ?gesdd called by LinearAlgebra.svd at
-// src/svd.jl:26-27 and in switch! (src/switch.jl, file line 77): X (mm x nn,
+// src/svd.jl:26-27 and in switch! (src/switch.jl:39): X (mm x nn,
 // mm >= nn) is driven to orthogonal columns, X <- X V, so X = U diag(s) and
 // the input equals U diag(s) V^H.
 //
@@ -1192,7 +1192,7 @@ jacobi_sweep32_kernel(float2* __restrict__ xb0, float2* __restrict__ xb1, int64_
                       int has_prev, double tol, float tol_inner, double nu_rel2, const double* __restrict__ xnorm2,
                       float2* __restrict__ wbuf, int* __restrict__ rotbuf, int* __restrict__ done,
                       int* __restrict__ flags, int max_inner, float keep2, float* __restrict__ dnorm,
-                      unsigned long long* phase_ns) {
+                      unsigned long long* phase_ns, int spin, int stall) {
   extern __shared__ __align__(16) float2 ps_slab[];  // [2][PS_SLAB][PS_LDS]
   __shared__ __align__(16) float2 wsub[2][JC][JW];    // 16x8 unitary blocks that rebuild the two blocks
   __shared__ float2 psum[3][PS_TILES * PS_TE];
@@ -1231,6 +1231,17 @@ jacobi_sweep32_kernel(float2* __restrict__ xb0, float2* __restrict__ xb1, int64_
     tournament(r, q, nb, bi, bj);
     // ---- wait for the round g - 1 CTAs this round depends on
     int gave_up = 0;
+    if (stall && q == 0 && t == 0 && r == 0) {
+      // test hook (QT_JACOBI_STALL_TEST): a bounded wait on a status word that
+      // nothing sets, which must end in QT_ETIMEOUT with the context usable
+      int it = 0;
+      for (; it < spin; it++) {
+        if (ld_acquire_gpu(flags + QT_FLAG_STALL) != 0) break;
+        if (*(volatile int*)(flags + QT_FLAG_ABORT)) { it = spin; break; }
+        __nanosleep(64);
+      }
+      if (it >= spin) { gave_up = 1; atomicExch(flags + QT_FLAG_ABORT, 1); }
+    }
     if (prev && t < 6) {
       int target = -1, qq, s;
       if (t < 2) {  // read after write: the pairs that held our blocks in round g - 1
@@ -1251,12 +1262,12 @@ jacobi_sweep32_kernel(float2* __restrict__ xb0, float2* __restrict__ xb1, int64_
       }
       if (target >= 0) {
         int it = 0;
-        for (; it < PS_SPIN; it++) {
+        for (; it < spin; it++) {
           if (ld_acquire_gpu(done + target) >= g - 1) break;
-          if (*(volatile int*)(flags + QT_FLAG_ABORT)) { it = PS_SPIN; break; }
+          if (*(volatile int*)(flags + QT_FLAG_ABORT)) { it = spin; break; }
           __nanosleep(64);
         }
-        if (it >= PS_SPIN) { gave_up = 1; atomicExch(flags + QT_FLAG_ABORT, 1); }
+        if (it >= spin) { gave_up = 1; atomicExch(flags + QT_FLAG_ABORT, 1); }
       }
     }
     if (__syncthreads_or(gave_up)) return;
@@ -1608,10 +1619,16 @@ static int launch_sweep32(qt_handle* h, int pairs, float2* x0, float2* x1, int64
   attr[0].val.cooperative = 1;
   lc.attrs = attr;
   lc.numAttrs = 1;
+  // QT_JACOBI_STALL_TEST=N (tests only): CTA 0 waits at most N polls on a
+  // status word nothing sets, and every round wait is limited to N polls
+  const char* stall_env = std::getenv("QT_JACOBI_STALL_TEST");
+  const int stall_polls = stall_env ? std::atoi(stall_env) : 0;
+  const int spin = stall_polls > 0 ? stall_polls : PS_SPIN;
+  const int stall = stall_polls > 0 ? 1 : 0;
   if (h->prof) qt_prof_before(h, "jacobi_sweep32_kernel");
   const cudaError_t e = cudaLaunchKernelEx(&lc, jacobi_sweep32_kernel, x0, x1, ldx, mm, v0, v1, ldv, nn, nb, g0,
                                            has_prev, tol, tol_inner, nu_rel2, xnorm2, wbuf, rotbuf, done, h->d_flags,
-                                           max_inner, keep2, dnorm, phase_ns);
+                                           max_inner, keep2, dnorm, phase_ns, spin, stall);
   if (h->prof) qt_prof_after(h);
   h->launches++;
   if (e != cudaSuccess)
@@ -1679,12 +1696,13 @@ int qt_jacobi_svd_ws(qt_handle* h, TS* X, int64_t mm, int64_t nn, int64_t ldx, T
                                           (int)smem));
   // QT_JACOBI_TRACE=1 in the environment prints one line per sweep to stderr;
   // QT_JACOBI_PHASES=1 adds the average time per phase of the one-launch
-  // rounds at the end (CTA 0 of each cluster / the others)
+  // rounds at the end (CTA 0 of each cluster / the others); a handle without
+  // a pool (the allocation-free entry point's) allocates nothing and skips them
   static const bool trace = std::getenv("QT_JACOBI_TRACE") != nullptr;
   static const bool phases = std::getenv("QT_JACOBI_PHASES") != nullptr;
   unsigned long long* phase_ns = nullptr;
   qt_scratch pscratch(h);
-  if (phases && (csize || two_launch || sweep_kernel)) {
+  if (phases && h->pool && (csize || two_launch || sweep_kernel)) {
     QT_TRY(pscratch.get(&phase_ns, 16));
     QT_CHECK_CUDA(h, cudaMemsetAsync(phase_ns, 0, 16 * sizeof(unsigned long long), h->stream));
   }

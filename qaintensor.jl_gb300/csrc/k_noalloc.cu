@@ -10,12 +10,19 @@
 // cudaMalloc, cudaFree or allocating library routine.
 //
 // Limits and rules:
-//   * m, n <= QT_NOALLOC_MAX_DIM (256); larger sizes are rejected with
-//     QT_ENOTSUP.  The array (about 2.2 MB) stays allocated on every device
-//     that loads the library until the process exits.
+//   * m, n <= 256; larger sizes are rejected with QT_ENOTSUP.  The array
+//     (NA_BYTES, about 2.6 MB: 1 MiB each for the working matrix and the
+//     rotations, 516 KiB of Jacobi workspace, the values and status words)
+//     stays allocated on every device that loads the library until the
+//     process exits.
 //   * The first call on a device looks up the array's device address with
 //     cudaGetSymbolAddress (once per device, that device current); make that
-//     first call before any stream capture.
+//     first call before any stream capture.  The address is kept for the
+//     life of the process: after a cudaDeviceReset the library must be
+//     reloaded before this entry point is used again on that device.
+//   * Failures come back as the status code only (there is no handle to
+//     carry a message).  The Jacobi phase counters of QT_JACOBI_PHASES are
+//     not collected here, since they would need an allocation.
 //   * All calls share the one array and each call leaves its contents
 //     behind; calls that overlap on the GPU (different streams or threads)
 //     race on it and must be serialised by the caller.
@@ -37,6 +44,7 @@ constexpr size_t NA_PARTS = 16 * 8 * 256 + 256;            // Jacobi workspace (
 constexpr size_t NA_SIG = NA_MAX;                          // singular values
 constexpr size_t NA_BYTES = sizeof(double2) * (NA_X + NA_V + NA_PARTS) + sizeof(double) * NA_SIG +
                             sizeof(int) * (NA_MAX + QT_FLAG_COUNT) + 256;
+static_assert(NA_BYTES > 2600000 && NA_BYTES < 2700000, "the documented size of the scratch array is about 2.6 MB");
 
 __device__ __align__(256) unsigned char g_noalloc_scratch[NA_BYTES];
 

@@ -1,6 +1,6 @@
 // Truncation and split: singular values from converged Jacobi columns, the
 // absolute tail-norm rank rule of src/svd.jl:29-33, and the split of
-// src/switch.jl (file lines 77-93): U[:, 1:k] -> left site, diag(S) V'[1:k, :]
+// src/switch.jl:42-53: U[:, 1:k] -> left site, diag(S) V'[1:k, :]
 // -> right site.
 #include <cuda_runtime.h>
 

@@ -69,7 +69,8 @@ enum {
   QT_FLAG_OFFBIG = 5,    // Jacobi: OFFMAX over pairs of columns above 1e-3 ||X||_F (float bits)
   QT_FLAG_ABORT = 6,     // Jacobi sweep kernel: a bounded round wait gave up
   QT_FLAG_OFFKEPT = 7,   // Jacobi sweep kernel: OFFMAX over pairs with a column above the keep threshold
-  QT_FLAG_COUNT = 8
+  QT_FLAG_STALL = 8,     // never set: the bounded-wait test hook of the sweep kernel waits on it
+  QT_FLAG_COUNT = 9
 };
 
 struct qt_mps {

@@ -147,3 +147,20 @@ def test_sharded_ensemble_two_gloo_ranks():
         assert x["res"]["ranks"] == 2
         assert x["res"]["updates"] == x["tasks"]  # the ranks' update counts add up to the ensemble's
         assert x["z"] == [float(n) for n in x["n"]]  # the gather puts every circuit's value in its place
+
+
+def test_bench_gpus_flag_starts_one_rank_per_gpu():
+    """`bench.py --gpus 2` with no launcher starts two local ranks through
+    torch.distributed.run (here on the reference arm, which needs no GPU):
+    rank 0 alone prints the line; a WORLD_SIZE that disagrees with --gpus is
+    refused."""
+    env = {k: v for k, v in os.environ.items() if k not in ("WORLD_SIZE", "RANK", "LOCAL_RANK")}
+    cmd = [sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--gpus", "2", "--chi", "16",
+           "--steps", "2", "--warmup", "1"]
+    p = subprocess.run(cmd, env=env, capture_output=True, text=True, timeout=300)
+    assert p.returncode == 0, p.stderr[-2000:]
+    lines = [json.loads(x) for x in p.stdout.splitlines() if x.startswith("{")]
+    assert len(lines) == 1 and lines[0]["impl"] == "reference" and lines[0]["steps"] == 2, p.stdout
+    bad = dict(env, WORLD_SIZE="3", RANK="0", LOCAL_RANK="0")
+    p = subprocess.run(cmd, env=bad, capture_output=True, text=True, timeout=120)
+    assert p.returncode == 2 and "WORLD_SIZE=3" in p.stderr
