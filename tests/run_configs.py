@@ -152,23 +152,103 @@ def c2(qt, args):
     return {"config": "c2", "rows": out}
 
 
+def zz_all_bonds(sites):
+    """<Z_i Z_i+1>/<psi|psi> on every bond from one left and one right
+    environment sweep (FP64, the oracle's transfer convention)."""
+    n = len(sites)
+    z = np.diag([1.0, -1.0]).astype(np.complex128)
+    left = [np.ones((1, 1), dtype=np.complex128)]
+    for a in sites:
+        left.append(np.einsum("ab,asc,bsd->cd", left[-1], a.conj(), a, optimize=True))
+    right = [np.ones((1, 1), dtype=np.complex128)]
+    for a in reversed(sites):
+        right.append(np.einsum("asc,bsd,cd->ab", a.conj(), a, right[-1], optimize=True))
+    right = right[::-1]  # right[i]: environment of sites i..n-1 (0-based)
+    norm = float(np.real(left[n][0, 0]))
+    out = []
+    for i in range(n - 1):
+        a, b = sites[i], sites[i + 1]
+        e = np.einsum("ab,asc,st,btd->cd", left[i], a.conj(), z, a, optimize=True)
+        e = np.einsum("ab,asc,st,btd->cd", e, b.conj(), z, b, optimize=True)
+        out.append(float(np.real(np.einsum("cd,cd->", e, right[i + 2]))) / norm)
+    return out
+
+
+def run_reference_chain(n, gates, cutoff, chi_max, storage):
+    """The FP64 oracle's update chain (src/switch.jl split, src/svd.jl:29-33
+    rule, chi_max cap); storage "c64" rounds every updated site to complex64,
+    the storage of the chosen mode, so the run isolates what the FP64 split
+    achieves on that storage.  Returns the sites."""
+    import oracle as O
+    sites = O.product_state(n)
+    for (_, w, g) in gates:
+        O.apply_2q(sites, g, w, cutoff, chi_max)
+        if storage == "c64":
+            sites[w - 1] = sites[w - 1].astype(np.complex64).astype(np.complex128)
+            sites[w] = sites[w].astype(np.complex64).astype(np.complex128)
+    return sites
+
+
+def c3_gates(args):
+    return brickwork(args.c3_n, args.c3_depth, np.random.default_rng(64))
+
+
+def c3ref(qt, args):
+    """The FP64 oracle run of the c3 circuit on the CPU (complex128 storage,
+    or complex64 storage with --c3-ref-storage c64): <Z_i Z_i+1> on every bond."""
+    sites = run_reference_chain(args.c3_n, c3_gates(args), 1e-8, args.c3_chi_max, args.c3_ref_storage)
+    return {"config": "c3ref", "storage": args.c3_ref_storage, "n": args.c3_n, "depth": args.c3_depth,
+            "chi_max": args.c3_chi_max, "ZZ": zz_all_bonds(sites)}
+
+
 def c3(qt, args):
-    rng = np.random.default_rng(64)
-    n, depth, chi_max, cutoff = 64, args.c3_depth, 1024, 1e-8
-    gates = brickwork(n, depth, rng)
-    eng = qt.Engine(mode="chosen", tc_gemm=1)
-    model = load_rank_model(eng)
-    mps = eng.product_state(n, dtype=np.complex64)
-    t0 = time.perf_counter()
-    stats = []
-    for (layer, w, g) in gates:
-        mps.set_circuit_position(layer, depth)
-        stats.append(mps.apply_2q(g, w, cutoff, chi_max))
-    dt = time.perf_counter() - t0
-    zz = [mps.expect_zz(i) for i in range(1, n)] if args.c3_observables else []
-    return {"config": "c3", "depth": depth, "updates": len(gates), "seconds": dt, "updates_per_s": len(gates) / dt,
-            "max_rank": max(s["rank"] for s in stats), "fallbacks": sum(1 for s in stats if s["fallback"]),
-            "sketched": sum(1 for s in stats if s["sketch_size"] > 0), "rank_model": model, "ZZ": zz}
+    """64-qubit brickwork, complex64, chi_max 1024, cutoff 1e-8, chosen mode:
+    updates/s, the rank decisions and <Z_i Z_i+1> on every bond, compared with
+    the FP64 oracle runs given by --c3-ref-json (made by c3ref on the CPU);
+    --c3-ablate also runs without the rank model."""
+    n, depth, chi_max, cutoff = args.c3_n, args.c3_depth, args.c3_chi_max, 1e-8
+    gates = c3_gates(args)
+    out = {"config": "c3", "n": n, "depth": depth, "chi_max": chi_max, "updates": len(gates)}
+    refs = {}
+    for path in args.c3_ref_json or []:
+        with open(path) as f:
+            r = json.load(f)
+        if (r["n"], r["depth"], r["chi_max"]) == (n, depth, chi_max):
+            refs[r["storage"]] = np.array(r["ZZ"])
+    for use_model in ((True, False) if args.c3_ablate else (True,)):
+        eng = qt.Engine(mode="chosen", tc_gemm=1)
+        model = load_rank_model(eng) if use_model else False
+        mps = eng.product_state(n, dtype=np.complex64)
+        eng.sync()
+        t0 = time.perf_counter()
+        stats = []
+        for (layer, w, g) in gates:
+            mps.set_circuit_position(layer, depth)
+            stats.append(mps.apply_2q(g, w, cutoff, chi_max))
+        eng.sync()
+        dt = time.perf_counter() - t0
+        row = {"seconds": dt, "updates_per_s": len(gates) / dt, "rank_model": model,
+               "max_rank": max(s["rank"] for s in stats), "fallbacks": sum(1 for s in stats if s["fallback"]),
+               "sketched": sum(1 for s in stats if s["sketch_size"] > 0), "cert": eng.cert_counters()}
+        pr = [(s["predicted_rank"], s["rank"]) for s in stats if s["predicted_rank"] > 0]
+        if pr:
+            p, k = np.array(pr, dtype=float).T
+            row["predicted_vs_rank"] = {"updates": len(pr), "exact": int(np.sum(p == k)),
+                                        "mean_abs_rel": float(np.mean(np.abs(p - k) / k)),
+                                        "under": int(np.sum(p < k))}
+        if args.c3_observables or refs:
+            zz = np.array([mps.expect_zz(i) for i in range(1, n)])
+            row["ZZ"] = zz.tolist()
+            for st, zr in refs.items():
+                row["dZZ_max_vs_fp64_" + st] = float(np.abs(zz - zr).max())
+                row["dZZ_median_vs_fp64_" + st] = float(np.median(np.abs(zz - zr)))
+        out["with_model" if use_model else "without_model"] = row
+        mps.free()
+        eng.close()
+    if "c128" in refs and "c64" in refs:
+        d = np.abs(refs["c64"] - refs["c128"])
+        out["dZZ_fp64_split_c64_storage"] = {"max": float(d.max()), "median": float(np.median(d))}
+    return out
 
 
 def c4_circuits(nc, rng):
@@ -214,7 +294,10 @@ def c4(qt, args):
     """The batched ensemble, sharded by circuit over the ranks when launched
     with one process per GPU (RANK, WORLD_SIZE, LOCAL_RANK): each rank runs
     its circuits on its own GPU with no collective in the timed region; the
-    rate is all ranks' updates over the slowest rank's time."""
+    rate is all ranks' updates over the slowest rank's time.  With
+    --c4-autotune the tuned launch shapes are timed beside the defaults;
+    --c4-dump writes every circuit's <Z_1> for c4check (the oracle check on
+    the CPU, off the GPU machine)."""
     import oracle as O
     dist = getattr(args, "dist", None)
     world, rank, local = (dist.world, dist.rank, dist.local) if dist is not None else (1, 0, 0)
@@ -229,34 +312,81 @@ def c4(qt, args):
             layers[layer - 1].append((j, w, g))
     ntask = sum(len(l) for l in layers)
     eng = qt.Engine(mode="chosen", device=local)
-    b = qt.Batch(eng, [circuits[ci][0] for ci in mine], [circuits[ci][2] for ci in mine])
-    b.run(layers, 1e-8, use_graph=True)  # capture + first run (warm-up)
-    b.reset()
-    eng.sync()
-    if dist is not None:
-        dist.barrier()
-    t0 = time.perf_counter()
-    b.replay()
-    eng.sync()
-    dt = time.perf_counter() - t0
-    if dist is not None:
-        dt, ntask_all = dist.max(dt), int(dist.sum(ntask))
-    else:
-        ntask_all = ntask
-    z = gather_by_circuit(dist, mine, [float(v) for v in b.expect_z(1)], nc)
-    b.free()
+    variants = [("default", None)]
+    tuned_entry = None
+    if getattr(args, "c4_autotune", None):
+        import importlib.util
+        spec = importlib.util.spec_from_file_location(
+            "qaintensor_gb300_autotune", os.path.join(ROOT, "qaintensor.jl_gb300", "autotune.py"))
+        at = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(at)
+        cache = at.load(args.c4_autotune)
+        if not at.device_entry(cache, local).get("batch"):
+            at.tune(qt, args.c4_autotune, device=local, ncirc=args.c4_tune_circuits, reps=2)
+            cache = at.load(args.c4_autotune)
+        tuned_entry = at.device_entry(cache, local).get("batch")
+        variants.append(("tuned", lambda bb: at.apply_batch(bb, cache, local)))
+    rates, ntask_all, z, cert = {}, ntask, None, None
+    for name, apply in variants:
+        b = qt.Batch(eng, [circuits[ci][0] for ci in mine], [circuits[ci][2] for ci in mine])
+        if apply is not None:
+            apply(b)
+        b.run(layers, 1e-8, use_graph=True)  # capture + first run (warm-up)
+        b.reset()
+        eng.sync()
+        if dist is not None:
+            dist.barrier()
+        t0 = time.perf_counter()
+        b.replay()
+        eng.sync()
+        dt = time.perf_counter() - t0
+        if dist is not None:
+            dt, ntask_all = dist.max(dt), int(dist.sum(ntask))
+        rates[name] = {"seconds": dt, "updates_per_s": ntask_all / dt}
+        z = gather_by_circuit(dist, mine, [float(v) for v in b.expect_z(1)], nc)
+        cert = b.cert_counts()
+        b.free()
     eng.close()
-    errs = []
-    if rank == 0:
-        for ci in rng.choice(nc, size=min(nc, args.c4_check), replace=False):
-            n, depth, chi, gates = circuits[ci]
-            if chi > 32 or n > 24:
-                continue
-            sites, _ = O.run_brickwork(n, gates, 1e-8, chi)
-            errs.append(abs(z[ci] - O.expect_z(sites, 1)))
-    return {"config": "c4", "circuits": nc, "ranks": world, "updates": ntask_all, "seconds": dt,
-            "updates_per_s": ntask_all / dt, "Z1_err_max_sample": max(errs) if errs else None,
-            "checked": len(errs)}
+    dt = rates[variants[-1][0]]["seconds"]
+    res = {"config": "c4", "circuits": nc, "ranks": world, "updates": ntask_all, "seconds": dt,
+           "updates_per_s": ntask_all / dt, "launch_shapes": rates, "cert": cert}
+    if tuned_entry:
+        res["tuned"] = {k: {"threads": v["threads"], "ctas_per_sm": v["ctas_per_sm"]} for k, v in tuned_entry.items()}
+    if rank == 0 and getattr(args, "c4_dump", None):
+        with open(args.c4_dump, "w") as f:
+            json.dump({"circuits": nc, "Z1": z}, f)
+    if rank == 0 and args.c4_check > 0:
+        res.update(c4_errors(O, circuits, z, args, rng))
+    return res
+
+
+def c4_errors(O, circuits, z, args, rng):
+    """<Z_1> of a sample of circuits against the FP64 oracle (and, with
+    --c4-storage-ref, the FP64 split on complex64 storage against it)."""
+    errs, errs_c64 = [], []
+    for ci in rng.choice(len(circuits), size=min(len(circuits), args.c4_check), replace=False):
+        n, depth, chi, gates = circuits[ci]
+        zr = O.expect_z(run_reference_chain(n, gates, 1e-8, chi, "c128"), 1)
+        errs.append(abs(z[ci] - zr))
+        if getattr(args, "c4_storage_ref", False):
+            errs_c64.append(abs(O.expect_z(run_reference_chain(n, gates, 1e-8, chi, "c64"), 1) - zr))
+    out = {"checked": len(errs)}
+    if errs:
+        out["Z1_err"] = {"max": max(errs), "median": float(np.median(errs)),
+                         "le_1e-6": int(sum(e <= 1e-6 for e in errs))}
+    if errs_c64:
+        out["Z1_err_fp64_split_c64_storage"] = {"max": max(errs_c64), "median": float(np.median(errs_c64))}
+    return out
+
+
+def c4check(qt, args):
+    """The oracle check of a c4 run's dumped <Z_1> values, on the CPU."""
+    import oracle as O
+    with open(args.c4_dump) as f:
+        d = json.load(f)
+    rng = np.random.default_rng(4096)
+    circuits = c4_circuits(d["circuits"], rng)
+    return dict({"config": "c4check", "circuits": d["circuits"]}, **c4_errors(O, circuits, d["Z1"], args, rng))
 
 
 def c5(qt, args):
@@ -279,22 +409,35 @@ def c5(qt, args):
         m.upload_site(1, first / math.sqrt(m.norm2()))
 
     # the FP64 reference run splits with cuSOLVER (FP64, the faster of the
-    # two FP64 paths at bond 3 chi)
-    for mode, dt in (("chosen", np.complex64), ("cusolver", np.complex128)):
+    # two FP64 paths at bond 3 chi) on complex128 storage; --c5-storage-ref
+    # adds the same FP64 splits on complex64 storage (the floor of that storage)
+    runs = [("chosen", np.complex64), ("cusolver", np.complex128)]
+    if args.c5_storage_ref:
+        runs.append(("cusolver", np.complex64))
+    for mode, dt in runs:
         eng = qt.Engine(mode=mode, tc_gemm=1 if mode == "chosen" else 0)
         m = eng.mps([s.astype(dt) for s in sites], dtype=dt)
         normalise(m)
         m.compress(cutoff, chi, mode=mode)
         t0 = time.perf_counter()
+        energies = []
         for _ in range(steps):
             m.apply_mpo(mpo)
             m.compress(cutoff, chi, mode=mode)
             normalise(m)
+            energies.append(m.expect_mpo(mpo))
         sec = time.perf_counter() - t0
-        res[mode] = {"seconds": sec, "energy": m.expect_mpo(mpo)}
+        key = mode if (dt == np.complex128 or mode == "chosen") else mode + "_c64"
+        res[key] = {"seconds": sec, "energy": energies[-1], "energies": energies}
+        if mode == "chosen":
+            res[key]["cert"] = eng.cert_counters()
         m.free()
         eng.close()
     res["dE"] = abs(res["chosen"]["energy"] - res["cusolver"]["energy"])
+    res["dE_max_over_steps"] = max(abs(x - y) for x, y in zip(res["chosen"]["energies"], res["cusolver"]["energies"]))
+    if "cusolver_c64" in res:
+        res["dE_max_fp64_split_c64_storage"] = max(abs(x - y) for x, y in zip(res["cusolver_c64"]["energies"],
+                                                                               res["cusolver"]["energies"]))
     return res
 
 
@@ -359,6 +502,16 @@ def main():
     ap.add_argument("--c2-chis", type=int, nargs="+", default=[64, 256, 1024])
     ap.add_argument("--c3-depth", type=int, default=20)
     ap.add_argument("--c3-observables", action="store_true")
+    ap.add_argument("--c3-n", type=int, default=64)
+    ap.add_argument("--c3-chi-max", type=int, default=1024)
+    ap.add_argument("--c3-ref-json", nargs="*", default=[], help="c3ref outputs (JSON) to compare <ZZ> with")
+    ap.add_argument("--c3-ref-storage", default="c128", choices=["c128", "c64"])
+    ap.add_argument("--c3-ablate", action="store_true", help="also run c3 without the rank model")
+    ap.add_argument("--c4-dump", default=None, help="write the per-circuit <Z_1> to this JSON (for c4check)")
+    ap.add_argument("--c4-storage-ref", action="store_true")
+    ap.add_argument("--c4-autotune", default=None, help="autotuner cache (JSON): time the tuned launch shapes too")
+    ap.add_argument("--c4-tune-circuits", type=int, default=256)
+    ap.add_argument("--c5-storage-ref", action="store_true")
     ap.add_argument("--c4-circuits", type=int, default=4096)
     ap.add_argument("--c4-check", type=int, default=24)
     ap.add_argument("--c5-chi", type=int, default=512)
@@ -366,7 +519,7 @@ def main():
     ap.add_argument("--cpu-reps", type=int, default=5)
     args = ap.parse_args()
     qt = None
-    if any(c not in ("cpu", "cpu1") for c in args.configs):
+    if any(c not in ("cpu", "cpu1", "c3ref", "c4check") for c in args.configs):
         import __graft_entry__ as g
         qt = g.load_package()
     # one process per GPU (torchrun): only c4 shards; rank 0 prints
@@ -379,7 +532,8 @@ def main():
         if c != "c4" and rank != 0:
             continue
         t0 = time.perf_counter()
-        r = {"c1": c1, "c2": c2, "c3": c3, "c4": c4, "c5": c5, "cpu": cpu, "cpu1": cpu1}[c](qt, args)
+        r = {"c1": c1, "c2": c2, "c3": c3, "c3ref": c3ref, "c4": c4, "c4check": c4check, "c5": c5, "cpu": cpu,
+             "cpu1": cpu1}[c](qt, args)
         r["wall_seconds"] = time.perf_counter() - t0
         if rank == 0:
             print(json.dumps(r), flush=True)
