@@ -146,3 +146,48 @@ def test_errors_are_reported(eng, engine):
     bad[0, 0] = np.nan
     with pytest.raises(engine.EngineError):
         mps.apply_2q(bad, 1, 0.0, 0)
+
+
+@pytest.mark.parametrize("chi", [256, 1024])
+def test_plain_single_bond_sweep_matches_oracle(eng, chi):
+    # the single-bond workload in complex128 (theta = Q1 diag(0.97^k) Q2^H,
+    # Haar gate, truncation back to chi) in plain mode against the oracle's
+    # update (src/switch.jl:26-54 split, src/svd.jl:29-33 rule): identical
+    # ranks, and theta' rebuilt from the new sites within 1e-10 ||theta'||
+    rng = np.random.default_rng(7 + chi)
+    a, b, _ = O.decay_theta_factors(chi, rng)
+    g = O.haar_unitary(rng)
+    cutoff = 1e-10
+    mps = eng.mps([a, b])
+    st = mps.apply_2q(g, 1, cutoff, chi)
+    sites = [a.copy(), b.copy()]
+    ref = O.apply_2q(sites, g, 1, cutoff, chi)
+    tail = np.sqrt(np.cumsum(ref.s[::-1] ** 2))[::-1]
+    near = np.abs(tail / cutoff - 1.0).min()  # a tie of the tail rule would show here
+    assert st["rank"] == ref.rank, (st, ref.rank, near)
+    assert st["rank_cutoff"] == ref.rank_cutoff, (st, ref.rank_cutoff, near)
+    np.testing.assert_allclose(st["discarded_weight"], ref.discarded_weight, rtol=1e-9)
+    got = O.theta_of(mps.site(1), mps.site(2))
+    want = O.theta_of(*sites)
+    assert np.linalg.norm(got - want) <= 1e-10 * np.sqrt(ref.norm2)
+    mps.free()
+
+
+def test_chosen_single_bond_at_chi_64_complex64(engine):
+    # the same workload at chi = 64 in complex64, chosen mode: the exact rank
+    # and a truncation error within 1.1x of the exact FP64 split's
+    rng = np.random.default_rng(71)
+    chi = 64
+    a, b, _ = O.decay_theta_factors(chi, rng)
+    g = O.haar_unitary(rng)
+    a32, b32 = a.astype(np.complex64), b.astype(np.complex64)
+    ex = O.apply_2q([a32.astype(complex), b32.astype(complex)], g, 1, 1e-10, chi)
+    ch = engine.Engine(mode="chosen", tc_gemm=1)
+    m = ch.mps([a32, b32], dtype=np.complex64)
+    st = m.apply_2q(g, 1, 1e-10, chi)
+    assert st["rank"] == ex.rank == chi
+    th = O.apply_gate_to_theta(O.theta_of(a32.astype(complex), b32.astype(complex)), g, chi, chi)
+    err = np.linalg.norm(th - O.theta_of(m.site(1).astype(complex), m.site(2).astype(complex)))
+    assert err <= 1.1 * np.sqrt(ex.discarded_weight), (err, np.sqrt(ex.discarded_weight))
+    m.free()
+    ch.close()
