@@ -162,7 +162,7 @@ def test_plain_single_bond_sweep_matches_oracle(eng, chi):
     st = mps.apply_2q(g, 1, cutoff, chi)
     sites = [a.copy(), b.copy()]
     ref = O.apply_2q(sites, g, 1, cutoff, chi)
-    tail = np.sqrt(np.cumsum(ref.s[::-1] ** 2))[::-1]
+    tail = np.sqrt(np.cumsum(ref.spectrum[::-1] ** 2))[::-1]
     near = np.abs(tail / cutoff - 1.0).min()  # a tie of the tail rule would show here
     assert st["rank"] == ref.rank, (st, ref.rank, near)
     assert st["rank_cutoff"] == ref.rank_cutoff, (st, ref.rank_cutoff, near)
