@@ -1142,7 +1142,8 @@ static int update_impl(qt_handle* h, qt_mps* mps, int site, const double* G, dou
   replace_site(h, mps, site + 1, k, cr, Bn, sizeof(TO) * k * n);
   mps->spectrum[site].assign(o.s.begin(), o.s.begin() + std::min<size_t>(o.s.size(), (size_t)k));
   mps->bond_updates[site]++;
-  if (mode == QT_MODE_PLAIN && cutoff >= 0) qt_rank_model_log(h, feat, o.k, kmax);
+  // the rank model learns from exact FP64 splits (the engine's Jacobi or cuSOLVER)
+  if ((mode == QT_MODE_PLAIN || mode == QT_MODE_CUSOLVER) && cutoff >= 0) qt_rank_model_log(h, feat, o.k, kmax);
   QT_CHECK_CUDA(h, cudaStreamSynchronize(h->stream));
   if (st) {
     st->rank = k;

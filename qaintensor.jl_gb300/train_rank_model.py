@@ -1,11 +1,15 @@
 """Train the learned-rank MLP from exact kept ranks logged by the plain FP64 path.
 
-Training data: every update of a seeded ensemble run in plain mode (exact
-FP64 Jacobi SVD, the rank from the tail rule) is logged by the engine as
+Training data: every update of a seeded ensemble run with an exact FP64
+split (the rank from the tail rule) is logged by the engine as
 (16 features, k / k_max):
 
+* depth-10 runs of the 64-qubit Haar brickwork ensemble (chi_max 1024,
+  cutoff 1e-8, complex128), split by cuSOLVER's exact FP64 SVD, the faster
+  exact path at the 1024 x 1024 theta' of the tenth layer;
 * brickwork circuits of depth 10 with Haar gates on 16-40 qubits,
-  chi_max in {16, 32, 64, 128}, cutoffs 1e-10 .. 1e-4;
+  chi_max in {16, 32, 64, 128}, cutoffs 1e-10 .. 1e-4 (the engine's FP64
+  Jacobi);
 * single-bond updates of decaying-spectrum bonds theta = Q1 diag(d^k) Q2^H
   (d in 0.80 .. 0.98, chi 64 .. 512) under Haar gates, cutoffs 1e-8 .. 1e-3,
   the bond's spectrum supplied as the previous spectrum.
@@ -14,7 +18,7 @@ The network is then trained on the GPU with the engine's forward/backward
 and Adam kernels.  Parameters go to rank_model_params.npy next to this file
 and a summary to rank_model_train.json.
 
-    python qaintensor.jl_gb300/train_rank_model.py [--circuits 48] [--bonds 96]
+    python qaintensor.jl_gb300/train_rank_model.py [--c3-circuits 24] [--circuits 48] [--bonds 96]
 """
 
 from __future__ import annotations
@@ -53,11 +57,20 @@ def decay_bond(chi, d, rng):
     return a, b, s
 
 
-def collect(eng, circuits: int, bonds: int, seed: int, log=print):
+def collect(eng, circuits: int, bonds: int, seed: int, c3_circuits: int = 0, log=print):
     rng = np.random.default_rng(seed)
     eng.set_rank_logging(True)
     eng.clear_rank_log()
     t0 = time.time()
+    for c in range(c3_circuits):
+        n, depth = 64, 10
+        mps = eng.product_state(n)
+        for layer in range(1, depth + 1):
+            mps.set_circuit_position(layer, depth)
+            for w in range(1 if layer % 2 else 2, n, 2):
+                mps.apply_2q(haar(rng), w, 1e-8, 1024, mode="cusolver")
+        mps.free()
+        log(f"  64-qubit circuits {c + 1}/{c3_circuits}: {eng.rank_log()[1].size} samples, {time.time() - t0:.0f}s")
     for c in range(circuits):
         n = int(rng.integers(16, 41))
         chi_max = int(rng.choice([16, 32, 64, 128]))
@@ -89,6 +102,7 @@ def collect(eng, circuits: int, bonds: int, seed: int, log=print):
 
 def main():
     ap = argparse.ArgumentParser()
+    ap.add_argument("--c3-circuits", type=int, default=24)
     ap.add_argument("--circuits", type=int, default=48)
     ap.add_argument("--bonds", type=int, default=96)
     ap.add_argument("--epochs", type=int, default=200)
@@ -100,7 +114,7 @@ def main():
     qt = g.load_package()
     eng = qt.Engine(mode="plain")
     t0 = time.time()
-    X, Y = collect(eng, args.circuits, args.bonds, args.seed)
+    X, Y = collect(eng, args.circuits, args.bonds, args.seed, args.c3_circuits)
     t_log = time.time() - t0
     rng = np.random.default_rng(args.seed + 1)
     idx = rng.permutation(len(Y))
@@ -114,7 +128,9 @@ def main():
     np.save(args.out, eng.rank_params())
     summary = {"samples": int(len(Y)), "train": int(len(tr)), "val": int(nval), "train_mse": loss,
                "val_rmse_fraction": val_rmse, "log_seconds": t_log, "train_seconds": t_train,
-               "epochs": args.epochs, "seed": args.seed, "circuits": args.circuits, "bonds": args.bonds}
+               "epochs": args.epochs, "seed": args.seed, "c3_circuits": args.c3_circuits,
+               "c3_samples": int(args.c3_circuits * sum(len(range(1 if l % 2 else 2, 64, 2)) for l in range(1, 11))),
+               "circuits": args.circuits, "bonds": args.bonds}
     with open(os.path.join(HERE, "rank_model_train.json"), "w") as f:
         json.dump(summary, f, indent=1)
     if args.log:
