@@ -327,7 +327,7 @@ int qt_batch_reset(qt_handle* h, qt_batch* b);
 int qt_batch_task_stats(qt_handle* h, const qt_batch* b, int* rank, int* sweeps, float* discarded);
 /* Launch shape of the persistent layer kernel for circuits whose bond cap
  * lies in the bucket bucket_cap (16: caps <= 16, 32, 64, 128): threads per CTA
- * (128, 256 or 512) and CTAs per SM (1 to 4).  A program runs one launch per
+ * (128, 256, 512 or 1024) and CTAs per SM (1 to 4).  A program runs one launch per
  * layer and bucket; set the shapes before qt_batch_run (the graph captures
  * them).  Defaults 256 threads, 1 CTA per SM; the autotuner chooses them. */
 int qt_batch_set_launch(qt_handle* h, qt_batch* b, int bucket_cap, int threads, int ctas_per_sm);

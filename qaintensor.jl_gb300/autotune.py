@@ -3,8 +3,8 @@
 Two choices are tuned on the GPU the engine runs on:
 
 * the launch shape of the batched path's persistent layer kernel, per
-  bond-cap bucket (caps 16, 32, 64, 128): threads per CTA (128, 256, 512)
-  and CTAs per SM (1, 2, 4).  Each candidate runs the same seeded ensemble
+  bond-cap bucket (caps 16, 32, 64, 128): threads per CTA (128 to 1024)
+  and CTAs per SM (1 or 2).  Each candidate runs the same seeded ensemble
   of Haar brickwork circuits (qubits uniform in [8, 40], depths uniform in
   [4, 24], every circuit at the bucket's cap) as a captured CUDA graph;
   the fastest replay wins.  Every candidate computes the same updates -- a
@@ -37,7 +37,7 @@ from typing import Dict, Iterable, List, Sequence, Tuple
 import numpy as np
 
 BUCKETS = (16, 32, 64, 128)
-BATCH_CANDIDATES: Tuple[Tuple[int, int], ...] = ((128, 1), (128, 2), (128, 4), (256, 1), (256, 2), (512, 1))
+BATCH_CANDIDATES: Tuple[Tuple[int, int], ...] = ((128, 2), (256, 1), (256, 2), (512, 1), (512, 2), (1024, 1))
 SKETCH_CANDIDATES: Tuple[float, ...] = (1.0625, 1.125, 1.1875, 1.25)
 
 

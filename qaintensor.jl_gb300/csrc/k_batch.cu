@@ -670,6 +670,7 @@ extern "C" int qt_batch_run(qt_handle* h, qt_batch* b, int nlayers, const int* l
       switch (b->threads[bk]) {
         case 128: QT_LAUNCH(h, batch_layer_kernel<128>, grid, 128, 0, al); break;
         case 512: QT_LAUNCH(h, batch_layer_kernel<512>, grid, 512, 0, al); break;
+        case 1024: QT_LAUNCH(h, batch_layer_kernel<1024>, grid, 1024, 0, al); break;
         default: QT_LAUNCH(h, batch_layer_kernel<256>, grid, 256, 0, al); break;
       }
     }
@@ -738,8 +739,8 @@ extern "C" int qt_batch_set_launch(qt_handle* h, qt_batch* b, int bucket_cap, in
   if (!h || !b) return qt_fail(h, QT_EINVAL, "batch_set_launch: bad argument");
   if (bucket_cap != 16 && bucket_cap != 32 && bucket_cap != 64 && bucket_cap != 128)
     return qt_fail(h, QT_EINVAL, "batch_set_launch: bucket_cap must be 16, 32, 64 or 128");
-  if (threads != 128 && threads != 256 && threads != 512)
-    return qt_fail(h, QT_EINVAL, "batch_set_launch: threads must be 128, 256 or 512");
+  if (threads != 128 && threads != 256 && threads != 512 && threads != 1024)
+    return qt_fail(h, QT_EINVAL, "batch_set_launch: threads must be 128, 256, 512 or 1024");
   if (ctas_per_sm < 1 || ctas_per_sm > 4) return qt_fail(h, QT_EINVAL, "batch_set_launch: ctas_per_sm must be 1..4");
   const int bk = bucket_of(bucket_cap);
   b->threads[bk] = threads;

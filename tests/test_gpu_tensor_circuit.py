@@ -80,14 +80,17 @@ def test_qft_without_decompose(engine, optimize):
 
 def test_decomposed_two_and_three_qubit_gates(engine):
     # test/test_tensor_circuit.jl:62-126: decompose! chains of non-symmetric
-    # gates (controlled-Y pins "U acts on the input legs")
+    # gates (controlled-Y pins "U acts on the input legs").  A one-qubit gate
+    # has no chain: it is inserted as one tensor whose row leg meets the state
+    # (src/tensor_circuit.jl:44-51), i.e. as its transpose -- Y^T = -Y here,
+    # which the dense reference must apply too
     rng = np.random.default_rng(22)
     psi = net_chain(rng, [6, 7, 5])
     gates = [(controlled(X), (3, 1)), (controlled(Y), (3, 1)), (controlled(Y), (1, 2)), (controlled(Z), (2, 1)),
              (controlled(SWAP), (4, 1, 3)), (Y, (2,)), (controlled(X, 2), (4, 1, 2)), (Z, (3,))]
     state = O.contract(psi).reshape(-1, order="F")
     for m, w in gates:
-        state = O.apply_statevector(state, m, w)
+        state = O.apply_statevector(state, m.T if len(w) == 1 else m, w)
         O.tensor_circuit(psi, m, w, is_decompose=True)
     eng = engine.Engine(mode="plain")
     got = gpu_contract(engine, eng, psi)
