@@ -108,6 +108,7 @@ def main():
     ap.add_argument("--epochs", type=int, default=200)
     ap.add_argument("--seed", type=int, default=2026)
     ap.add_argument("--out", default=os.path.join(HERE, "rank_model_params.npy"))
+    ap.add_argument("--summary", default=os.path.join(HERE, "rank_model_train.json"))
     ap.add_argument("--log", default="", help="also save the logged (features, rank) samples to this .npz")
     args = ap.parse_args()
     import __graft_entry__ as g
@@ -131,7 +132,7 @@ def main():
                "epochs": args.epochs, "seed": args.seed, "c3_circuits": args.c3_circuits,
                "c3_samples": int(args.c3_circuits * sum(len(range(1 if l % 2 else 2, 64, 2)) for l in range(1, 11))),
                "circuits": args.circuits, "bonds": args.bonds}
-    with open(os.path.join(HERE, "rank_model_train.json"), "w") as f:
+    with open(args.summary, "w") as f:
         json.dump(summary, f, indent=1)
     if args.log:
         np.savez_compressed(args.log, X=X, Y=Y)

@@ -79,12 +79,16 @@ def theta_prime(a, b, g):
     return th.reshape((2 * chi_l, 2 * chi_r), order="F")
 
 
-def load_rank_model(eng):
-    p = os.path.join(HERE, "rank_model_params.npy")
+RANK_MODEL = os.path.join(ROOT, "qaintensor.jl_gb300", "rank_model_params.npy")
+
+
+def load_rank_model(eng, path=None):
+    """Enable the shipped rank model (or the one at `path`); returns its path or None."""
+    p = path or RANK_MODEL
     if os.path.exists(p):
         eng.set_rank_params(np.load(p), enable=True)
-        return True
-    return False
+        return os.path.relpath(p, ROOT)
+    return None
 
 
 def c1(qt, args):
@@ -217,7 +221,7 @@ def c3(qt, args):
             refs[r["storage"]] = np.array(r["ZZ"])
     for use_model in ((True, False) if args.c3_ablate else (True,)):
         eng = qt.Engine(mode="chosen", tc_gemm=1)
-        model = load_rank_model(eng) if use_model else False
+        model = load_rank_model(eng, args.rank_model) if use_model else None
         mps = eng.product_state(n, dtype=np.complex64)
         eng.sync()
         t0 = time.perf_counter()
@@ -507,6 +511,7 @@ def main():
     ap.add_argument("--c3-ref-json", nargs="*", default=[], help="c3ref outputs (JSON) to compare <ZZ> with")
     ap.add_argument("--c3-ref-storage", default="c128", choices=["c128", "c64"])
     ap.add_argument("--c3-ablate", action="store_true", help="also run c3 without the rank model")
+    ap.add_argument("--rank-model", default=None, help="rank-model parameters (.npy) instead of the shipped ones")
     ap.add_argument("--c4-dump", default=None, help="write the per-circuit <Z_1> to this JSON (for c4check)")
     ap.add_argument("--c4-storage-ref", action="store_true")
     ap.add_argument("--c4-autotune", default=None, help="autotuner cache (JSON): time the tuned launch shapes too")
