@@ -20,6 +20,16 @@ tail_rule.npz    spectra and cutoffs with the tail rule's kept rank (clamped
 tfim10.npz       10-site TFIM MPO (J = 1, h seeded in [0.5, 1.5]), a seeded
                  chi = 12 MPS, compression then 3 rounds of MPO application +
                  compression (cutoff 1e-9, chi_max 12): ranks and <H> per round.
+
+Two more fixtures come from the workload-config runner, because one run of
+each takes about twenty minutes on four host cores:
+
+c3_zz_fp64_c128.json  <Z_i Z_i+1> on all 63 bonds of the 64-qubit, depth-20
+                      Haar brickwork (seed 64, chi_max 1024, cutoff 1e-8) run
+                      by the FP64 oracle:
+                      python tests/run_configs.py c3ref --c3-ref-storage c128
+c3_zz_fp64_c64.json   the same with every updated site rounded to complex64:
+                      python tests/run_configs.py c3ref --c3-ref-storage c64
 """
 
 import os
