@@ -1036,6 +1036,16 @@ pair_apply32_kernel(float2* __restrict__ X, int64_t ldx, int mm, float2* __restr
 // wait is bounded; a wait that gives up sets QT_FLAG_ABORT, which ends the
 // other CTAs' waits too.  The pending unitaries of the last round are applied
 // in place by pair_apply32_kernel after the last sweep.
+//
+// With halves = 2 each pair is served by two CTAs, CTA 2q + h holding rows
+// [row_lo(h), row_hi(h)) of the pair's columns (and the matching rows of V).
+// A row half reads and writes only its own rows, so each half runs the round
+// protocol above on its own copies of the round flags, unitaries and rotate
+// decisions (done, wbuf, rotbuf offset by h); the two halves of a pair meet
+// once per round: each publishes its partial Gram (the 160 upper-tile entries
+// of its rows) in gx and its round in xflag, waits (bounded) for the other's,
+// and both add the two partials in the same order.  Both then run the same
+// pair solver on the same Gram and reach the same unitary, bit for bit.
 
 constexpr int PS_SLAB = 256;                 // rows per slab
 constexpr int PS_LDS = JC + 2;               // slab row stride in float2 (16-byte aligned rows)
@@ -1192,7 +1202,8 @@ jacobi_sweep32_kernel(float2* __restrict__ xb0, float2* __restrict__ xb1, int64_
                       int has_prev, double tol, float tol_inner, double nu_rel2, const double* __restrict__ xnorm2,
                       float2* __restrict__ wbuf, int* __restrict__ rotbuf, int* __restrict__ done,
                       int* __restrict__ flags, int max_inner, float keep2, float* __restrict__ dnorm,
-                      unsigned long long* phase_ns, int spin, int stall) {
+                      unsigned long long* phase_ns, int spin, int stall, int halves, int row_mid, int vrow_mid,
+                      float2* __restrict__ gx, int* __restrict__ xflag) {
   extern __shared__ __align__(16) float2 ps_slab[];  // [2][PS_SLAB][PS_LDS]
   __shared__ __align__(16) float2 wsub[2][JC][JW];    // 16x8 unitary blocks that rebuild the two blocks
   __shared__ float2 psum[3][PS_TILES * PS_TE];
@@ -1200,7 +1211,15 @@ jacobi_sweep32_kernel(float2* __restrict__ xb0, float2* __restrict__ xb1, int64_
   __shared__ sweep_solver sh;
   __shared__ int col[JC], scol[2][JC], srcq[2], sside[2], srot[2];
   __shared__ int any_rot, bad, offmax_blk, offbig_blk, offkept_blk;
-  const int t = threadIdx.x, q = blockIdx.x, pairs = gridDim.x, R = nb - 1;
+  const int H = halves, t = threadIdx.x, q = blockIdx.x / H, hf = blockIdx.x % H, pairs = gridDim.x / H,
+            R = nb - 1;
+  // this CTA's rows of X and V, and its half's copies of the round state
+  const int row_lo = hf ? row_mid : 0, row_hi = (hf || H == 1) ? mm : row_mid;
+  const int vrow_lo = hf ? vrow_mid : 0, vrow_hi = (hf || H == 1) ? nn : vrow_mid;
+  done += (size_t)hf * pairs;
+  wbuf += (size_t)hf * 2 * pairs * NGRAM;
+  rotbuf += (size_t)hf * 2 * pairs;
+  if (hf) { phase_ns = nullptr; dnorm = nullptr; }  // half 0 reports for the pair
   __shared__ unsigned long long tp;
   auto phase = [&](int ph) {  // optional diagnostics: time per phase into phase_ns[ph - 1]
     if (phase_ns && t == 0) {
@@ -1220,7 +1239,7 @@ jacobi_sweep32_kernel(float2* __restrict__ xb0, float2* __restrict__ xb1, int64_
   const bool act = tile < PS_TILES;
   int ti = 0, tj = 0;
   if (act) ps_tile(tile, ti, tj);
-  const int nslab = (mm + PS_SLAB - 1) / PS_SLAB;
+  const int nslab = (row_hi - row_lo + PS_SLAB - 1) / PS_SLAB;
   for (int r = 0; r < R; r++) {
     const int g = g0 + r;
     const bool prev = r > 0 || has_prev;
@@ -1353,10 +1372,10 @@ jacobi_sweep32_kernel(float2* __restrict__ xb0, float2* __restrict__ xb1, int64_
       }
     };
     auto build_slab = [&](int s) {
-      const int rr = s * PS_SLAB + lr;
+      const int rr = row_lo + s * PS_SLAB + lr;
       float2 o[JW];
       rebuild(o);
-      if (prev && rr < mm) {
+      if (prev && rr < row_hi) {
 #pragma unroll
         for (int c = 0; c < JW; c++)
           if (oc[c] >= 0) __stcg(dst + rr + ldx * oc[c], o[c]);
@@ -1368,14 +1387,14 @@ jacobi_sweep32_kernel(float2* __restrict__ xb0, float2* __restrict__ xb1, int64_
     float2 acc[PS_TE];
 #pragma unroll
     for (int e = 0; e < PS_TE; e++) acc[e] = make_float2(0.f, 0.f);
-    load_row(src, ldx, mm, lr);
+    load_row(src, ldx, row_hi, row_lo + lr);
     build_slab(0);
     __syncthreads();
     for (int s = 0; s < nslab; s++) {
-      if (s + 1 < nslab) load_row(src, ldx, mm, (s + 1) * PS_SLAB + lr);
+      if (s + 1 < nslab) load_row(src, ldx, row_hi, row_lo + (s + 1) * PS_SLAB + lr);
       if (act) {
         const float2* base = ps_slab + (size_t)(s & 1) * PS_SLAB * PS_LDS;
-        const int rows = min(PS_SLAB, mm - s * PS_SLAB);
+        const int rows = min(PS_SLAB, row_hi - row_lo - s * PS_SLAB);
 #pragma unroll 1
         for (int rr = grp; rr < rows; rr += PS_NGRP) {
           const float4* rowp = reinterpret_cast<const float4*>(base + (size_t)rr * PS_LDS);
@@ -1397,8 +1416,8 @@ jacobi_sweep32_kernel(float2* __restrict__ xb0, float2* __restrict__ xb1, int64_
     if (prev && vb0) {
       const float2* __restrict__ vsrc = ((g - 1) & 1) ? vb1 : vb0;
       float2* __restrict__ vdst = (g & 1) ? vb1 : vb0;
-      for (int rr = lr; rr < nn; rr += PS_SLAB) {
-        load_row(vsrc, ldv, nn, rr);
+      for (int rr = vrow_lo + lr; rr < vrow_hi; rr += PS_SLAB) {
+        load_row(vsrc, ldv, vrow_hi, rr);
         float2 o[JW];
         rebuild(o);
 #pragma unroll
@@ -1425,8 +1444,34 @@ jacobi_sweep32_kernel(float2* __restrict__ xb0, float2* __restrict__ xb1, int64_
       psum[part][ent] = v;
     }
     __syncthreads();
+    float2 xv = make_float2(0.f, 0.f);
     if (t < PS_TILES * PS_TE) {
-      const float2 v = cadd(cadd(psum[0][t], psum[1][t]), psum[2][t]);
+      xv = cadd(cadd(psum[0][t], psum[1][t]), psum[2][t]);
+      if (H > 1) __stcg(gx + (((size_t)(g & 1) * pairs + q) * H + hf) * (PS_TILES * PS_TE) + t, xv);
+    }
+    if (H > 1) {
+      // the two row halves of the pair exchange their partial Grams (bounded wait)
+      __threadfence();
+      __syncthreads();
+      int gave = 0;
+      if (t == 0) {
+        st_release_gpu(xflag + (size_t)hf * pairs + q, g);
+        int it = 0;
+        for (; it < spin; it++) {
+          if (ld_acquire_gpu(xflag + (size_t)(1 - hf) * pairs + q) >= g) break;
+          if (*(volatile int*)(flags + QT_FLAG_ABORT)) { it = spin; break; }
+          __nanosleep(32);
+        }
+        if (it >= spin) { gave = 1; atomicExch(flags + QT_FLAG_ABORT, 1); }
+      }
+      if (__syncthreads_or(gave)) return;
+      if (t < PS_TILES * PS_TE) {
+        const float2 o = __ldcg(gx + (((size_t)(g & 1) * pairs + q) * H + (1 - hf)) * (PS_TILES * PS_TE) + t);
+        xv = hf == 0 ? cadd(xv, o) : cadd(o, xv);  // (half 0) + (half 1) in both CTAs
+      }
+    }
+    if (t < PS_TILES * PS_TE) {
+      const float2 v = xv;
       int ai, aj;
       ps_tile(t / PS_TE, ai, aj);
       const int e = t % PS_TE;
@@ -1478,16 +1523,18 @@ jacobi_sweep32_kernel(float2* __restrict__ xb0, float2* __restrict__ xb1, int64_
     if (t == 0) {
       if (bad) atomicOr(&flags[QT_FLAG_NONFINITE], 1);
       __stcg(rotbuf + (size_t)(g & 1) * pairs + q, any_rot);
-      if (offmax_blk > 0) atomicMax(&flags[QT_FLAG_OFFMAX], offmax_blk);
-      if (offbig_blk > 0) atomicMax(&flags[QT_FLAG_OFFBIG], offbig_blk);
-      if (offkept_blk > 0) atomicMax(&flags[QT_FLAG_OFFKEPT], offkept_blk);
-      if (any_rot) atomicAdd(&flags[QT_FLAG_ROTATED], 1);
+      if (hf == 0) {  // the pair's statistics, once
+        if (offmax_blk > 0) atomicMax(&flags[QT_FLAG_OFFMAX], offmax_blk);
+        if (offbig_blk > 0) atomicMax(&flags[QT_FLAG_OFFBIG], offbig_blk);
+        if (offkept_blk > 0) atomicMax(&flags[QT_FLAG_OFFKEPT], offkept_blk);
+        if (any_rot) atomicAdd(&flags[QT_FLAG_ROTATED], 1);
+      }
     }
     phase(3);  // 2: reduction, scaled Gram, test
     if (any_rot) {
       int buf = 0;
       const int inner = diagonalise_lanes(sh, col, tol_inner, nu2, max_inner, &buf);
-      if (t == 0) atomicAdd(&flags[QT_FLAG_INNER], inner);
+      if (t == 0 && hf == 0) atomicAdd(&flags[QT_FLAG_INNER], inner);
       // each solver thread stores the entry it finished itself
       if (owner) __stcg(wbuf + (size_t)(g & 1) * pairs * NGRAM + (size_t)q * NGRAM + t, sh.W[buf][i][j]);
     }
@@ -1528,8 +1575,9 @@ int qt_jacobi_layout(int64_t mm, int64_t nn, int* nb_out, int* chunks_out) {
   chunks = std::max(1, std::min<int>(chunks, (int)((mm + 127) / 128)));
   *nb_out = nb;
   *chunks_out = chunks;
-  // double2 entries: partial Grams, ||X||_F^2, one 16x16 unitary per pair, rotate flags
-  return pairs * chunks * NGRAM + 1 + pairs * NGRAM + (pairs + 1) / 2;
+  // double2 entries: partial Grams, ||X||_F^2, two round slots of one 16x16
+  // unitary per pair, two round slots of the pairs' rotate flags
+  return pairs * chunks * NGRAM + 1 + pairs * NGRAM + pairs;
 }
 
 // Cluster shape of the one-launch round: the smallest cluster (<= 8 CTAs)
@@ -1608,9 +1656,12 @@ static bool sweep32_fits(qt_handle* h, int pairs) {
 static int launch_sweep32(qt_handle* h, int pairs, float2* x0, float2* x1, int64_t ldx, int mm, float2* v0,
                           float2* v1, int64_t ldv, int nn, int nb, int g0, int has_prev, double tol, float tol_inner,
                           double nu_rel2, const double* xnorm2, float2* wbuf, int* rotbuf, int* done, int max_inner,
-                          float keep2, float* dnorm, unsigned long long* phase_ns) {
+                          float keep2, float* dnorm, unsigned long long* phase_ns, int halves, float2* gx,
+                          int* xflag) {
+  // row split of the two halves of a pair: at a multiple of 32 rows
+  const int row_mid = ((mm / 2 + 31) / 32) * 32, vrow_mid = ((nn / 2 + 31) / 32) * 32;
   cudaLaunchConfig_t lc = {};
-  lc.gridDim = dim3((unsigned)pairs);
+  lc.gridDim = dim3((unsigned)(pairs * halves));
   lc.blockDim = dim3(NTG);
   lc.dynamicSmemBytes = PS_SMEM;
   lc.stream = h->stream;
@@ -1628,7 +1679,8 @@ static int launch_sweep32(qt_handle* h, int pairs, float2* x0, float2* x1, int64
   if (h->prof) qt_prof_before(h, "jacobi_sweep32_kernel");
   const cudaError_t e = cudaLaunchKernelEx(&lc, jacobi_sweep32_kernel, x0, x1, ldx, mm, v0, v1, ldv, nn, nb, g0,
                                            has_prev, tol, tol_inner, nu_rel2, xnorm2, wbuf, rotbuf, done, h->d_flags,
-                                           max_inner, keep2, dnorm, phase_ns, spin, stall);
+                                           max_inner, keep2, dnorm, phase_ns, spin, stall, halves, row_mid, vrow_mid,
+                                           gx, xflag);
   if (h->prof) qt_prof_after(h);
   h->launches++;
   if (e != cudaSuccess)
@@ -1726,10 +1778,31 @@ int qt_jacobi_svd_ws(qt_handle* h, TS* X, int64_t mm, int64_t nn, int64_t ldx, T
   double prev_tail2 = -1.0, prev_change = -1.0;
   static const double keep_tol =
       std::getenv("QT_JACOBI_KEEP_TOL") ? std::atof(std::getenv("QT_JACOBI_KEEP_TOL")) : 1e-3;
+  // Two CTAs per pair (each holding half of the rows) when the doubled grid
+  // is still resident and each half has rows to work on; QT_JACOBI_HALVES=1
+  // keeps one CTA per pair.  The halves run on their own copies of the round
+  // flags, unitaries and rotate decisions, and exchange partial Grams.
+  const int halves_env = std::getenv("QT_JACOBI_HALVES") ? std::atoi(std::getenv("QT_JACOBI_HALVES")) : 2;
+  const int halves = (sweep_kernel && halves_env == 2 && mm >= 512 && sweep32_fits(h, 2 * pairs)) ? 2 : 1;
+  float2* gx = nullptr;
+  int* xflag = nullptr;
+  if (sweep_kernel && halves == 2) {
+    double2* wb2;
+    int *rf2, *dn2;
+    QT_TRY(pscratch.get(&wb2, (size_t)2 * pairs * NGRAM));  // 2 halves x 2 round slots x pairs x NGRAM float2
+    QT_TRY(pscratch.get(&rf2, (size_t)4 * pairs));
+    QT_TRY(pscratch.get(&dn2, (size_t)2 * pairs));
+    QT_TRY(pscratch.get(&xflag, (size_t)2 * pairs));
+    QT_TRY(pscratch.get(&gx, (size_t)2 * pairs * 2 * 160));
+    wbuf = wb2;
+    rotf = rf2;
+    done = dn2;
+    QT_CHECK_CUDA(h, cudaMemsetAsync(xflag, 0xff, sizeof(int) * 2 * pairs, h->stream));
+  }
   if (sweep_kernel) {
     QT_TRY(pscratch.get(&X1, (size_t)ldx * nn));
     if (V) QT_TRY(pscratch.get(&V1, (size_t)ldv * nn));
-    QT_CHECK_CUDA(h, cudaMemsetAsync(done, 0xff, sizeof(int) * pairs, h->stream));
+    QT_CHECK_CUDA(h, cudaMemsetAsync(done, 0xff, sizeof(int) * pairs * halves, h->stream));
     if (keep_track) {
       QT_TRY(pscratch.get(&dnorm, (size_t)nn));
       hnorm.resize(nn);
@@ -1751,7 +1824,7 @@ int qt_jacobi_svd_ws(qt_handle* h, TS* X, int64_t mm, int64_t nn, int64_t ldx, T
       if constexpr (sizeof(typename real_of<TS>::type) == 4) {
         QT_TRY(launch_sweep32(h, pairs, (float2*)X, (float2*)X1, ldx, (int)mm, (float2*)V, (float2*)V1, ldv, (int)nn,
                               nb, gcount, pending ? 1 : 0, tol, (float)tol_inner, nu_rel2, (const double*)xnorm2,
-                              (float2*)wbuf, rotf, done, max_inner, keep2, dnorm, phase_ns));
+                              (float2*)wbuf, rotf, done, max_inner, keep2, dnorm, phase_ns, halves, gx, xflag));
       }
       gcount += rounds;
       pending = true;

@@ -177,3 +177,31 @@ def test_cluster_cholqr_equals_four_kernel_passes(engine, monkeypatch, chi):
         out.append(S[:k])
     for other in out[1:]:
         assert np.abs(out[0] - other).max() <= 1e-4 * ref[0]
+
+
+@pytest.mark.parametrize("shape", [(2048, 1152), (1100, 1003), (700, 1400)])
+def test_sweep_kernel_row_halves_equal_one_cta_per_pair(engine, monkeypatch, shape):
+    """Two CTAs per pair (each holding half of the rows, the pair's partial
+    Grams exchanged every round) against one CTA per pair
+    (QT_JACOBI_HALVES=1): the same truncation -- rank, values within the
+    FP32 floor, errors within 1.1x of the exact SVD's."""
+    rng = np.random.default_rng(3 * sum(shape))
+    m, n = shape
+    M, _ = graded(rng, m, n, 0.97)
+    M32 = M.astype(np.complex64)
+    floor = 4 * np.sqrt(max(m, n)) * 5.96e-8 * np.linalg.norm(M32)
+    ref = np.linalg.svd(M32.astype(np.complex128), compute_uv=False)
+    out = []
+    for halves in ("1", "2"):
+        monkeypatch.setenv("QT_JACOBI_HALVES", halves)
+        eng = engine.Engine(mode="chosen", jacobi_kernel=0)
+        out.append(eng.truncated_svd(M32, 50 * floor, mode="chosen"))
+        eng.close()
+    (U0, S0, V0, k0, _), (U1, S1, V1, k1, _) = out
+    assert abs(k0 - k1) <= 1
+    k = min(k0, k1)
+    assert np.abs(S0[:k] - S1[:k]).max() <= 2 * floor
+    for U, S, Vh, kk in ((U0, S0, V0, k0), (U1, S1, V1, k1)):
+        err = np.linalg.norm((U * S) @ Vh - M32)
+        assert err <= 1.1 * np.sqrt(np.sum(ref[kk:] ** 2)) + floor, (err, floor)
+        assert np.abs(U.conj().T @ U - np.eye(kk)).max() <= 2e-6 * np.sqrt(m)
