@@ -205,3 +205,93 @@ def test_pingpong_rebuild_equals_in_place_rotation():
                     if c >= 0:
                         fin[:, c] = out[:, i]
         assert np.allclose(fin, seq)
+
+
+def run_schedule_halves(nb, sweeps, seed):
+    """The protocol with two CTAs per pair (row halves): each half runs the
+    rounds above on its own copies of the columns' rows, the unitaries and the
+    round flags, and the two halves of a pair exchange partial Grams once per
+    round (publish its partial into slot g&1 of the pair, then wait for the
+    other half's).  Checks the same properties, plus that an exchange reads
+    the partner's partial of the same round and that a partial is never
+    overwritten before the partner has read it."""
+    rnd = random.Random(seed)
+    P, R = nb // 2, nb - 1
+    G = sweeps * R
+    H = 2
+    buf = [[{b: 0 for b in range(nb)}, {b: -1 for b in range(nb)}] for _ in range(H)]
+    wslot = [[[-1] * P, [-1] * P] for _ in range(H)]
+    done = [[-1] * P for _ in range(H)]
+    xflag = [[-1] * P for _ in range(H)]
+    gx = {}          # (slot, q, h) -> round of the partial held
+    consumed = {}    # (slot, q, h) -> whether the partner has read it
+    state = {(q, h): (0, "A") for q in range(P) for h in range(H)}
+    active, reads_of = {}, {}
+    sweep_end = R
+    while True:
+        cand = []
+        for (q, h), (g, st) in state.items():
+            if g >= min(G, sweep_end):
+                continue
+            if st == "A" and not all(done[h][t] >= g - 1 for t in wait_targets(g, g % R, q, nb)):
+                continue
+            if st == "Y" and xflag[1 - h][q] < g:
+                continue
+            cand.append((q, h))
+        if not cand:
+            if any(g < G for (g, _) in state.values()):
+                assert all(g == sweep_end for (g, _) in state.values()), "deadlock"
+                sweep_end += R
+                continue
+            break
+        q, h = rnd.choice(cand)
+        g, st = state[(q, h)]
+        r = g % R
+        bi, bj = tournament(r, q, nb)
+        if st == "A":
+            locs = []
+            for b in (bi, bj):
+                if g > 0:
+                    qq, _ = pair_of((r - 1) % R, b, nb)
+                    assert wslot[h][(g - 1) & 1][qq] == g - 1, "unitary read before it was written"
+                    locs.append(("w", h, (g - 1) & 1, qq))
+                    for c in tournament((r - 1) % R, qq, nb):
+                        assert buf[h][(g - 1) & 1][c] == g - 1, "rows read before they were written"
+                        locs.append(("x", h, (g - 1) & 1, c))
+                else:
+                    locs.append(("x", h, 0, b))
+            reads_of[(q, h)] = locs
+            for loc in locs:
+                active.setdefault(loc, set()).add((q, h))
+            state[(q, h)] = (g, "X")
+        elif st == "X":
+            key = (g & 1, q, h)
+            assert key not in gx or consumed[key], "partial overwritten before the partner read it"
+            gx[key], consumed[key] = g, False
+            xflag[h][q] = g
+            state[(q, h)] = (g, "Y")
+        elif st == "Y":
+            key = (g & 1, q, 1 - h)
+            assert gx.get(key) == g, "exchange read a partial of another round"
+            consumed[key] = True
+            state[(q, h)] = (g, "B")
+        elif st == "B":
+            writes = [("w", h, g & 1, q)] + ([("x", h, g & 1, bi), ("x", h, g & 1, bj)] if g > 0 else [])
+            for w in writes:
+                assert not (active.get(w, set()) - {(q, h)}), "write while another CTA reads"
+            for kind, hh, sl, idx in writes:
+                (buf[hh][sl] if kind == "x" else wslot[hh][sl])[idx] = g
+            state[(q, h)] = (g, "C")
+        else:
+            for loc in reads_of.pop((q, h)):
+                active[loc].discard((q, h))
+            done[h][q] = g
+            state[(q, h)] = (g + 1, "A")
+    assert done == [[G - 1] * P] * H
+
+
+@pytest.mark.parametrize("nb", [2, 4, 6, 16, 34])
+@pytest.mark.parametrize("sweeps", [1, 3])
+def test_row_halves_protocol_random_schedules(nb, sweeps):
+    for seed in range(40 if nb <= 16 else 10):
+        run_schedule_halves(nb, sweeps, seed)
