@@ -219,8 +219,10 @@ def c3(qt, args):
             r = json.load(f)
         if (r["n"], r["depth"], r["chi_max"]) == (n, depth, chi_max):
             refs[r["storage"]] = np.array(r["ZZ"])
+    opts = {"jacobi_tol": args.c3_jacobi_tol} if args.c3_jacobi_tol else {}
+    out["jacobi_tol"] = args.c3_jacobi_tol or "default"
     for use_model in ((True, False) if args.c3_ablate else (True,)):
-        eng = qt.Engine(mode="chosen", tc_gemm=1)
+        eng = qt.Engine(mode="chosen", tc_gemm=1, **opts)
         model = load_rank_model(eng, args.rank_model) if use_model else None
         mps = eng.product_state(n, dtype=np.complex64)
         eng.sync()
@@ -511,6 +513,7 @@ def main():
     ap.add_argument("--c3-ref-json", nargs="*", default=[], help="c3ref outputs (JSON) to compare <ZZ> with")
     ap.add_argument("--c3-ref-storage", default="c128", choices=["c128", "c64"])
     ap.add_argument("--c3-ablate", action="store_true", help="also run c3 without the rank model")
+    ap.add_argument("--c3-jacobi-tol", type=float, default=0.0, help="FP32 Jacobi tolerance (0: the engine's default)")
     ap.add_argument("--rank-model", default=None, help="rank-model parameters (.npy) instead of the shipped ones")
     ap.add_argument("--c4-dump", default=None, help="write the per-circuit <Z_1> to this JSON (for c4check)")
     ap.add_argument("--c4-storage-ref", action="store_true")
