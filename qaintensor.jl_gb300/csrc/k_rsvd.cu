@@ -245,6 +245,122 @@ __host__ __device__ constexpr size_t cq_smem_bytes(int nrb) {
          BW * sizeof(double) + BW * sizeof(float) + 16;
 }
 
+// Step (E) of a CholeskyQR pass, called by all 256 threads of the CTA.
+// From the FP32 Gram in the upper triangle of Gl (row stride CQ_RS) and its
+// FP64 diagonal Gd: R = chol(G + shift trace(G) I) in place of the Gram's
+// upper triangle, then X = R^{-1}, both blocked by 8 columns.  Cholesky: for
+// each diagonal block, warp 0 runs its 8 pivot steps on the block's rows
+// of every column to the right (lane l: column k0 + l, an 8-row register
+// window moving down one row per step, rows travelling by shuffles), then
+// all threads subtract the block's rank-8 product from the trailing upper
+// triangle.  Inverse: the four 8 x 8 diagonal blocks by column sweeps (one
+// warp each), then the blocks at distance d = 1, 2, 3 from the diagonal,
+// X_ij = -X_ii (sum_{i < l <= j} R_il X_lj).  Pivots past b are skipped
+// (1 / R[k][k] = 0 there), so X is zero outside the leading b x b block.
+// Ry receives 1 / R[k][k] (and the tiny pivot at Ry[BW]), Xs = R^{-1}
+// (BW x BW, row-major), Tb is 256 entries of scratch.  `report` marks the
+// one CTA that raises QT_FLAG_CHOL for a non-positive pivot.
+__device__ void cq_factor(float2* __restrict__ Gl, const double* __restrict__ Gd, float* __restrict__ Ry,
+                          float2* __restrict__ Xs, float2* __restrict__ Tb, int b, double shift,
+                          int* __restrict__ flags, bool report) {
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+  float* trs = (float*)(Ry + BW);
+  if (w == 0) {
+    double tr = lane < b ? Gd[lane] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) tr += __shfl_xor_sync(0xffffffffu, tr, o);
+    if (lane < b) Gl[lane * CQ_RS + lane] = make_float2((float)(Gd[lane] + shift * tr), 0.f);
+    Ry[lane] = 0.f;
+    if (lane == 0) trs[0] = (float)(fabs(tr) * 1e-30 + 1e-37);
+  }
+  __syncthreads();
+  for (int k0 = 0; k0 < b; k0 += 8) {
+    if (w == 0) {
+      const int col = k0 + lane;
+      float2 c[8];
+#pragma unroll
+      for (int r = 0; r < 8; r++)
+        c[r] = (col < BW && k0 + r <= col) ? Gl[(k0 + r) * CQ_RS + col] : make_float2(0.f, 0.f);
+      // dn: the next pivot as seen by its own lane (lane kk + 1 holds
+      // R[k][k + 1] itself), so the pivot chain needs no row shuffle
+      float dn = c[0].x;
+#pragma unroll
+      for (int kk = 0; kk < 8; kk++) {
+        const int k = k0 + kk;
+        if (k < b) {
+          float d = __shfl_sync(0xffffffffu, dn, kk);
+          if (!(d > 0.f)) {
+            if (lane == 0 && report) atomicOr(&flags[QT_FLAG_CHOL], 1);
+            d = trs[0];
+          }
+          const float y = rsqrtf(d);
+          const float2 rk =
+              lane == kk ? make_float2(d * y, 0.f) : (lane > kk ? cscale(c[0], y) : make_float2(0.f, 0.f));
+          dn = c[1].x - (rk.x * rk.x + rk.y * rk.y);
+          if (col < BW) Gl[k * CQ_RS + col] = rk;  // row k of R (zeros left of the diagonal)
+          if (lane == 0) Ry[k] = y;
+#pragma unroll
+          for (int r = 1; r < 8; r++) {
+            float2 rkr;  // R[k][k + r] from lane kk + r (slots past the block are discarded)
+            rkr.x = __shfl_sync(0xffffffffu, rk.x, min(kk + r, 31));
+            rkr.y = __shfl_sync(0xffffffffu, rk.y, min(kk + r, 31));
+            c[r - 1] = csub(c[r], cmul(cconj(rkr), rk));
+          }
+        }
+      }
+    }
+    __syncthreads();
+    // trailing upper triangle: warp w the rows k0 + 8 + w, + 16, ...;
+    // lane j column j (two partial sums)
+    for (int i = k0 + 8 + w; i < BW; i += 8) {
+      if (lane >= i) {
+        float2 v0 = Gl[i * CQ_RS + lane], v1 = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int q = 0; q < 8; q += 2) {
+          v0 = csub(v0, cmul(cconj(Gl[(k0 + q) * CQ_RS + i]), Gl[(k0 + q) * CQ_RS + lane]));
+          v1 = csub(v1, cmul(cconj(Gl[(k0 + q + 1) * CQ_RS + i]), Gl[(k0 + q + 1) * CQ_RS + lane]));
+        }
+        Gl[i * CQ_RS + lane] = cadd(v0, v1);
+      }
+    }
+    __syncthreads();
+  }
+  // diagonal blocks of X; the blocks below the diagonal are zero
+  if (w < 4 && lane < 8) {
+    const int k0 = 8 * w;
+    float2 x[8];
+#pragma unroll
+    for (int r = 0; r < 8; r++) x[r] = make_float2(r == lane ? 1.f : 0.f, 0.f);
+#pragma unroll
+    for (int kk = 7; kk >= 0; kk--) {
+      x[kk] = cscale(x[kk], Ry[k0 + kk]);
+#pragma unroll
+      for (int i = 0; i < kk; i++) x[i] = csub(x[i], cmul(Gl[(k0 + i) * CQ_RS + k0 + kk], x[kk]));
+    }
+#pragma unroll
+    for (int r = 0; r < 8; r++) Xs[(k0 + r) * BW + k0 + lane] = x[r];
+  }
+  for (int e = t; e < BW * BW; e += 256)
+    if ((e / BW) / 8 > (e % BW) / 8) Xs[e] = make_float2(0.f, 0.f);
+  __syncthreads();
+  for (int d = 1; d < 4; d++) {
+    const int bi = t / 64, a = (t / 8) % 8, cc = t % 8, bj = bi + d, i = 8 * bi + a, j = 8 * bj + cc;
+    if (bj < 4) {
+      float2 v = make_float2(0.f, 0.f);
+      for (int l = 8 * (bi + 1); l < 8 * (bj + 1); l++) cfma(v, Gl[i * CQ_RS + l], Xs[l * BW + j]);
+      Tb[t] = v;
+    }
+    __syncthreads();
+    if (bj < 4) {
+      float2 v = make_float2(0.f, 0.f);
+#pragma unroll
+      for (int q = 0; q < 8; q++) cfma(v, Xs[i * BW + 8 * bi + q], Tb[64 * bi + 8 * q + cc]);
+      Xs[i * BW + j] = make_float2(-v.x, -v.y);
+    }
+    __syncthreads();
+  }
+}
+
 // CholeskyQR passes of one FP32 block (m x b, b <= 32) in one launch: a
 // thread-block cluster of CS CTAs holds the block's rows in shared memory
 // (CTA q: rows 32 NRB q .. 32 NRB (q+1) - 1, zero-padded), and each pass
@@ -380,117 +496,9 @@ __global__ void __launch_bounds__(256, 1) cholqr_cluster_kernel(float2* __restri
     }
     __syncthreads();
     phase(5);  // gather
-    // (E) R = chol(G + shift trace(G) I) in place of the Gram's upper
-    // triangle, then X = R^{-1}, both blocked by 8 columns.  Cholesky: for
-    // each diagonal block, warp 0 runs its 8 pivot steps on the block's rows
-    // of every column to the right (lane l: column k0 + l, an 8-row register
-    // window moving down one row per step, rows travelling by shuffles), then
-    // all threads subtract the block's rank-8 product from the trailing upper
-    // triangle.  Inverse: the four 8 x 8 diagonal blocks by column sweeps (one
-    // warp each), then the blocks at distance d = 1, 2, 3 from the diagonal,
-    // X_ij = -X_ii (sum_{i < l <= j} R_il X_lj).  Pivots past b are skipped
-    // (1 / R[k][k] = 0 there), so X is zero outside the leading b x b block.
-    {
-      float* trs = (float*)(Ry + BW);
-      if (w == 0) {
-        double tr = lane < b ? Gd[lane] : 0.0;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) tr += __shfl_xor_sync(0xffffffffu, tr, o);
-        const double shift = p == 0 ? shift0 : 0.0;
-        if (lane < b) Gl[lane * CQ_RS + lane] = make_float2((float)(Gd[lane] + shift * tr), 0.f);
-        Ry[lane] = 0.f;
-        if (lane == 0) trs[0] = (float)(fabs(tr) * 1e-30 + 1e-37);
-      }
-      __syncthreads();
-      for (int k0 = 0; k0 < b; k0 += 8) {
-        if (w == 0) {
-          const int col = k0 + lane;
-          float2 c[8];
-#pragma unroll
-          for (int r = 0; r < 8; r++)
-            c[r] = (col < BW && k0 + r <= col) ? Gl[(k0 + r) * CQ_RS + col] : make_float2(0.f, 0.f);
-          // dn: the next pivot as seen by its own lane (lane kk + 1 holds
-          // R[k][k + 1] itself), so the pivot chain needs no row shuffle
-          float dn = c[0].x;
-#pragma unroll
-          for (int kk = 0; kk < 8; kk++) {
-            const int k = k0 + kk;
-            if (k < b) {
-              float d = __shfl_sync(0xffffffffu, dn, kk);
-              if (!(d > 0.f)) {
-                if (lane == 0 && crank == 0) atomicOr(&flags[QT_FLAG_CHOL], 1);
-                d = trs[0];
-              }
-              const float y = rsqrtf(d);
-              const float2 rk =
-                  lane == kk ? make_float2(d * y, 0.f) : (lane > kk ? cscale(c[0], y) : make_float2(0.f, 0.f));
-              dn = c[1].x - (rk.x * rk.x + rk.y * rk.y);
-              if (col < BW) Gl[k * CQ_RS + col] = rk;  // row k of R (zeros left of the diagonal)
-              if (lane == 0) Ry[k] = y;
-#pragma unroll
-              for (int r = 1; r < 8; r++) {
-                float2 rkr;  // R[k][k + r] from lane kk + r (slots past the block are discarded)
-                rkr.x = __shfl_sync(0xffffffffu, rk.x, min(kk + r, 31));
-                rkr.y = __shfl_sync(0xffffffffu, rk.y, min(kk + r, 31));
-                c[r - 1] = csub(c[r], cmul(cconj(rkr), rk));
-              }
-            }
-          }
-        }
-        __syncthreads();
-        // trailing upper triangle: warp w the rows k0 + 8 + w, + 16, ...;
-        // lane j column j (two partial sums)
-        for (int i = k0 + 8 + w; i < BW; i += 8) {
-          if (lane >= i) {
-            float2 v0 = Gl[i * CQ_RS + lane], v1 = make_float2(0.f, 0.f);
-#pragma unroll
-            for (int q = 0; q < 8; q += 2) {
-              v0 = csub(v0, cmul(cconj(Gl[(k0 + q) * CQ_RS + i]), Gl[(k0 + q) * CQ_RS + lane]));
-              v1 = csub(v1, cmul(cconj(Gl[(k0 + q + 1) * CQ_RS + i]), Gl[(k0 + q + 1) * CQ_RS + lane]));
-            }
-            Gl[i * CQ_RS + lane] = cadd(v0, v1);
-          }
-        }
-        __syncthreads();
-      }
-      phase(6);  // Cholesky
-      // diagonal blocks of X; the blocks below the diagonal are zero
-      if (w < 4 && lane < 8) {
-        const int k0 = 8 * w;
-        float2 x[8];
-#pragma unroll
-        for (int r = 0; r < 8; r++) x[r] = make_float2(r == lane ? 1.f : 0.f, 0.f);
-#pragma unroll
-        for (int kk = 7; kk >= 0; kk--) {
-          x[kk] = cscale(x[kk], Ry[k0 + kk]);
-#pragma unroll
-          for (int i = 0; i < kk; i++) x[i] = csub(x[i], cmul(Gl[(k0 + i) * CQ_RS + k0 + kk], x[kk]));
-        }
-#pragma unroll
-        for (int r = 0; r < 8; r++) Xs[(k0 + r) * BW + k0 + lane] = x[r];
-      }
-      for (int e = t; e < BW * BW; e += 256)
-        if ((e / BW) / 8 > (e % BW) / 8) Xs[e] = make_float2(0.f, 0.f);
-      __syncthreads();
-      float2* Tb = (float2*)Gt;  // free during (E)
-      for (int d = 1; d < 4; d++) {
-        const int bi = t / 64, a = (t / 8) % 8, cc = t % 8, bj = bi + d, i = 8 * bi + a, j = 8 * bj + cc;
-        if (bj < 4) {
-          float2 v = make_float2(0.f, 0.f);
-          for (int l = 8 * (bi + 1); l < 8 * (bj + 1); l++) cfma(v, Gl[i * CQ_RS + l], Xs[l * BW + j]);
-          Tb[t] = v;
-        }
-        __syncthreads();
-        if (bj < 4) {
-          float2 v = make_float2(0.f, 0.f);
-#pragma unroll
-          for (int q = 0; q < 8; q++) cfma(v, Xs[i * BW + 8 * bi + q], Tb[64 * bi + 8 * q + cc]);
-          Xs[i * BW + j] = make_float2(-v.x, -v.y);
-        }
-        __syncthreads();
-      }
-    }
-    phase(7);  // inverse
+    // (E) R = chol(G + shift trace(G) I) and X = R^{-1}, the same in every CTA
+    cq_factor(Gl, Gd, Ry, Xs, (float2*)Gt, b, p == 0 ? shift0 : 0.0, flags, crank == 0);
+    phase(6);  // Cholesky + inverse
     // (F) rows <- rows X: warp w owns columns 4 cg .. 4 cg + 3 (warps w and
     // w + 4 share a scheduler and take column groups w and 7 - w, which
     // balances the triangle), lane l the rows l + 32 rb
@@ -529,7 +537,7 @@ __global__ void __launch_bounds__(256, 1) cholqr_cluster_kernel(float2* __restri
           if (j0 + c < b) Ys[(rb * 32 + lane) * CQ_LDY + j0 + c] = acc[rb][c];
       __syncthreads();
     }
-    phase(8);  // update
+    phase(7);  // update
   }
 #pragma unroll
   for (int cc = 0; cc < 4; cc++)
@@ -540,7 +548,7 @@ __global__ void __launch_bounds__(256, 1) cholqr_cluster_kernel(float2* __restri
       if (r < m && c < b) Y[r + m * (int64_t)c] = Ys[(lane + 32 * u) * CQ_LDY + c];
     }
   cluster.sync();  // no CTA leaves while another may still read its shared memory
-  phase(9);  // write-back + barrier
+  phase(8);  // write-back + barrier
 }
 
 typedef void (*cq_kernel_t)(float2*, int64_t, int, int, double, int*, unsigned long long*);
@@ -782,6 +790,402 @@ int block_cholqr(qt_handle* h, C* Yb, int64_t m, int b, bool shifted, double2* d
   return QT_OK;
 }
 
+// ---------------------------------------------------------------------------
+// The whole orthonormalisation of an FP32 basis in one cooperative launch.
+// CTA c keeps rows 16 c .. 16 c + 15 of Y (all l columns, zero-padded) in
+// shared memory from start to end, and the steps of the block Gram-Schmidt
+// above (project, shifted CholeskyQR, project, CholeskyQR, CholeskyQR per
+// 32-column block; three CholeskyQR passes for the first block) become
+// phases between grid barriers:
+//   projection of block j0 .. j0 + 31 against the j0 columns before it:
+//     (1) the CTA's partial coefficients Y[rows, :j0]^H Y[rows, block] in
+//         FP32 over its 16 rows, to part[c];                      barrier
+//     (2) CTA c adds the partials of its slice of the j0 x 32 coefficients,
+//         CTAs in order, to coef;                                 barrier
+//     (3) every CTA subtracts Y[rows, :j0] coef from its rows of the block,
+//         the coefficients staged through shared memory 64 rows at a time;
+//   CholeskyQR pass:
+//     (1) the CTA's partial Gram of the block (FP32 over its rows) to
+//         gpart[c];                                               barrier
+//     (2) CTA c adds its slice of the 32 x 32 entries over the CTAs in
+//         float-float, CTAs in order, to gsum;                    barrier
+//     (3) every CTA reads the summed Gram, forms the same R and R^{-1}
+//         (cq_factor) and replaces its rows of the block by rows R^{-1}.
+// The rows go back to global memory once, at the end.  Sums run in a fixed
+// order, so the result is reproducible for a given m.  The barrier is a
+// monotone arrival counter; every wait is bounded, and a wait that gives up
+// sets an abort word (ending the other CTAs' waits) and the handle's sticky
+// device status (2).  Data written by other CTAs is read past L1
+// (ld.global.cg / cp.async.cg).
+// ---------------------------------------------------------------------------
+constexpr int OP_NT = 256;     // threads per CTA
+constexpr int OP_R = 16;       // rows per CTA
+constexpr int OP_KC = 64;      // coefficient rows per staged chunk
+constexpr int OP_SPIN = 1 << 22;  // polls of a barrier wait before it gives up
+
+struct OrthArgs {
+  float2* Y;
+  int64_t m;
+  int l, ldy;     // columns; row stride of the staged rows (float2)
+  float2* part;   // [ncta][l][BW] coefficient partials
+  float2* coef;   // [l][BW] summed coefficients
+  float2* gpart;  // [ncta][BW * BW] Gram partials
+  float4* gsum;   // [BW * BW] summed Gram (re hi, re lo, im hi, im lo)
+  int* bar;       // [0] arrivals, [1] abort word
+  int* flags;     // QT_FLAG_CHOL
+  int* status;    // sticky device status
+  int spin;
+};
+
+__host__ __device__ constexpr size_t op_smem_bytes(int ldy) {
+  return (size_t)OP_R * ldy * sizeof(float2) + 2 * OP_KC * BW * sizeof(float2) + (size_t)BW * CQ_RS * sizeof(float2) +
+         (size_t)BW * BW * sizeof(float2) + OP_NT * sizeof(float2) + BW * sizeof(double) + (BW + 4) * sizeof(float);
+}
+
+__device__ inline int op_ld_acquire(const int* p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ inline void op_cp_async16(void* dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)), "l"(src)
+               : "memory");
+}
+
+// Grid barrier: false (in every thread of the CTA) when a wait gave up.
+__device__ bool op_barrier(const OrthArgs& a, int& epoch) {
+  __syncthreads();
+  epoch++;
+  int ok = 1;
+  if (threadIdx.x == 0) {
+    __threadfence();
+    atomicAdd(a.bar, 1);
+    const int target = epoch * (int)gridDim.x;
+    int it = 0;
+    for (; it < a.spin; it++) {
+      if (op_ld_acquire(a.bar) >= target) break;
+      if (*(volatile int*)(a.bar + 1)) { it = a.spin; break; }
+      __nanosleep(32);
+    }
+    if (it >= a.spin) {
+      ok = 0;
+      atomicExch(a.bar + 1, 1);
+      atomicExch(a.status, 2);
+    }
+    __threadfence();
+  }
+  return __syncthreads_and(ok) != 0;
+}
+
+// Projection of the block at column j0 (> 0) against the columns before it.
+__device__ bool op_project(const OrthArgs& a, float2* Ys, float2* Cs, int j0, int& epoch) {
+  const int t = threadIdx.x, c = blockIdx.x, nc = gridDim.x, L = a.ldy;
+  // (1) partials: tile tau = (previous columns 4 kt .. 4 kt + 3, block columns 8 jt .. 8 jt + 7)
+  float2* part = a.part + (size_t)c * a.l * BW;
+  for (int tau = t; tau < j0; tau += OP_NT) {
+    const int kt = tau >> 2, jt = tau & 3;
+    float2 acc[4][8];
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+#pragma unroll
+      for (int j = 0; j < 8; j++) acc[i][j] = make_float2(0.f, 0.f);
+#pragma unroll 4
+    for (int r = 0; r < OP_R; r++) {
+      const float4* q4 = (const float4*)(Ys + r * L + 4 * kt);
+      const float4* y4 = (const float4*)(Ys + r * L + j0 + 8 * jt);
+      const float4 qa = q4[0], qb = q4[1];
+      const float2 q[4] = {make_float2(qa.x, qa.y), make_float2(qa.z, qa.w), make_float2(qb.x, qb.y),
+                           make_float2(qb.z, qb.w)};
+      float2 y[8];
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        const float4 v = y4[u];
+        y[2 * u] = make_float2(v.x, v.y);
+        y[2 * u + 1] = make_float2(v.z, v.w);
+      }
+#pragma unroll
+      for (int i = 0; i < 4; i++)
+#pragma unroll
+        for (int j = 0; j < 8; j++) cfma_conj(acc[i][j], q[i], y[j]);
+    }
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+      float4* dst = (float4*)(part + (size_t)(4 * kt + i) * BW + 8 * jt);
+#pragma unroll
+      for (int u = 0; u < 4; u++)
+        __stcg(dst + u, make_float4(acc[i][2 * u].x, acc[i][2 * u].y, acc[i][2 * u + 1].x, acc[i][2 * u + 1].y));
+    }
+  }
+  if (!op_barrier(a, epoch)) return false;
+  // (2) this CTA's slice of the j0 * BW coefficients: 8 lanes per entry, lane
+  // s adds the CTAs s S .. s S + S - 1 in order, then a fixed shuffle tree
+  {
+    const int E = j0 * BW, per = (E + nc - 1) / nc, e_lo = c * per, e_hi = min(E, e_lo + per);
+    const int g = t >> 3, s = t & 7, S = (nc + 7) / 8;
+    const size_t stride = (size_t)a.l * BW;
+    for (int e0 = e_lo; e0 < e_hi; e0 += OP_NT / 8) {
+      const int e = e0 + g;
+      float2 v = make_float2(0.f, 0.f);
+      if (e < e_hi) {
+        const int q1 = min(nc, (s + 1) * S);
+#pragma unroll 8
+        for (int q = s * S; q < q1; q++) v = cadd(v, __ldcg(a.part + (size_t)q * stride + e));
+      }
+#pragma unroll
+      for (int o = 1; o < 8; o <<= 1) {
+        v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
+        v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
+      }
+      if (s == 0 && e < e_hi) __stcg(a.coef + e, v);
+    }
+  }
+  if (!op_barrier(a, epoch)) return false;
+  // (3) rows -= rows[:, :j0] coef: thread (rows 4 rt .., block columns 4 jt .., previous columns = ks mod 8)
+  {
+    const int ks = t & 7, jt = (t >> 3) & 7, rt = t >> 6;
+    float2 acc[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+#pragma unroll
+      for (int j = 0; j < 4; j++) acc[i][j] = make_float2(0.f, 0.f);
+    const int nch = (j0 + OP_KC - 1) / OP_KC;
+    auto stage = [&](int ch) {
+      const int k0 = ch * OP_KC, kn = min(OP_KC, j0 - k0);
+      const float2* src = a.coef + (size_t)k0 * BW;
+      float2* dst = Cs + (ch & 1) * OP_KC * BW;
+      for (int p = t; p < kn * BW / 2; p += OP_NT) op_cp_async16(dst + 2 * p, src + 2 * p);
+      asm volatile("cp.async.commit_group;" ::: "memory");
+    };
+    stage(0);
+    for (int ch = 0; ch < nch; ch++) {
+      if (ch + 1 < nch) {
+        stage(ch + 1);
+        asm volatile("cp.async.wait_group 1;" ::: "memory");
+      } else {
+        asm volatile("cp.async.wait_group 0;" ::: "memory");
+      }
+      __syncthreads();
+      const float2* cs = Cs + (ch & 1) * OP_KC * BW;
+      const int k0 = ch * OP_KC, kn = min(OP_KC, j0 - k0);
+      for (int kk = ks; kk < kn; kk += 8) {
+        float2 q[4];
+#pragma unroll
+        for (int i = 0; i < 4; i++) q[i] = Ys[(4 * rt + i) * L + k0 + kk];
+        const float4 ca = *(const float4*)(cs + kk * BW + 4 * jt), cb = *(const float4*)(cs + kk * BW + 4 * jt + 2);
+        const float2 cv[4] = {make_float2(ca.x, ca.y), make_float2(ca.z, ca.w), make_float2(cb.x, cb.y),
+                              make_float2(cb.z, cb.w)};
+#pragma unroll
+        for (int i = 0; i < 4; i++)
+#pragma unroll
+          for (int j = 0; j < 4; j++) cfma(acc[i][j], q[i], cv[j]);
+      }
+      __syncthreads();  // the buffer is restaged two chunks later
+    }
+    // the eight previous-column slices added in order (Cs reused: 8 x 16 x 32 entries)
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+#pragma unroll
+      for (int j = 0; j < 4; j++) Cs[ks * (OP_R * BW) + (4 * rt + i) * BW + 4 * jt + j] = acc[i][j];
+    __syncthreads();
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+      const int o = t + OP_NT * h, r = o / BW, j = o % BW;
+      float2 v = Cs[o];
+#pragma unroll
+      for (int q = 1; q < 8; q++) v = cadd(v, Cs[q * (OP_R * BW) + o]);
+      Ys[r * L + j0 + j] = csub(Ys[r * L + j0 + j], v);
+    }
+    __syncthreads();
+  }
+  return true;
+}
+
+// One CholeskyQR pass of the block at column j0 (b columns).
+__device__ bool op_cholqr(const OrthArgs& a, float2* Ys, float2* Gl, float2* Xs, float2* Tb, double* Gd, float* Ry,
+                          int j0, int b, double shift, int& epoch) {
+  const int t = threadIdx.x, c = blockIdx.x, nc = gridDim.x, L = a.ldy;
+  // (1) partial Gram: thread (i = t mod 32, j = t / 32 + 8 u)
+  {
+    const int i = t & 31, jq = t >> 5;
+    float2 g[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) g[u] = make_float2(0.f, 0.f);
+#pragma unroll 4
+    for (int r = 0; r < OP_R; r++) {
+      const float2 yi = Ys[r * L + j0 + i];
+#pragma unroll
+      for (int u = 0; u < 4; u++) cfma_conj(g[u], yi, Ys[r * L + j0 + jq + 8 * u]);
+    }
+    float2* gp = a.gpart + (size_t)c * BW * BW;
+#pragma unroll
+    for (int u = 0; u < 4; u++) __stcg(gp + i + BW * (jq + 8 * u), g[u]);
+  }
+  if (!op_barrier(a, epoch)) return false;
+  // (2) this CTA's slice of the entries: warp w the entries e_lo + w + 8 v,
+  // lane l the CTAs l, l + 32, ... in float-float, then a fixed shuffle tree
+  {
+    const int per = (BW * BW + nc - 1) / nc, e_lo = c * per, e_hi = min(BW * BW, e_lo + per);
+    const int w = t >> 5, lane = t & 31;
+    for (int e = e_lo + w; e < e_hi; e += OP_NT / 32) {
+      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+      for (int q = lane; q < nc; q += 32) {
+        const float2 x = __ldcg(a.gpart + (size_t)q * BW * BW + e);
+        v = ff4_add(v, make_float4(x.x, 0.f, x.y, 0.f));
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        float4 u;
+        u.x = __shfl_xor_sync(0xffffffffu, v.x, o);
+        u.y = __shfl_xor_sync(0xffffffffu, v.y, o);
+        u.z = __shfl_xor_sync(0xffffffffu, v.z, o);
+        u.w = __shfl_xor_sync(0xffffffffu, v.w, o);
+        v = ff4_add(v, u);
+      }
+      if (lane == 0) __stcg(a.gsum + e, v);
+    }
+  }
+  if (!op_barrier(a, epoch)) return false;
+  // (3) the Gram in FP32 (diagonal in FP64), R, R^{-1}, rows <- rows R^{-1}
+  for (int e = t; e < BW * BW; e += OP_NT) {
+    const int i = e % BW, j = e / BW;
+    if (i <= j) {
+      const float4 v = __ldcg(a.gsum + e);
+      Gl[i * CQ_RS + j] = make_float2(v.x + v.y, v.z + v.w);
+      if (i == j) Gd[i] = (double)v.x + (double)v.y;
+    }
+  }
+  __syncthreads();
+  cq_factor(Gl, Gd, Ry, Xs, Tb, b, shift, a.flags, c == 0);
+  {
+    const int r = t >> 4, jc = 2 * (t & 15);
+    float2 a0 = make_float2(0.f, 0.f), a1 = make_float2(0.f, 0.f);
+#pragma unroll 8
+    for (int k = 0; k < BW; k++) {
+      const float2 y = Ys[r * L + j0 + k];
+      if (k <= jc) cfma(a0, y, Xs[k * BW + jc]);
+      if (k <= jc + 1) cfma(a1, y, Xs[k * BW + jc + 1]);
+    }
+    __syncthreads();  // every row of the block has been read
+    Ys[r * L + j0 + jc] = a0;
+    Ys[r * L + j0 + jc + 1] = a1;
+    __syncthreads();
+  }
+  return true;
+}
+
+__global__ void __launch_bounds__(OP_NT, 1) orth_one_launch_kernel(OrthArgs a) {
+  extern __shared__ __align__(16) unsigned char op_smem[];
+  const int t = threadIdx.x, L = a.ldy;
+  float2* Ys = (float2*)op_smem;          // [OP_R][L]
+  float2* Cs = Ys + (size_t)OP_R * L;     // [2][OP_KC][BW]
+  float2* Gl = Cs + 2 * OP_KC * BW;       // [BW][CQ_RS]
+  float2* Xs = Gl + BW * CQ_RS;           // [BW][BW]
+  float2* Tb = Xs + BW * BW;              // [OP_NT]
+  double* Gd = (double*)(Tb + OP_NT);     // [BW]
+  float* Ry = (float*)(Gd + BW);          // [BW + 1]
+  const int64_t r0 = (int64_t)blockIdx.x * OP_R;
+  for (int e = t; e < OP_R * L; e += OP_NT) {
+    const int rr = e % OP_R, cc = e / OP_R;
+    const int64_t r = r0 + rr;
+    Ys[rr * L + cc] = (r < a.m && cc < a.l) ? a.Y[r + a.m * (int64_t)cc] : make_float2(0.f, 0.f);
+  }
+  __syncthreads();
+  int epoch = 0;
+  for (int j0 = 0; j0 < a.l; j0 += BW) {
+    const int b = min(BW, a.l - j0);
+    const double shift = 11.0 * ((double)a.m * b + (double)b * (b + 1)) * 5.96e-8;
+    if (j0 > 0) {
+      if (!op_project(a, Ys, Cs, j0, epoch)) return;
+      if (!op_cholqr(a, Ys, Gl, Xs, Tb, Gd, Ry, j0, b, shift, epoch)) return;
+      if (!op_project(a, Ys, Cs, j0, epoch)) return;
+      if (!op_cholqr(a, Ys, Gl, Xs, Tb, Gd, Ry, j0, b, 0.0, epoch)) return;
+    } else {
+      if (!op_cholqr(a, Ys, Gl, Xs, Tb, Gd, Ry, j0, b, shift, epoch)) return;
+      if (!op_cholqr(a, Ys, Gl, Xs, Tb, Gd, Ry, j0, b, 0.0, epoch)) return;
+    }
+    if (!op_cholqr(a, Ys, Gl, Xs, Tb, Gd, Ry, j0, b, 0.0, epoch)) return;
+  }
+  for (int e = t; e < OP_R * a.l; e += OP_NT) {
+    const int rr = e % OP_R, cc = e / OP_R;
+    const int64_t r = r0 + rr;
+    if (r < a.m) a.Y[r + a.m * (int64_t)cc] = Ys[rr * L + cc];
+  }
+}
+
+// CTAs and row stride of the one-launch orthonormalisation of an m x l FP32
+// basis; 0 when it does not apply (QT_ORTH_ONE_LAUNCH=0, no cooperative
+// launch, the rows' columns beyond shared memory, or more CTAs than fit).
+int op_shape(int64_t m, int64_t l, int* ldy, size_t* smem) {
+  static int sms = -1, max_smem = 0;
+  if (sms < 0) {
+    int dev = 0, coop = 0;
+    sms = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess &&
+        cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) == cudaSuccess && coop &&
+        cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) == cudaSuccess &&
+        cudaFuncSetAttribute(orth_one_launch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem) ==
+            cudaSuccess)
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaGetLastError();
+  }
+  const char* env = std::getenv("QT_ORTH_ONE_LAUNCH");
+  if ((env && env[0] == '0') || sms <= 0) return 0;
+  *ldy = (int)((l + BW - 1) / BW * BW + 2);
+  *smem = op_smem_bytes(*ldy);
+  if (*smem > (size_t)max_smem) return 0;
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, orth_one_launch_kernel, OP_NT, *smem) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  const int64_t ncta = (m + OP_R - 1) / OP_R;
+  return ncta <= (int64_t)per_sm * sms ? (int)ncta : 0;
+}
+
+int orth_one_launch(qt_handle* h, float2* Y, int64_t m, int64_t l, int ncta, int ldy, size_t smem) {
+  qt_scratch s(h);
+  OrthArgs a;
+  a.Y = Y;
+  a.m = m;
+  a.l = (int)l;
+  a.ldy = ldy;
+  QT_TRY(s.get(&a.part, (size_t)ncta * l * BW));
+  QT_TRY(s.get(&a.coef, (size_t)l * BW));
+  QT_TRY(s.get(&a.gpart, (size_t)ncta * BW * BW));
+  QT_TRY(s.get(&a.gsum, (size_t)BW * BW));
+  QT_TRY(s.get(&a.bar, 2));
+  a.flags = h->d_flags;
+  a.status = h->d_status;
+  if (!a.status) QT_TRY(s.get(&a.status, 1));
+  a.spin = OP_SPIN;
+  QT_CHECK_CUDA(h, cudaMemsetAsync(a.bar, 0, 2 * sizeof(int), h->stream));
+  if (a.status != h->d_status) QT_CHECK_CUDA(h, cudaMemsetAsync(a.status, 0, sizeof(int), h->stream));
+  cudaLaunchConfig_t lc = {};
+  lc.gridDim = dim3((unsigned)ncta);
+  lc.blockDim = dim3(OP_NT);
+  lc.dynamicSmemBytes = smem;
+  lc.stream = h->stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  lc.attrs = attr;
+  lc.numAttrs = 1;
+  if (h->prof) qt_prof_before(h, "orth_one_launch_kernel");
+  const cudaError_t e = cudaLaunchKernelEx(&lc, orth_one_launch_kernel, a);
+  if (h->prof) qt_prof_after(h);
+  h->launches++;
+  if (e != cudaSuccess)
+    return qt_fail(h, QT_ECUDA, std::string("launch orth_one_launch_kernel: ") + cudaGetErrorString(e));
+  if (a.status != h->d_status) {  // a handle without a status word: check here
+    int hs = 0;
+    QT_CHECK_CUDA(h, cudaMemcpyAsync(&hs, a.status, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    QT_CHECK_CUDA(h, cudaStreamSynchronize(h->stream));
+    if (hs) return qt_fail(h, QT_ETIMEOUT, "orthonormalize: a grid barrier wait timed out");
+  }
+  return QT_OK;
+}
+
 }  // namespace
 
 template <typename C>
@@ -797,6 +1201,12 @@ template int qt_gaussian<double2>(qt_handle*, double2*, int64_t, int64_t, int64_
 template <typename C>
 int qt_orthonormalize(qt_handle* h, C* Y, int64_t m, int64_t l) {
   if (l > m) return qt_fail(h, QT_EINVAL, "orthonormalize: more columns than rows");
+  if constexpr (std::is_same<C, float2>::value) {
+    int ldy = 0;
+    size_t smem = 0;
+    const int ncta = op_shape(m, l, &ldy, &smem);
+    if (ncta > 0) return orth_one_launch(h, Y, m, l, ncta, ldy, smem);
+  }
   qt_scratch s(h);
   double2* dG;
   C *coef, *part;
@@ -848,15 +1258,15 @@ int qt_orthonormalize(qt_handle* h, C* Y, int64_t m, int64_t l) {
     if (sizeof(typename real_of<C>::type) == 4) QT_TRY(block_cholqr<C>(h, Yb, m, b, false, dG));
   }
   if (phase_ns && cq_launches > 0) {
-    unsigned long long hp[9];
+    unsigned long long hp[8];
     QT_CHECK_CUDA(h, cudaStreamSynchronize(h->stream));
     QT_CHECK_CUDA(h, cudaMemcpy(hp, phase_ns, sizeof(hp), cudaMemcpyDeviceToHost));
-    const char* nm[9] = {"stage", "gram", "groups+barrier", "scatter+barrier", "gather", "cholesky", "inverse",
+    const char* nm[8] = {"stage", "gram", "groups+barrier", "scatter+barrier", "gather", "cholesky+inverse",
                          "update", "writeback+barrier"};
     std::fprintf(stderr, "cluster CholeskyQR (%d CTAs of %d rows), %d launches, %d passes; SM kilocycles per "
                  "launch (stage, writeback) or pass:", cs, 32 * nrb, cq_launches, cq_passes);
-    for (int i = 0; i < 9; i++)
-      std::fprintf(stderr, " %s %.2f", nm[i], hp[i] * 1e-3 / (i == 0 || i == 8 ? cq_launches : cq_passes));
+    for (int i = 0; i < 8; i++)
+      std::fprintf(stderr, " %s %.2f", nm[i], hp[i] * 1e-3 / (i == 0 || i == 7 ? cq_launches : cq_passes));
     std::fprintf(stderr, "\n");
   }
   return QT_OK;

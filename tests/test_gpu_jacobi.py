@@ -147,15 +147,20 @@ def test_sweep_kernel_equals_two_launch_round_fp32(engine, shape):
         assert err <= 1.1 * np.sqrt(np.sum(ref[kk:] ** 2)) + floor, (err, floor)
 
 
-@pytest.mark.parametrize("chi", [200, 512])
-def test_cluster_cholqr_equals_four_kernel_passes(engine, monkeypatch, chi):
-    """The sketch basis orthonormalised by the one-launch cluster CholeskyQR
-    (the block's rows in the shared memory of 16 CTAs, or of 8 with
-    QT_CHOLQR_CLUSTER=8) and by the four-kernel passes (QT_CHOLQR_CLUSTER=0)
-    gives the same truncation of a rank-deficient
-    theta' at the chi cap: same rank, error within 1.1x of the exact SVD's,
-    values within 1e-4 of the largest.  chi = 200 sketches 264 columns (a
-    last block of 8) over 400 rows (CTAs of 64 rows, the last ones padded)."""
+# the orthonormalisations of an FP32 sketch: (QT_ORTH_ONE_LAUNCH, QT_CHOLQR_CLUSTER)
+ORTH_VARIANTS = {"one-launch": ("1", "1"), "cluster16": ("0", "1"), "cluster8": ("0", "8"), "four-kernel": ("0", "0")}
+
+
+@pytest.mark.parametrize("chi", [200, 512, 1024])
+def test_orthonormalisations_give_the_same_truncation(engine, monkeypatch, chi):
+    """The sketch basis orthonormalised in one cooperative launch (16 rows
+    per CTA in shared memory, grid barriers between the Gram-Schmidt
+    phases), by the one-launch cluster CholeskyQR per block (the block's rows
+    in the shared memory of 16 CTAs, or of 8) with the three projection
+    kernels, and by the four-kernel passes gives the same truncation of a
+    rank-deficient theta' at the chi cap: same rank, error within 1.1x of the
+    exact SVD's, values within 1e-4 of the largest.  chi = 200 sketches 264
+    columns (a last block of 8) over 400 rows (the last CTA's rows padded)."""
     import oracle as O
     rng = np.random.default_rng(5 * chi)
     a, b, _ = O.decay_theta_factors(chi, rng, 0.97)
@@ -164,19 +169,39 @@ def test_cluster_cholqr_equals_four_kernel_passes(engine, monkeypatch, chi):
                                g, chi, chi).astype(np.complex64)
     ref = np.linalg.svd(th.astype(complex), compute_uv=False)
     exact = np.sqrt(np.sum(ref[chi:] ** 2))
-    out = []
-    for flag in ("1", "8", "0"):
-        monkeypatch.setenv("QT_CHOLQR_CLUSTER", flag)
+    out = {}
+    for name, (one, cluster) in ORTH_VARIANTS.items():
+        if chi == 1024 and name == "four-kernel":
+            continue  # the slowest variant adds nothing at this size
+        monkeypatch.setenv("QT_ORTH_ONE_LAUNCH", one)
+        monkeypatch.setenv("QT_CHOLQR_CLUSTER", cluster)
         eng = engine.Engine(mode="chosen", tc_gemm=1)
         U, S, Vh, k, _ = eng.truncated_svd(th, 1e-6, chi_max=chi, mode="chosen")
         eng.close()
-        assert k == chi
+        assert k == chi, name
         err = np.linalg.norm((U * S) @ Vh - th.astype(complex))
-        assert err <= 1.1 * exact, (flag, err, exact)
-        assert np.abs(U.conj().T @ U - np.eye(k)).max() <= 1e-4
-        out.append(S[:k])
-    for other in out[1:]:
-        assert np.abs(out[0] - other).max() <= 1e-4 * ref[0]
+        assert err <= 1.1 * exact, (name, err, exact)
+        assert np.abs(U.conj().T @ U - np.eye(k)).max() <= 1e-4, name
+        out[name] = S[:k]
+    for name, s in out.items():
+        assert np.abs(out["one-launch"] - s).max() <= 1e-4 * ref[0], name
+
+
+def test_one_launch_orthonormalisation_is_reproducible(engine):
+    """Fixed summation orders: two runs of the same sketch give the same
+    factors bit for bit."""
+    import oracle as O
+    rng = np.random.default_rng(77)
+    a, b, _ = O.decay_theta_factors(256, rng, 0.97)
+    th = O.apply_gate_to_theta(O.theta_of(a, b), O.haar_unitary(rng), 256, 256).astype(np.complex64)
+    outs = []
+    for _ in range(2):
+        eng = engine.Engine(mode="chosen", tc_gemm=1)
+        outs.append(eng.truncated_svd(th, 1e-6, chi_max=256, mode="chosen"))
+        eng.close()
+    (U0, S0, V0, k0, _), (U1, S1, V1, k1, _) = outs
+    assert k0 == k1
+    assert np.array_equal(S0, S1) and np.array_equal(U0, U1) and np.array_equal(V0, V1)
 
 
 @pytest.mark.parametrize("shape", [(2048, 1152), (1100, 1003), (700, 1400)])
