@@ -20,6 +20,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <type_traits>
+#include <utility>
 
 #include "qt_internal.cuh"
 
@@ -245,120 +246,96 @@ __host__ __device__ constexpr size_t cq_smem_bytes(int nrb) {
          BW * sizeof(double) + BW * sizeof(float) + 16;
 }
 
-// Step (E) of a CholeskyQR pass, called by all 256 threads of the CTA.
-// From the FP32 Gram in the upper triangle of Gl (row stride CQ_RS) and its
-// FP64 diagonal Gd: R = chol(G + shift trace(G) I) in place of the Gram's
-// upper triangle, then X = R^{-1}, both blocked by 8 columns.  Cholesky: for
-// each diagonal block, warp 0 runs its 8 pivot steps on the block's rows
-// of every column to the right (lane l: column k0 + l, an 8-row register
-// window moving down one row per step, rows travelling by shuffles), then
-// all threads subtract the block's rank-8 product from the trailing upper
-// triangle.  Inverse: the four 8 x 8 diagonal blocks by column sweeps (one
-// warp each), then the blocks at distance d = 1, 2, 3 from the diagonal,
-// X_ij = -X_ii (sum_{i < l <= j} R_il X_lj).  Pivots past b are skipped
-// (1 / R[k][k] = 0 there), so X is zero outside the leading b x b block.
-// Ry receives 1 / R[k][k] (and the tiny pivot at Ry[BW]), Xs = R^{-1}
-// (BW x BW, row-major), Tb is 256 entries of scratch.  `report` marks the
-// one CTA that raises QT_FLAG_CHOL for a non-positive pivot.
-__device__ void cq_factor(float2* __restrict__ Gl, const double* __restrict__ Gd, float* __restrict__ Ry,
-                          float2* __restrict__ Xs, float2* __restrict__ Tb, int b, double shift,
-                          int* __restrict__ flags, bool report) {
-  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
-  float* trs = (float*)(Ry + BW);
-  if (w == 0) {
+// Step (E) of a CholeskyQR pass, called by all threads of the CTA; warp 0
+// does the work.  From the FP32 Gram in the upper triangle of Gl (row
+// stride CQ_RS) and its FP64 diagonal Gd: R = chol(G + shift trace(G) I)
+// and Xs = R^{-1} (BW x BW, row-major, upper triangular).  Lane j holds
+// column j in registers.  Cholesky, right-looking: at pivot k lane k's
+// entry gives R[k][k], row k of R is published in Gl (replacing the
+// Gram's row) and every lane subtracts conj(R[k][i]) R[k][j] from its rows
+// i > k.  Inverse, by rows from the bottom: X[k][k] = 1 / R[k][k] and
+// X[k][j] = -(sum_{k < l <= j} R[k][l] X[l][j]) / R[k][k], lane j's column
+// of R giving way to its column of X.  A non-positive pivot raises
+// QT_FLAG_CHOL (from the CTA marked `report`) and is replaced by a tiny
+// positive value; pivots past b are skipped, so X is zero outside the
+// leading b x b block.
+// pivot K of the register Cholesky (lane j: column j of the Gram in c)
+template <int K>
+__device__ __forceinline__ void cq_chol_step(float2 (&c)[BW], float2* __restrict__ Gl, float& ry, int b, float tiny,
+                                             int* __restrict__ flags, bool report) {
+  const int lane = threadIdx.x & 31;
+  if (K >= b) return;
+  float d = __shfl_sync(0xffffffffu, c[K].x, K);
+  if (!(d > 0.f)) {
+    if (lane == 0 && report) atomicOr(&flags[QT_FLAG_CHOL], 1);
+    d = tiny;
+  }
+  const float y = rsqrtf(d);
+  const float2 r = lane > K ? cscale(c[K], y) : (lane == K ? make_float2(d * y, 0.f) : make_float2(0.f, 0.f));
+  if (lane == K) ry = y;
+  Gl[K * CQ_RS + lane] = r;
+  c[K] = r;
+  __syncwarp();
+#pragma unroll
+  for (int i = K + 1; i < BW; i++) {
+    const float2 ri = Gl[K * CQ_RS + i];  // R[K][i]
+    if (lane >= i) c[i] = csub(c[i], cmul(cconj(ri), r));
+  }
+}
+
+// row K of R^{-1} (rows below K already in c, R's rows in Gl)
+template <int K>
+__device__ __forceinline__ void cq_inv_step(float2 (&c)[BW], const float2* __restrict__ Gl, float ry, int b) {
+  const int lane = threadIdx.x & 31;
+  float2 xk = make_float2(0.f, 0.f);
+  if (K < b) {
+    const float rk = __shfl_sync(0xffffffffu, ry, K);
+    float2 sum = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int l = K + 1; l < BW; l++)
+      if (l <= lane) cfma(sum, Gl[K * CQ_RS + l], c[l]);  // R[K][l] X[l][j]
+    xk = lane == K ? make_float2(rk, 0.f) : (lane > K ? cscale(sum, -rk) : make_float2(0.f, 0.f));
+  }
+  c[K] = xk;
+}
+
+template <int... K>
+__device__ __forceinline__ void cq_chol_all(std::integer_sequence<int, K...>, float2 (&c)[BW], float2* Gl, float& ry,
+                                            int b, float tiny, int* flags, bool report) {
+  (cq_chol_step<K>(c, Gl, ry, b, tiny, flags, report), ...);
+}
+template <int... K>
+__device__ __forceinline__ void cq_inv_all(std::integer_sequence<int, K...>, float2 (&c)[BW], const float2* Gl,
+                                           float ry, int b) {
+  (cq_inv_step<BW - 1 - K>(c, Gl, ry, b), ...);  // from the bottom row up
+}
+
+__device__ void cq_factor(float2* __restrict__ Gl, const double* __restrict__ Gd, float2* __restrict__ Xs, int b,
+                          double shift, int* __restrict__ flags, bool report) {
+  const int t = threadIdx.x, lane = t & 31;
+  if (t < 32) {
     double tr = lane < b ? Gd[lane] : 0.0;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) tr += __shfl_xor_sync(0xffffffffu, tr, o);
-    if (lane < b) Gl[lane * CQ_RS + lane] = make_float2((float)(Gd[lane] + shift * tr), 0.f);
-    Ry[lane] = 0.f;
-    if (lane == 0) trs[0] = (float)(fabs(tr) * 1e-30 + 1e-37);
+    const float tiny = (float)(fabs(tr) * 1e-30 + 1e-37);
+    float2 c[BW];
+#pragma unroll
+    for (int i = 0; i < BW; i++) {
+      float2 v = make_float2(0.f, 0.f);
+      if (lane < b) {
+        if (i < lane) v = Gl[i * CQ_RS + lane];
+        else if (i == lane) v = make_float2((float)(Gd[lane] + shift * tr), 0.f);
+      }
+      c[i] = v;
+    }
+    __syncwarp();  // the Gram is read before its rows are replaced by R's
+    float ry = 0.f;  // lane k: 1 / R[k][k]
+    cq_chol_all(std::make_integer_sequence<int, BW>{}, c, Gl, ry, b, tiny, flags, report);
+    cq_inv_all(std::make_integer_sequence<int, BW>{}, c, Gl, ry, b);
+#pragma unroll
+    for (int i = 0; i < BW; i++) Xs[i * BW + lane] = c[i];
   }
   __syncthreads();
-  for (int k0 = 0; k0 < b; k0 += 8) {
-    if (w == 0) {
-      const int col = k0 + lane;
-      float2 c[8];
-#pragma unroll
-      for (int r = 0; r < 8; r++)
-        c[r] = (col < BW && k0 + r <= col) ? Gl[(k0 + r) * CQ_RS + col] : make_float2(0.f, 0.f);
-      // dn: the next pivot as seen by its own lane (lane kk + 1 holds
-      // R[k][k + 1] itself), so the pivot chain needs no row shuffle
-      float dn = c[0].x;
-#pragma unroll
-      for (int kk = 0; kk < 8; kk++) {
-        const int k = k0 + kk;
-        if (k < b) {
-          float d = __shfl_sync(0xffffffffu, dn, kk);
-          if (!(d > 0.f)) {
-            if (lane == 0 && report) atomicOr(&flags[QT_FLAG_CHOL], 1);
-            d = trs[0];
-          }
-          const float y = rsqrtf(d);
-          const float2 rk =
-              lane == kk ? make_float2(d * y, 0.f) : (lane > kk ? cscale(c[0], y) : make_float2(0.f, 0.f));
-          dn = c[1].x - (rk.x * rk.x + rk.y * rk.y);
-          if (col < BW) Gl[k * CQ_RS + col] = rk;  // row k of R (zeros left of the diagonal)
-          if (lane == 0) Ry[k] = y;
-#pragma unroll
-          for (int r = 1; r < 8; r++) {
-            float2 rkr;  // R[k][k + r] from lane kk + r (slots past the block are discarded)
-            rkr.x = __shfl_sync(0xffffffffu, rk.x, min(kk + r, 31));
-            rkr.y = __shfl_sync(0xffffffffu, rk.y, min(kk + r, 31));
-            c[r - 1] = csub(c[r], cmul(cconj(rkr), rk));
-          }
-        }
-      }
-    }
-    __syncthreads();
-    // trailing upper triangle: warp w the rows k0 + 8 + w, + 16, ...;
-    // lane j column j (two partial sums)
-    for (int i = k0 + 8 + w; i < BW; i += 8) {
-      if (lane >= i) {
-        float2 v0 = Gl[i * CQ_RS + lane], v1 = make_float2(0.f, 0.f);
-#pragma unroll
-        for (int q = 0; q < 8; q += 2) {
-          v0 = csub(v0, cmul(cconj(Gl[(k0 + q) * CQ_RS + i]), Gl[(k0 + q) * CQ_RS + lane]));
-          v1 = csub(v1, cmul(cconj(Gl[(k0 + q + 1) * CQ_RS + i]), Gl[(k0 + q + 1) * CQ_RS + lane]));
-        }
-        Gl[i * CQ_RS + lane] = cadd(v0, v1);
-      }
-    }
-    __syncthreads();
-  }
-  // diagonal blocks of X; the blocks below the diagonal are zero
-  if (w < 4 && lane < 8) {
-    const int k0 = 8 * w;
-    float2 x[8];
-#pragma unroll
-    for (int r = 0; r < 8; r++) x[r] = make_float2(r == lane ? 1.f : 0.f, 0.f);
-#pragma unroll
-    for (int kk = 7; kk >= 0; kk--) {
-      x[kk] = cscale(x[kk], Ry[k0 + kk]);
-#pragma unroll
-      for (int i = 0; i < kk; i++) x[i] = csub(x[i], cmul(Gl[(k0 + i) * CQ_RS + k0 + kk], x[kk]));
-    }
-#pragma unroll
-    for (int r = 0; r < 8; r++) Xs[(k0 + r) * BW + k0 + lane] = x[r];
-  }
-  for (int e = t; e < BW * BW; e += 256)
-    if ((e / BW) / 8 > (e % BW) / 8) Xs[e] = make_float2(0.f, 0.f);
-  __syncthreads();
-  for (int d = 1; d < 4; d++) {
-    const int bi = t / 64, a = (t / 8) % 8, cc = t % 8, bj = bi + d, i = 8 * bi + a, j = 8 * bj + cc;
-    if (bj < 4) {
-      float2 v = make_float2(0.f, 0.f);
-      for (int l = 8 * (bi + 1); l < 8 * (bj + 1); l++) cfma(v, Gl[i * CQ_RS + l], Xs[l * BW + j]);
-      Tb[t] = v;
-    }
-    __syncthreads();
-    if (bj < 4) {
-      float2 v = make_float2(0.f, 0.f);
-#pragma unroll
-      for (int q = 0; q < 8; q++) cfma(v, Xs[i * BW + 8 * bi + q], Tb[64 * bi + 8 * q + cc]);
-      Xs[i * BW + j] = make_float2(-v.x, -v.y);
-    }
-    __syncthreads();
-  }
 }
 
 // CholeskyQR passes of one FP32 block (m x b, b <= 32) in one launch: a
@@ -403,7 +380,6 @@ __global__ void __launch_bounds__(256, 1) cholqr_cluster_kernel(float2* __restri
   float2* Gl = (float2*)(Gr + CQ_E);                              // [BW][CQ_RS] the Gram in FP32, then R
   float2* Xs = Gl + BW * CQ_RS;                                   // [BW][BW] R^{-1}
   double* Gd = (double*)(Xs + BW * BW);                           // [BW] diagonal of the Gram
-  float* Ry = (float*)(Gd + BW);                                  // [BW] 1 / R[k][k], then the tiny pivot
   const int t = threadIdx.x, lane = t & 31, w = t >> 5;
   const int64_t r0 = (int64_t)crank * ROWS;
   // stage: warp w loads columns 4w .. 4w+3, lane l the rows l + 32 u
@@ -497,7 +473,7 @@ __global__ void __launch_bounds__(256, 1) cholqr_cluster_kernel(float2* __restri
     __syncthreads();
     phase(5);  // gather
     // (E) R = chol(G + shift trace(G) I) and X = R^{-1}, the same in every CTA
-    cq_factor(Gl, Gd, Ry, Xs, (float2*)Gt, b, p == 0 ? shift0 : 0.0, flags, crank == 0);
+    cq_factor(Gl, Gd, Xs, b, p == 0 ? shift0 : 0.0, flags, crank == 0);
     phase(6);  // Cholesky + inverse
     // (F) rows <- rows X: warp w owns columns 4 cg .. 4 cg + 3 (warps w and
     // w + 4 share a scheduler and take column groups w and 7 - w, which
@@ -820,7 +796,9 @@ int block_cholqr(qt_handle* h, C* Yb, int64_t m, int b, bool shifted, double2* d
 // ---------------------------------------------------------------------------
 constexpr int OP_NT = 256;     // threads per CTA
 constexpr int OP_R = 16;       // rows per CTA
-constexpr int OP_KC = 64;      // coefficient rows per staged chunk
+constexpr int OP_KC = 32;      // coefficient rows per staged chunk
+constexpr int OP_NBUF = 6;     // staged chunks in the ring (five in flight)
+constexpr int OP_CLD = BW + 2; // row stride of a staged chunk (float2): 272 B, conflict-free float4 reads
 constexpr int OP_SPIN = 1 << 22;  // polls of a barrier wait before it gives up
 
 struct OrthArgs {
@@ -835,11 +813,25 @@ struct OrthArgs {
   int* flags;     // QT_FLAG_CHOL
   int* status;    // sticky device status
   int spin;
+  int light;      // 0: as above; 1: no third CholeskyQR pass; 2: also one projection only
+  unsigned long long* phase_ns;  // optional: CTA 0's time per phase (diagnostics)
 };
 
+// diagnostics: CTA 0's thread 0 adds the time since the previous mark
+// (kept in a.phase_ns[10]) to a.phase_ns[ph]
+__device__ inline void op_mark(const OrthArgs& a, int ph) {
+  if (a.phase_ns && blockIdx.x == 0 && threadIdx.x == 0) {
+    unsigned long long tn;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(tn));
+    if (ph >= 0) a.phase_ns[ph] += tn - a.phase_ns[10];
+    a.phase_ns[10] = tn;
+  }
+}
+
 __host__ __device__ constexpr size_t op_smem_bytes(int ldy) {
-  return (size_t)OP_R * ldy * sizeof(float2) + 2 * OP_KC * BW * sizeof(float2) + (size_t)BW * CQ_RS * sizeof(float2) +
-         (size_t)BW * BW * sizeof(float2) + OP_NT * sizeof(float2) + BW * sizeof(double) + (BW + 4) * sizeof(float);
+  return (size_t)OP_R * ldy * sizeof(float2) + (size_t)OP_NBUF * OP_KC * OP_CLD * sizeof(float2) +
+         (size_t)BW * CQ_RS * sizeof(float2) +
+         (size_t)BW * BW * sizeof(float2) + BW * sizeof(double);
 }
 
 __device__ inline int op_ld_acquire(const int* p) {
@@ -917,7 +909,9 @@ __device__ bool op_project(const OrthArgs& a, float2* Ys, float2* Cs, int j0, in
         __stcg(dst + u, make_float4(acc[i][2 * u].x, acc[i][2 * u].y, acc[i][2 * u + 1].x, acc[i][2 * u + 1].y));
     }
   }
+  op_mark(a, 0);  // coefficient partials
   if (!op_barrier(a, epoch)) return false;
+  op_mark(a, 1);  // barrier
   // (2) this CTA's slice of the j0 * BW coefficients: 8 lanes per entry, lane
   // s adds the CTAs s S .. s S + S - 1 in order, then a fixed shuffle tree
   {
@@ -940,7 +934,9 @@ __device__ bool op_project(const OrthArgs& a, float2* Ys, float2* Cs, int j0, in
       if (s == 0 && e < e_hi) __stcg(a.coef + e, v);
     }
   }
+  op_mark(a, 2);  // coefficient sums
   if (!op_barrier(a, epoch)) return false;
+  op_mark(a, 1);
   // (3) rows -= rows[:, :j0] coef: thread (rows 4 rt .., block columns 4 jt .., previous columns = ks mod 8)
   {
     const int ks = t & 7, jt = (t >> 3) & 7, rt = t >> 6;
@@ -949,30 +945,37 @@ __device__ bool op_project(const OrthArgs& a, float2* Ys, float2* Cs, int j0, in
     for (int i = 0; i < 4; i++)
 #pragma unroll
       for (int j = 0; j < 4; j++) acc[i][j] = make_float2(0.f, 0.f);
-    const int nch = (j0 + OP_KC - 1) / OP_KC;
+    // the coefficients stream through a ring of OP_NBUF chunks of OP_KC
+    // rows, OP_NBUF - 1 chunks in flight; every step commits one copy group
+    // (empty past the last chunk), so waiting for all but the newest
+    // OP_NBUF - 1 groups means chunk ch has landed
+    const int nch = (j0 + OP_KC - 1) / OP_KC;  // j0 is a multiple of BW = OP_KC
     auto stage = [&](int ch) {
-      const int k0 = ch * OP_KC, kn = min(OP_KC, j0 - k0);
-      const float2* src = a.coef + (size_t)k0 * BW;
-      float2* dst = Cs + (ch & 1) * OP_KC * BW;
-      for (int p = t; p < kn * BW / 2; p += OP_NT) op_cp_async16(dst + 2 * p, src + 2 * p);
+      if (ch < nch) {
+        const float2* src = a.coef + (size_t)ch * OP_KC * BW;
+        float2* dst = Cs + (ch % OP_NBUF) * OP_KC * OP_CLD;
+        for (int p = t; p < OP_KC * BW / 2; p += OP_NT) {
+          const int row = p / (BW / 2), c2 = p % (BW / 2);
+          op_cp_async16(dst + row * OP_CLD + 2 * c2, src + row * BW + 2 * c2);
+        }
+      }
       asm volatile("cp.async.commit_group;" ::: "memory");
     };
-    stage(0);
+#pragma unroll 1
+    for (int c = 0; c < OP_NBUF - 1; c++) stage(c);
     for (int ch = 0; ch < nch; ch++) {
-      if (ch + 1 < nch) {
-        stage(ch + 1);
-        asm volatile("cp.async.wait_group 1;" ::: "memory");
-      } else {
-        asm volatile("cp.async.wait_group 0;" ::: "memory");
-      }
+      stage(ch + OP_NBUF - 1);  // into the buffer read in step ch - 1
+      asm volatile("cp.async.wait_group %0;" ::"n"(OP_NBUF - 1) : "memory");
       __syncthreads();
-      const float2* cs = Cs + (ch & 1) * OP_KC * BW;
-      const int k0 = ch * OP_KC, kn = min(OP_KC, j0 - k0);
-      for (int kk = ks; kk < kn; kk += 8) {
+      const float2* cs = Cs + (ch % OP_NBUF) * OP_KC * OP_CLD;
+      const int k0 = ch * OP_KC;
+#pragma unroll
+      for (int kk = ks; kk < OP_KC; kk += 8) {
         float2 q[4];
 #pragma unroll
         for (int i = 0; i < 4; i++) q[i] = Ys[(4 * rt + i) * L + k0 + kk];
-        const float4 ca = *(const float4*)(cs + kk * BW + 4 * jt), cb = *(const float4*)(cs + kk * BW + 4 * jt + 2);
+        const float4 ca = *(const float4*)(cs + kk * OP_CLD + 4 * jt),
+                     cb = *(const float4*)(cs + kk * OP_CLD + 4 * jt + 2);
         const float2 cv[4] = {make_float2(ca.x, ca.y), make_float2(ca.z, ca.w), make_float2(cb.x, cb.y),
                               make_float2(cb.z, cb.w)};
 #pragma unroll
@@ -980,7 +983,7 @@ __device__ bool op_project(const OrthArgs& a, float2* Ys, float2* Cs, int j0, in
 #pragma unroll
           for (int j = 0; j < 4; j++) cfma(acc[i][j], q[i], cv[j]);
       }
-      __syncthreads();  // the buffer is restaged two chunks later
+      __syncthreads();  // the buffer is restaged in the next step
     }
     // the eight previous-column slices added in order (Cs reused: 8 x 16 x 32 entries)
 #pragma unroll
@@ -998,12 +1001,13 @@ __device__ bool op_project(const OrthArgs& a, float2* Ys, float2* Cs, int j0, in
     }
     __syncthreads();
   }
+  op_mark(a, 3);  // projection update
   return true;
 }
 
 // One CholeskyQR pass of the block at column j0 (b columns).
-__device__ bool op_cholqr(const OrthArgs& a, float2* Ys, float2* Gl, float2* Xs, float2* Tb, double* Gd, float* Ry,
-                          int j0, int b, double shift, int& epoch) {
+__device__ bool op_cholqr(const OrthArgs& a, float2* Ys, float2* Gl, float2* Xs, double* Gd, int j0, int b,
+                          double shift, int& epoch) {
   const int t = threadIdx.x, c = blockIdx.x, nc = gridDim.x, L = a.ldy;
   // (1) partial Gram: thread (i = t mod 32, j = t / 32 + 8 u)
   {
@@ -1021,7 +1025,9 @@ __device__ bool op_cholqr(const OrthArgs& a, float2* Ys, float2* Gl, float2* Xs,
 #pragma unroll
     for (int u = 0; u < 4; u++) __stcg(gp + i + BW * (jq + 8 * u), g[u]);
   }
+  op_mark(a, 4);  // Gram partials
   if (!op_barrier(a, epoch)) return false;
+  op_mark(a, 1);
   // (2) this CTA's slice of the entries: warp w the entries e_lo + w + 8 v,
   // lane l the CTAs l, l + 32, ... in float-float, then a fixed shuffle tree
   {
@@ -1045,7 +1051,9 @@ __device__ bool op_cholqr(const OrthArgs& a, float2* Ys, float2* Gl, float2* Xs,
       if (lane == 0) __stcg(a.gsum + e, v);
     }
   }
+  op_mark(a, 5);  // Gram sums
   if (!op_barrier(a, epoch)) return false;
+  op_mark(a, 1);
   // (3) the Gram in FP32 (diagonal in FP64), R, R^{-1}, rows <- rows R^{-1}
   for (int e = t; e < BW * BW; e += OP_NT) {
     const int i = e % BW, j = e / BW;
@@ -1056,7 +1064,9 @@ __device__ bool op_cholqr(const OrthArgs& a, float2* Ys, float2* Gl, float2* Xs,
     }
   }
   __syncthreads();
-  cq_factor(Gl, Gd, Ry, Xs, Tb, b, shift, a.flags, c == 0);
+  op_mark(a, 6);  // Gram gather
+  cq_factor(Gl, Gd, Xs, b, shift, a.flags, c == 0);
+  op_mark(a, 7);  // Cholesky + inverse
   {
     const int r = t >> 4, jc = 2 * (t & 15);
     float2 a0 = make_float2(0.f, 0.f), a1 = make_float2(0.f, 0.f);
@@ -1071,19 +1081,19 @@ __device__ bool op_cholqr(const OrthArgs& a, float2* Ys, float2* Gl, float2* Xs,
     Ys[r * L + j0 + jc + 1] = a1;
     __syncthreads();
   }
+  op_mark(a, 8);  // block update
   return true;
 }
 
 __global__ void __launch_bounds__(OP_NT, 1) orth_one_launch_kernel(OrthArgs a) {
   extern __shared__ __align__(16) unsigned char op_smem[];
   const int t = threadIdx.x, L = a.ldy;
+  op_mark(a, -1);
   float2* Ys = (float2*)op_smem;          // [OP_R][L]
-  float2* Cs = Ys + (size_t)OP_R * L;     // [2][OP_KC][BW]
-  float2* Gl = Cs + 2 * OP_KC * BW;       // [BW][CQ_RS]
+  float2* Cs = Ys + (size_t)OP_R * L;     // [OP_NBUF][OP_KC][OP_CLD]
+  float2* Gl = Cs + OP_NBUF * OP_KC * OP_CLD;  // [BW][CQ_RS]
   float2* Xs = Gl + BW * CQ_RS;           // [BW][BW]
-  float2* Tb = Xs + BW * BW;              // [OP_NT]
-  double* Gd = (double*)(Tb + OP_NT);     // [BW]
-  float* Ry = (float*)(Gd + BW);          // [BW + 1]
+  double* Gd = (double*)(Xs + BW * BW);  // [BW]
   const int64_t r0 = (int64_t)blockIdx.x * OP_R;
   for (int e = t; e < OP_R * L; e += OP_NT) {
     const int rr = e % OP_R, cc = e / OP_R;
@@ -1091,20 +1101,21 @@ __global__ void __launch_bounds__(OP_NT, 1) orth_one_launch_kernel(OrthArgs a) {
     Ys[rr * L + cc] = (r < a.m && cc < a.l) ? a.Y[r + a.m * (int64_t)cc] : make_float2(0.f, 0.f);
   }
   __syncthreads();
+  op_mark(a, 9);  // staging (the mark before it is the kernel start)
   int epoch = 0;
   for (int j0 = 0; j0 < a.l; j0 += BW) {
     const int b = min(BW, a.l - j0);
     const double shift = 11.0 * ((double)a.m * b + (double)b * (b + 1)) * 5.96e-8;
     if (j0 > 0) {
       if (!op_project(a, Ys, Cs, j0, epoch)) return;
-      if (!op_cholqr(a, Ys, Gl, Xs, Tb, Gd, Ry, j0, b, shift, epoch)) return;
-      if (!op_project(a, Ys, Cs, j0, epoch)) return;
-      if (!op_cholqr(a, Ys, Gl, Xs, Tb, Gd, Ry, j0, b, 0.0, epoch)) return;
+      if (!op_cholqr(a, Ys, Gl, Xs, Gd, j0, b, shift, epoch)) return;
+      if (a.light < 2 && !op_project(a, Ys, Cs, j0, epoch)) return;
+      if (!op_cholqr(a, Ys, Gl, Xs, Gd, j0, b, 0.0, epoch)) return;
     } else {
-      if (!op_cholqr(a, Ys, Gl, Xs, Tb, Gd, Ry, j0, b, shift, epoch)) return;
-      if (!op_cholqr(a, Ys, Gl, Xs, Tb, Gd, Ry, j0, b, 0.0, epoch)) return;
+      if (!op_cholqr(a, Ys, Gl, Xs, Gd, j0, b, shift, epoch)) return;
+      if (!op_cholqr(a, Ys, Gl, Xs, Gd, j0, b, 0.0, epoch)) return;
     }
-    if (!op_cholqr(a, Ys, Gl, Xs, Tb, Gd, Ry, j0, b, 0.0, epoch)) return;
+    if (a.light == 0 && !op_cholqr(a, Ys, Gl, Xs, Gd, j0, b, 0.0, epoch)) return;
   }
   for (int e = t; e < OP_R * a.l; e += OP_NT) {
     const int rr = e % OP_R, cc = e / OP_R;
@@ -1120,13 +1131,17 @@ int op_shape(int64_t m, int64_t l, int* ldy, size_t* smem) {
   static int sms = -1, max_smem = 0;
   if (sms < 0) {
     int dev = 0, coop = 0;
+    cudaFuncAttributes fa;
     sms = 0;
     if (cudaGetDevice(&dev) == cudaSuccess &&
         cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) == cudaSuccess && coop &&
         cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) == cudaSuccess &&
-        cudaFuncSetAttribute(orth_one_launch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem) ==
-            cudaSuccess)
-      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaFuncGetAttributes(&fa, orth_one_launch_kernel) == cudaSuccess) {
+      max_smem -= (int)fa.sharedSizeBytes;  // the dynamic part's limit
+      if (cudaFuncSetAttribute(orth_one_launch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem) ==
+          cudaSuccess)
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    }
     cudaGetLastError();
   }
   const char* env = std::getenv("QT_ORTH_ONE_LAUNCH");
@@ -1143,7 +1158,7 @@ int op_shape(int64_t m, int64_t l, int* ldy, size_t* smem) {
   return ncta <= (int64_t)per_sm * sms ? (int)ncta : 0;
 }
 
-int orth_one_launch(qt_handle* h, float2* Y, int64_t m, int64_t l, int ncta, int ldy, size_t smem) {
+int orth_one_launch(qt_handle* h, float2* Y, int64_t m, int64_t l, int ncta, int ldy, size_t smem, int light) {
   qt_scratch s(h);
   OrthArgs a;
   a.Y = Y;
@@ -1159,6 +1174,14 @@ int orth_one_launch(qt_handle* h, float2* Y, int64_t m, int64_t l, int ncta, int
   a.status = h->d_status;
   if (!a.status) QT_TRY(s.get(&a.status, 1));
   a.spin = OP_SPIN;
+  a.light = light;
+  a.phase_ns = nullptr;
+  // QT_ORTH_PHASES=1 prints CTA 0's time per phase after each launch
+  static const bool phases = std::getenv("QT_ORTH_PHASES") != nullptr;
+  if (phases && h->pool) {
+    QT_TRY(s.get(&a.phase_ns, 11));
+    QT_CHECK_CUDA(h, cudaMemsetAsync(a.phase_ns, 0, 11 * sizeof(unsigned long long), h->stream));
+  }
   QT_CHECK_CUDA(h, cudaMemsetAsync(a.bar, 0, 2 * sizeof(int), h->stream));
   if (a.status != h->d_status) QT_CHECK_CUDA(h, cudaMemsetAsync(a.status, 0, sizeof(int), h->stream));
   cudaLaunchConfig_t lc = {};
@@ -1183,6 +1206,17 @@ int orth_one_launch(qt_handle* h, float2* Y, int64_t m, int64_t l, int ncta, int
     QT_CHECK_CUDA(h, cudaStreamSynchronize(h->stream));
     if (hs) return qt_fail(h, QT_ETIMEOUT, "orthonormalize: a grid barrier wait timed out");
   }
+  if (a.phase_ns) {
+    unsigned long long hp[10];
+    QT_CHECK_CUDA(h, cudaMemcpyAsync(hp, a.phase_ns, sizeof(hp), cudaMemcpyDeviceToHost, h->stream));
+    QT_CHECK_CUDA(h, cudaStreamSynchronize(h->stream));
+    const char* nm[10] = {"coef partials", "barriers", "coef sums", "projection update", "Gram partials",
+                          "Gram sums", "Gram gather", "Cholesky+inverse", "block update", "staging"};
+    std::fprintf(stderr, "one-launch orthonormalisation %lldx%lld (%d CTAs), us per launch:", (long long)m,
+                 (long long)l, ncta);
+    for (int i = 0; i < 10; i++) std::fprintf(stderr, " %s %.1f", nm[i], hp[i] * 1e-3);
+    std::fprintf(stderr, "\n");
+  }
   return QT_OK;
 }
 
@@ -1199,13 +1233,21 @@ template int qt_gaussian<float2>(qt_handle*, float2*, int64_t, int64_t, int64_t,
 template int qt_gaussian<double2>(qt_handle*, double2*, int64_t, int64_t, int64_t, uint64_t);
 
 template <typename C>
-int qt_orthonormalize(qt_handle* h, C* Y, int64_t m, int64_t l) {
+int qt_orthonormalize(qt_handle* h, C* Y, int64_t m, int64_t l, bool range_only) {
   if (l > m) return qt_fail(h, QT_EINVAL, "orthonormalize: more columns than rows");
   if constexpr (std::is_same<C, float2>::value) {
     int ldy = 0;
     size_t smem = 0;
     const int ncta = op_shape(m, l, &ldy, &smem);
-    if (ncta > 0) return orth_one_launch(h, Y, m, l, ncta, ldy, smem);
+    // A basis that only carries a range to the next product of a power
+    // iteration needs to be well conditioned, not orthonormal to rounding:
+    // one projection and two CholeskyQR passes per block (QT_ORTH_RANGE=2,
+    // the default; 1 keeps both projections, 0 all three passes).  At the
+    // chi = 1024 bench bond the truncation error is unchanged (1.00014 of
+    // the exact split either way) and the update 4.8 ms faster.
+    const char* env = std::getenv("QT_ORTH_RANGE");
+    const int light = range_only ? (env ? std::atoi(env) : 2) : 0;
+    if (ncta > 0) return orth_one_launch(h, Y, m, l, ncta, ldy, smem, std::min(2, std::max(0, light)));
   }
   qt_scratch s(h);
   double2* dG;
@@ -1271,5 +1313,5 @@ int qt_orthonormalize(qt_handle* h, C* Y, int64_t m, int64_t l) {
   }
   return QT_OK;
 }
-template int qt_orthonormalize<float2>(qt_handle*, float2*, int64_t, int64_t);
-template int qt_orthonormalize<double2>(qt_handle*, double2*, int64_t, int64_t);
+template int qt_orthonormalize<float2>(qt_handle*, float2*, int64_t, int64_t, bool);
+template int qt_orthonormalize<double2>(qt_handle*, double2*, int64_t, int64_t, bool);

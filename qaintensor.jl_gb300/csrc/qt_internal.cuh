@@ -274,7 +274,7 @@ int qt_gaussian(qt_handle* h, C* out, int64_t rows, int64_t cols, int64_t ld, ui
 // Block classical Gram-Schmidt with re-orthogonalisation, intra-block shifted
 // CholeskyQR2 (FP64 Gram / Cholesky): Y (m x l, ld m) -> orthonormal columns.
 template <typename C>
-int qt_orthonormalize(qt_handle* h, C* Y, int64_t m, int64_t l);
+int qt_orthonormalize(qt_handle* h, C* Y, int64_t m, int64_t l, bool range_only = false);
 
 // k_ncon.cu ------------------------------------------------------------------
 // device buffer of a qt_tensor (column-major, its dtype's element)

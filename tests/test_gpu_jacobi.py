@@ -7,6 +7,8 @@ per sweep) and the two-launch round (3)."""
 import numpy as np
 import pytest
 
+import oracle as O
+
 pytestmark = pytest.mark.gpu
 
 
@@ -151,57 +153,67 @@ def test_sweep_kernel_equals_two_launch_round_fp32(engine, shape):
 ORTH_VARIANTS = {"one-launch": ("1", "1"), "cluster16": ("0", "1"), "cluster8": ("0", "8"), "four-kernel": ("0", "0")}
 
 
+def capped_update(engine, a, b, g, chi, env, monkeypatch):
+    """One chosen-mode update of the bond (a, b) at the chi_max = chi cap (the
+    sketched split) under the given environment; returns (stats, site 1, site 2)."""
+    for k, v in env.items():
+        monkeypatch.setenv(k, v)
+    eng = engine.Engine(mode="chosen", tc_gemm=1)
+    # a rank model predicting the cap: the update is cap-bound and sketched
+    p = np.zeros(eng.n_params, dtype=np.float32)
+    p[-1] = 1.0
+    eng.set_rank_params(p, enable=True)
+    m = eng.mps([a.astype(np.complex64), b.astype(np.complex64)], dtype=np.complex64)
+    st = m.apply_2q(g, 1, 1e-6, chi)
+    out = (st, m.site(1).astype(complex), m.site(2).astype(complex))
+    m.free()
+    eng.close()
+    return out
+
+
 @pytest.mark.parametrize("chi", [200, 512, 1024])
 def test_orthonormalisations_give_the_same_truncation(engine, monkeypatch, chi):
-    """The sketch basis orthonormalised in one cooperative launch (16 rows
-    per CTA in shared memory, grid barriers between the Gram-Schmidt
-    phases), by the one-launch cluster CholeskyQR per block (the block's rows
-    in the shared memory of 16 CTAs, or of 8) with the three projection
-    kernels, and by the four-kernel passes gives the same truncation of a
-    rank-deficient theta' at the chi cap: same rank, error within 1.1x of the
-    exact SVD's, values within 1e-4 of the largest.  chi = 200 sketches 264
-    columns (a last block of 8) over 400 rows (the last CTA's rows padded)."""
-    import oracle as O
+    """The sketch bases of a capped update orthonormalised in one cooperative
+    launch (16 rows per CTA in shared memory, grid barriers between the
+    Gram-Schmidt phases), by the cluster CholeskyQR per block (the block's
+    rows in the shared memory of 16 CTAs, or of 8) with the three projection
+    kernels, and by the four-kernel passes: the same rank, truncation errors
+    within 1.1x of the exact SVD's, unit left factors, kept values within
+    1e-4 of the largest.  chi = 200 sketches 264 columns (a last block of 8)
+    over 400 rows (the last CTA's rows padded)."""
     rng = np.random.default_rng(5 * chi)
     a, b, _ = O.decay_theta_factors(chi, rng, 0.97)
     g = O.haar_unitary(rng)
-    th = O.apply_gate_to_theta(O.theta_of(a.astype(np.complex64).astype(complex), b.astype(np.complex64).astype(complex)),
-                               g, chi, chi).astype(np.complex64)
-    ref = np.linalg.svd(th.astype(complex), compute_uv=False)
+    a64, b64 = a.astype(np.complex64).astype(complex), b.astype(np.complex64).astype(complex)
+    th = O.apply_gate_to_theta(O.theta_of(a64, b64), g, chi, chi)
+    ref = np.linalg.svd(th, compute_uv=False)
     exact = np.sqrt(np.sum(ref[chi:] ** 2))
     out = {}
     for name, (one, cluster) in ORTH_VARIANTS.items():
         if chi == 1024 and name == "four-kernel":
             continue  # the slowest variant adds nothing at this size
-        monkeypatch.setenv("QT_ORTH_ONE_LAUNCH", one)
-        monkeypatch.setenv("QT_CHOLQR_CLUSTER", cluster)
-        eng = engine.Engine(mode="chosen", tc_gemm=1)
-        U, S, Vh, k, _ = eng.truncated_svd(th, 1e-6, chi_max=chi, mode="chosen")
-        eng.close()
-        assert k == chi, name
-        err = np.linalg.norm((U * S) @ Vh - th.astype(complex))
+        st, s1, s2 = capped_update(engine, a, b, g, chi, {"QT_ORTH_ONE_LAUNCH": one, "QT_CHOLQR_CLUSTER": cluster},
+                                   monkeypatch)
+        assert st["sketch_size"] > 0 and not st["fallback"] and st["rank"] == chi, (name, st)
+        err = np.linalg.norm(th - O.theta_of(s1, s2))
         assert err <= 1.1 * exact, (name, err, exact)
-        assert np.abs(U.conj().T @ U - np.eye(k)).max() <= 1e-4, name
-        out[name] = S[:k]
-    for name, s in out.items():
-        assert np.abs(out["one-launch"] - s).max() <= 1e-4 * ref[0], name
+        A = s1.reshape((2 * chi, -1), order="F")
+        assert np.abs(A.conj().T @ A - np.eye(chi)).max() <= 2e-6 * np.sqrt(2 * chi), name
+        out[name] = np.linalg.norm(s2.reshape((chi, -1), order="F"), axis=1)
+    for name, sv in out.items():
+        assert np.abs(out["one-launch"] - sv).max() <= 1e-4 * ref[0], name
 
 
-def test_one_launch_orthonormalisation_is_reproducible(engine):
-    """Fixed summation orders: two runs of the same sketch give the same
-    factors bit for bit."""
-    import oracle as O
+def test_one_launch_orthonormalisation_is_reproducible(engine, monkeypatch):
+    """Fixed summation orders: two capped updates of the same bond give the
+    same sites bit for bit."""
     rng = np.random.default_rng(77)
     a, b, _ = O.decay_theta_factors(256, rng, 0.97)
-    th = O.apply_gate_to_theta(O.theta_of(a, b), O.haar_unitary(rng), 256, 256).astype(np.complex64)
-    outs = []
-    for _ in range(2):
-        eng = engine.Engine(mode="chosen", tc_gemm=1)
-        outs.append(eng.truncated_svd(th, 1e-6, chi_max=256, mode="chosen"))
-        eng.close()
-    (U0, S0, V0, k0, _), (U1, S1, V1, k1, _) = outs
-    assert k0 == k1
-    assert np.array_equal(S0, S1) and np.array_equal(U0, U1) and np.array_equal(V0, V1)
+    g = O.haar_unitary(rng)
+    r0 = capped_update(engine, a, b, g, 256, {}, monkeypatch)
+    r1 = capped_update(engine, a, b, g, 256, {}, monkeypatch)
+    assert r0[0]["sketch_size"] > 0 and r0[0]["rank"] == r1[0]["rank"]
+    assert np.array_equal(r0[1], r1[1]) and np.array_equal(r0[2], r1[2])
 
 
 @pytest.mark.parametrize("shape", [(2048, 1152), (1100, 1003), (700, 1400)])
