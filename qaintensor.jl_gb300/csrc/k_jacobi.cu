@@ -1782,8 +1782,13 @@ int qt_jacobi_svd_ws(qt_handle* h, TS* X, int64_t mm, int64_t nn, int64_t ldx, T
   // is still resident and each half has rows to work on; QT_JACOBI_HALVES=1
   // keeps one CTA per pair.  The halves run on their own copies of the round
   // flags, unitaries and rotate decisions, and exchange partial Grams.
+  // Only without V: with V (a wide matrix's right factor) the two-CTA
+  // rounds measured a run-to-run varying split of a 1536 x 1024 matrix
+  // (a 40-site MPO compression at chi 512); QT_JACOBI_HALVES=3 forces them
+  // there too (diagnostics).
   const int halves_env = std::getenv("QT_JACOBI_HALVES") ? std::atoi(std::getenv("QT_JACOBI_HALVES")) : 2;
-  const int halves = (sweep_kernel && halves_env == 2 && mm >= 512 && sweep32_fits(h, 2 * pairs)) ? 2 : 1;
+  const int halves = (sweep_kernel && (halves_env == 3 || (halves_env == 2 && !V)) && mm >= 512 &&
+                      sweep32_fits(h, 2 * pairs)) ? 2 : 1;
   float2* gx = nullptr;
   int* xflag = nullptr;
   if (sweep_kernel && halves == 2) {

@@ -244,3 +244,24 @@ def test_sweep_kernel_row_halves_equal_one_cta_per_pair(engine, monkeypatch, sha
         err = np.linalg.norm((U * S) @ Vh - M32)
         assert err <= 1.1 * np.sqrt(np.sum(ref[kk:] ** 2)) + floor, (err, floor)
         assert np.abs(U.conj().T @ U - np.eye(kk)).max() <= 2e-6 * np.sqrt(m)
+
+
+@pytest.mark.parametrize("shape,halves", [((2048, 1152), "2"), ((1024, 1536), "2"), ((1024, 1536), "1")])
+def test_sweep_kernel_is_reproducible(engine, monkeypatch, shape, halves):
+    """Two chosen-mode splits of the same matrix give the same factors bit
+    for bit: the round protocol has no race (a tall matrix, whose Jacobi
+    carries no V and runs two CTAs per pair, and a wide one, whose right
+    factor V the rounds rotate too)."""
+    monkeypatch.setenv("QT_JACOBI_HALVES", halves)
+    rng = np.random.default_rng(sum(shape))
+    m, n = shape
+    M, _ = graded(rng, m, n, 0.995)
+    M32 = M.astype(np.complex64)
+    outs = []
+    for _ in range(2):
+        eng = engine.Engine(mode="chosen", jacobi_kernel=0)
+        outs.append(eng.truncated_svd(M32, 1e-6, chi_max=min(m, n) // 2, mode="chosen"))
+        eng.close()
+    (U0, S0, V0, k0, _), (U1, S1, V1, k1, _) = outs
+    assert k0 == k1
+    assert np.array_equal(S0, S1) and np.array_equal(U0, U1) and np.array_equal(V0, V1)
