@@ -1287,7 +1287,8 @@ int qt_orthonormalize(qt_handle* h, C* Y, int64_t m, int64_t l, bool range_only)
     // chi = 1024 bench bond the truncation error is unchanged (1.00014 of
     // the exact split either way) and the update 4.8 ms faster.
     const char* env = std::getenv("QT_ORTH_RANGE");
-    const int light = range_only ? (env ? std::atoi(env) : 2) : 0;
+    const char* fenv = std::getenv("QT_ORTH_FINAL");
+    const int light = range_only ? (env ? std::atoi(env) : 2) : (fenv ? std::atoi(fenv) : 0);
     if (ncta > 0) return orth_one_launch(h, Y, m, l, ncta, ldy, smem, std::min(2, std::max(0, light)));
   }
   qt_scratch s(h);
