@@ -1283,7 +1283,7 @@ jacobi_sweep32_kernel(float2* __restrict__ xb0, float2* __restrict__ xb1, int64_
         int it = 0;
         for (; it < spin; it++) {
           if (ld_acquire_gpu(done + target) >= g - 1) break;
-          if (*(volatile int*)(flags + QT_FLAG_ABORT)) { it = spin; break; }
+          if ((it & 7) == 7 && *(volatile int*)(flags + QT_FLAG_ABORT)) { it = spin; break; }
           __nanosleep(64);
         }
         if (it >= spin) { gave_up = 1; atomicExch(flags + QT_FLAG_ABORT, 1); }
@@ -1459,7 +1459,7 @@ jacobi_sweep32_kernel(float2* __restrict__ xb0, float2* __restrict__ xb1, int64_
         int it = 0;
         for (; it < spin; it++) {
           if (ld_acquire_gpu(xflag + (size_t)(1 - hf) * pairs + q) >= g) break;
-          if (*(volatile int*)(flags + QT_FLAG_ABORT)) { it = spin; break; }
+          if ((it & 7) == 7 && *(volatile int*)(flags + QT_FLAG_ABORT)) { it = spin; break; }
           __nanosleep(32);
         }
         if (it >= spin) { gave = 1; atomicExch(flags + QT_FLAG_ABORT, 1); }

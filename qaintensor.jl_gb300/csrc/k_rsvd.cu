@@ -886,7 +886,7 @@ __device__ bool op_barrier(const OrthArgs& a, int& epoch) {
       int it = 0;
       for (; it < a.spin; it++) {
         if (op_ld_acquire(a.bar + 2) >= epoch) break;
-        if (*(volatile int*)(a.bar + 1)) { it = a.spin; break; }
+        if ((it & 7) == 7 && *(volatile int*)(a.bar + 1)) { it = a.spin; break; }
         __nanosleep(20);
       }
       if (it >= a.spin) {
