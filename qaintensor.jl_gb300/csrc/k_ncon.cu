@@ -204,7 +204,10 @@ int contract_device(qt_handle* h, const qt_tensor* A, const qt_tensor* B, int nc
         rc = qt_cgemm<double2>(h, QT_OP_N, QT_OP_N, M, N, K, make_double2(1, 0), Am, M, Bm, K, make_double2(0, 0),
                                (double2*)Ct->data, M);
     }
-    if (rc == QT_OK) rc = qt_check_status(h);
+    {
+      const int st = qt_check_status(h);  // a timed-out device wait is the cause of what followed
+      if (st != QT_OK) rc = st;
+    }
     if (rc == QT_OK && cudaStreamSynchronize(h->stream) != cudaSuccess)
       rc = qt_fail(h, QT_ECUDA, "contract_pair: device error");
   }

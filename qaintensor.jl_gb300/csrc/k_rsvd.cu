@@ -834,11 +834,12 @@ struct OrthArgs {
   float2* coef;   // [l][BW] summed coefficients
   float2* gpart;  // [ncta][BW * BW] Gram partials
   float4* gsum;   // [BW * BW] summed Gram (re hi, re lo, im hi, im lo)
-  int* bar;       // [0] arrivals, [1] abort word, [2] the last completed barrier
+  int* bar;       // [0] arrivals, [1] abort word, [2] the last completed barrier, [3] the test hook's word
   int* flags;     // QT_FLAG_CHOL
   int* status;    // sticky device status
   int spin;
   int light;      // 0: as above; 1: no third CholeskyQR pass; 2: also one projection only
+  int stall;      // test hook: CTA 0 first waits this many polls on a word nothing sets
   unsigned long long* phase_ns;  // optional: CTA 0's time per phase (diagnostics)
 };
 
@@ -1143,6 +1144,25 @@ __global__ void __launch_bounds__(OP_NT, 1) orth_one_launch_kernel(OrthArgs a) {
   }
   __syncthreads();
   op_mark(a, 9);  // staging (the mark before it is the kernel start)
+  if (a.stall > 0) {
+    // test hook (QT_ORTH_STALL_TEST): CTA 0 waits a bounded number of polls
+    // on bar[3], which nothing sets, then gives up like a barrier wait; the
+    // other CTAs leave their first barrier through the abort word
+    int gave = 0;
+    if (blockIdx.x == 0 && t == 0) {
+      int it = 0;
+      for (; it < a.stall; it++) {
+        if (op_ld_acquire(a.bar + 3) != 0) break;
+        __nanosleep(20);
+      }
+      if (it >= a.stall) {
+        gave = 1;
+        atomicExch(a.bar + 1, 1);
+        atomicExch(a.status, 2);
+      }
+    }
+    if (__syncthreads_or(gave)) return;
+  }
   int epoch = 0;
   for (int j0 = 0; j0 < a.l; j0 += BW) {
     const int b = min(BW, a.l - j0);
@@ -1210,12 +1230,14 @@ int orth_one_launch(qt_handle* h, float2* Y, int64_t m, int64_t l, int ncta, int
   QT_TRY(s.get(&a.coef, (size_t)l * BW));
   QT_TRY(s.get(&a.gpart, (size_t)ncta * BW * BW));
   QT_TRY(s.get(&a.gsum, (size_t)BW * BW));
-  QT_TRY(s.get(&a.bar, 3));
+  QT_TRY(s.get(&a.bar, 4));
   a.flags = h->d_flags;
   a.status = h->d_status;
   if (!a.status) QT_TRY(s.get(&a.status, 1));
   a.spin = OP_SPIN;
   a.light = light;
+  // QT_ORTH_STALL_TEST=N (tests only): CTA 0 gives up a wait after N polls
+  a.stall = std::getenv("QT_ORTH_STALL_TEST") ? std::atoi(std::getenv("QT_ORTH_STALL_TEST")) : 0;
   a.phase_ns = nullptr;
   // QT_ORTH_PHASES=1 prints CTA 0's time per phase after each launch
   static const bool phases = std::getenv("QT_ORTH_PHASES") != nullptr;
@@ -1223,7 +1245,7 @@ int orth_one_launch(qt_handle* h, float2* Y, int64_t m, int64_t l, int ncta, int
     QT_TRY(s.get(&a.phase_ns, 11));
     QT_CHECK_CUDA(h, cudaMemsetAsync(a.phase_ns, 0, 11 * sizeof(unsigned long long), h->stream));
   }
-  QT_CHECK_CUDA(h, cudaMemsetAsync(a.bar, 0, 3 * sizeof(int), h->stream));
+  QT_CHECK_CUDA(h, cudaMemsetAsync(a.bar, 0, 4 * sizeof(int), h->stream));
   if (a.status != h->d_status) QT_CHECK_CUDA(h, cudaMemsetAsync(a.status, 0, sizeof(int), h->stream));
   cudaLaunchConfig_t lc = {};
   lc.gridDim = dim3((unsigned)ncta);

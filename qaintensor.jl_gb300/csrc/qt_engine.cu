@@ -29,7 +29,8 @@ int qt_check_status(qt_handle* h) {
   QT_CHECK_CUDA(h, cudaStreamSynchronize(h->stream));
   if (!hs) return QT_OK;
   QT_CHECK_CUDA(h, cudaMemsetAsync(h->d_status, 0, sizeof(int), h->stream));
-  return qt_fail(h, QT_ETIMEOUT, "tc gemm: a pipeline wait timed out");
+  return qt_fail(h, QT_ETIMEOUT, hs == 2 ? "orthonormalize: a grid barrier wait timed out"
+                                          : "tc gemm: a pipeline wait timed out");
 }
 
 int qt_dmalloc(qt_handle* h, void** p, size_t bytes) {
@@ -851,6 +852,20 @@ int svd_split_cusolver(qt_handle* h, double2* theta, int64_t m, int64_t n, doubl
 }
 
 
+// The exact FP64 split that decides where the chosen mode's FP32 split
+// cannot (an uncertified rank, an unsettled Jacobi, a sketch that lost
+// rank).  M (an FP64 copy) is overwritten.  For min(m, n) >= 512 it is
+// cuSOLVER's zgesvd (1.76 s against 7.2 s for the engine's FP64 Jacobi at
+// 2048 x 2048 on GB300, where FP64 runs at 1/64 of the FP32 rate); below,
+// the FP64 Jacobi.  QT_FALLBACK_JACOBI=1 keeps the Jacobi at every size.
+template <typename TO>
+int svd_split_exact64(qt_handle* h, double2* M, int64_t m, int64_t n, double cutoff, int chi_max, TO** A, TO** B,
+                      SvdOut* o) {
+  static const bool jacobi_only = std::getenv("QT_FALLBACK_JACOBI") && std::atoi(std::getenv("QT_FALLBACK_JACOBI"));
+  if (!jacobi_only && std::min(m, n) >= 512) return svd_split_cusolver<TO>(h, M, m, n, cutoff, chi_max, A, B, o);
+  return svd_split_jacobi<double2, TO>(h, M, m, n, cutoff, chi_max, false, A, B, o);
+}
+
 // Chosen mode: FP32-level products, randomized range finder sized by the
 // predicted rank, FP32-storage one-sided Jacobi on the small projected matrix
 // (FP64 Gram/angles); exact FP64 SVD as fallback when the tail rule needs
@@ -1041,7 +1056,7 @@ int qt_split_device(qt_handle* h, int dtype, const void* M, int64_t m, int64_t n
       QT_TRY(s.get(&Mc, (size_t)m * n));
       QT_TRY(qt_convert(h, M, QT_C64, Mc, QT_C128, m * n));
       o = SvdOut();
-      rc = svd_split_jacobi<double2, float2>(h, Mc, m, n, cutoff, chi_max, false, (float2**)A, (float2**)B, &o);
+      rc = svd_split_exact64<float2>(h, Mc, m, n, cutoff, chi_max, (float2**)A, (float2**)B, &o);
       if (rc != QT_OK) rc = QT_EFALLBACK_FAILED;
     }
   } else {
@@ -1054,7 +1069,11 @@ int qt_split_device(qt_handle* h, int dtype, const void* M, int64_t m, int64_t n
     else
       rc = svd_split_jacobi<double2, float2>(h, Mc, m, n, cutoff, chi_max, false, (float2**)A, (float2**)B, &o);
   }
-  if (rc == QT_OK) rc = qt_check_status(h);
+  {
+    // a bounded device wait that gave up is the cause of whatever followed it
+    const int st = qt_check_status(h);
+    if (st != QT_OK) rc = st;
+  }
   if (rc != QT_OK) {
     qt_dfree(h, *A);
     qt_dfree(h, *B);
@@ -1119,7 +1138,7 @@ static int update_impl(qt_handle* h, qt_mps* mps, int site, const double* G, dou
         double2* th64;
         QT_TRY(s.get(&th64, (size_t)m * n));
         QT_TRY(qt_theta_gate(h, mps->dtype, mps->site[site], mps->site[site + 1], cl, cm, cr, G, 0, th64));
-        rc = svd_split_jacobi<double2, TO>(h, th64, m, n, cutoff, chi_max, false, &An, &Bn, &o);
+        rc = svd_split_exact64<TO>(h, th64, m, n, cutoff, chi_max, &An, &Bn, &o);
         if (rc != QT_OK) rc = QT_EFALLBACK_FAILED;
       }
     } else {
@@ -1130,7 +1149,11 @@ static int update_impl(qt_handle* h, qt_mps* mps, int site, const double* G, dou
       else rc = svd_split_jacobi<double2, TO>(h, th, m, n, cutoff, chi_max, false, &An, &Bn, &o);
     }
   }
-  if (rc == QT_OK) rc = qt_check_status(h);
+  {
+    // a bounded device wait that gave up is the cause of whatever followed it
+    const int st = qt_check_status(h);
+    if (st != QT_OK) rc = st;
+  }
   if (rc != QT_OK) {
     qt_dfree(h, An);
     qt_dfree(h, Bn);
@@ -1295,7 +1318,7 @@ int host_truncated_svd64(qt_handle* h, const double2* M64, const float2* M32, in
       QT_TRY(s.get(&dM64, (size_t)m * n));
       QT_CHECK_CUDA(h, cudaMemcpyAsync(dM64, M64, sizeof(double2) * m * n, cudaMemcpyHostToDevice, h->stream));
       o = SvdOut();
-      rc = svd_split_jacobi<double2, double2>(h, dM64, m, n, cutoff, chi_max, false, &A, &B, &o);
+      rc = svd_split_exact64<double2>(h, dM64, m, n, cutoff, chi_max, &A, &B, &o);
       if (rc != QT_OK) rc = QT_EFALLBACK_FAILED;
     }
   } else {
@@ -1305,7 +1328,11 @@ int host_truncated_svd64(qt_handle* h, const double2* M64, const float2* M32, in
     rc = (mode == QT_MODE_CUSOLVER) ? svd_split_cusolver<double2>(h, dM, m, n, cutoff, chi_max, &A, &B, &o)
                                     : svd_split_jacobi<double2, double2>(h, dM, m, n, cutoff, chi_max, false, &A, &B, &o);
   }
-  if (rc == QT_OK) rc = qt_check_status(h);
+  {
+    // a bounded device wait that gave up is the cause of whatever followed it
+    const int st = qt_check_status(h);
+    if (st != QT_OK) rc = st;
+  }
   if (rc == QT_OK) {
     U->resize((size_t)m * o.k);
     Vh->resize((size_t)o.k * n);

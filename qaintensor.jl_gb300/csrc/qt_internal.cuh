@@ -91,7 +91,8 @@ struct qt_mps {
 
 int qt_fail(qt_handle* h, int code, const std::string& msg);
 // Reads and clears the sticky device status (after the work queued so far):
-// QT_ETIMEOUT when a tensor-core GEMM's pipeline wait gave up.
+// QT_ETIMEOUT when a tensor-core GEMM's pipeline wait (status 1) or a grid
+// barrier of the one-launch orthonormalisation (status 2) gave up.
 int qt_check_status(qt_handle* h);
 
 #define QT_CHECK_CUDA(h, call)                                                    \
