@@ -1658,8 +1658,10 @@ static int launch_sweep32(qt_handle* h, int pairs, float2* x0, float2* x1, int64
                           double nu_rel2, const double* xnorm2, float2* wbuf, int* rotbuf, int* done, int max_inner,
                           float keep2, float* dnorm, unsigned long long* phase_ns, int halves, float2* gx,
                           int* xflag) {
-  // row split of the two halves of a pair: at a multiple of 32 rows
-  const int row_mid = ((mm / 2 + 31) / 32) * 32, vrow_mid = ((nn / 2 + 31) / 32) * 32;
+  // row split of the two halves of a pair: at a multiple of 32 rows, never
+  // past the last row (a V of fewer than 32 rows belongs to half 0 alone)
+  const int row_mid = std::min(((mm / 2 + 31) / 32) * 32, mm);
+  const int vrow_mid = std::min(((nn / 2 + 31) / 32) * 32, nn);
   cudaLaunchConfig_t lc = {};
   lc.gridDim = dim3((unsigned)(pairs * halves));
   lc.blockDim = dim3(NTG);
@@ -1782,13 +1784,8 @@ int qt_jacobi_svd_ws(qt_handle* h, TS* X, int64_t mm, int64_t nn, int64_t ldx, T
   // is still resident and each half has rows to work on; QT_JACOBI_HALVES=1
   // keeps one CTA per pair.  The halves run on their own copies of the round
   // flags, unitaries and rotate decisions, and exchange partial Grams.
-  // Only without V: with V (a wide matrix's right factor) the two-CTA
-  // rounds measured a run-to-run varying split of a 1536 x 1024 matrix
-  // (a 40-site MPO compression at chi 512); QT_JACOBI_HALVES=3 forces them
-  // there too (diagnostics).
   const int halves_env = std::getenv("QT_JACOBI_HALVES") ? std::atoi(std::getenv("QT_JACOBI_HALVES")) : 2;
-  const int halves = (sweep_kernel && (halves_env == 3 || (halves_env == 2 && !V)) && mm >= 512 &&
-                      sweep32_fits(h, 2 * pairs)) ? 2 : 1;
+  const int halves = (sweep_kernel && halves_env == 2 && mm >= 512 && sweep32_fits(h, 2 * pairs)) ? 2 : 1;
   float2* gx = nullptr;
   int* xflag = nullptr;
   if (sweep_kernel && halves == 2) {

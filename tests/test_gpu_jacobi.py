@@ -265,3 +265,29 @@ def test_sweep_kernel_is_reproducible(engine, monkeypatch, shape, halves):
     (U0, S0, V0, k0, _), (U1, S1, V1, k1, _) = outs
     assert k0 == k1
     assert np.array_equal(S0, S1) and np.array_equal(U0, U1) and np.array_equal(V0, V1)
+
+
+@pytest.mark.parametrize("shape", [(2, 600), (8, 600), (31, 1024), (40, 600)])
+def test_two_cta_rounds_with_a_short_v(engine, monkeypatch, shape):
+    """A wide matrix whose right factor V has fewer rows than the 32-row
+    granule of the row split (the small splits at the ends of an MPS
+    compression): half 0 owns all of V's rows and half 1 none, and the split
+    matches LAPACK and the one-CTA rounds."""
+    rng = np.random.default_rng(sum(shape))
+    m, n = shape
+    M, _ = graded(rng, m, n, 0.9)
+    M32 = M.astype(np.complex64)
+    ref = np.linalg.svd(M32.astype(np.complex128), compute_uv=False)
+    floor = 4 * np.sqrt(max(m, n)) * 5.96e-8 * np.linalg.norm(M32)
+    out = []
+    for halves in ("2", "1"):
+        monkeypatch.setenv("QT_JACOBI_HALVES", halves)
+        eng = engine.Engine(mode="chosen", jacobi_kernel=0)
+        U, S, Vh, k, _ = eng.truncated_svd(M32, 50 * floor, mode="chosen")
+        eng.close()
+        err = np.linalg.norm((U * S) @ Vh - M32)
+        assert err <= 1.1 * np.sqrt(np.sum(ref[k:] ** 2)) + floor, (halves, err, floor)
+        assert np.abs(S[:k] - ref[:k]).max() <= 2 * floor, halves
+        assert np.abs(U.conj().T @ U - np.eye(k)).max() <= 2e-6 * np.sqrt(max(m, n)), halves
+        out.append((k, S))
+    assert out[0][0] == out[1][0]
