@@ -53,9 +53,11 @@ typedef enum {
   QT_MODE_CHOSEN = 1,    /* complex64: FP32-level products (tcgen05 split-TF32x3),
                             randomized range finder sized by the rank predictor,
                             FP32-storage Jacobi split with FP64 norms and tail sums;
-                            the exact FP64 split as fallback, also whenever the rank
-                            decision at the caller's cutoff lies below the FP32
-                            resolution and no certificate holds (qt_cert_counters) */
+                            the exact FP64 split as fallback (cuSOLVER zgesvd from
+                            min(m, n) = 512, the FP64 Jacobi below), also whenever
+                            the rank decision at the caller's cutoff lies below the
+                            FP32 resolution and no certificate holds
+                            (qt_cert_counters) */
   QT_MODE_CUSOLVER = 2   /* cross-check: FP64 GEMM + cuSOLVER zgesvd (library) */
 } qt_mode;
 
