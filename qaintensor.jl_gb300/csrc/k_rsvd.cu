@@ -1307,10 +1307,13 @@ int qt_orthonormalize(qt_handle* h, C* Y, int64_t m, int64_t l, bool range_only)
     // one projection and two CholeskyQR passes per block (QT_ORTH_RANGE=2,
     // the default; 1 keeps both projections, 0 all three passes).  At the
     // chi = 1024 bench bond the truncation error is unchanged (1.00014 of
-    // the exact split either way) and the update 4.8 ms faster.
+    // the exact split either way) and the update 4.8 ms faster.  The final
+    // basis keeps both projections and drops the third pass (QT_ORTH_FINAL=1,
+    // the default; 0 restores it): a second CholeskyQR after the shifted one
+    // already leaves the block orthonormal to a few u.
     const char* env = std::getenv("QT_ORTH_RANGE");
     const char* fenv = std::getenv("QT_ORTH_FINAL");
-    const int light = range_only ? (env ? std::atoi(env) : 2) : (fenv ? std::atoi(fenv) : 0);
+    const int light = range_only ? (env ? std::atoi(env) : 2) : (fenv ? std::atoi(fenv) : 1);
     if (ncta > 0) return orth_one_launch(h, Y, m, l, ncta, ldy, smem, std::min(2, std::max(0, light)));
   }
   qt_scratch s(h);
