@@ -1306,8 +1306,9 @@ int qt_orthonormalize(qt_handle* h, C* Y, int64_t m, int64_t l, bool range_only)
     // iteration needs to be well conditioned, not orthonormal to rounding:
     // one projection and two CholeskyQR passes per block (QT_ORTH_RANGE=2,
     // the default; 1 keeps both projections, 0 all three passes).  At the
-    // chi = 1024 bench bond the truncation error is unchanged (1.00014 of
-    // the exact split either way) and the update 4.8 ms faster.  The final
+    // chi = 1024 bench bond that leaves the truncation error unchanged
+    // (1.00014 of the exact split with a three-pass final basis) and saves
+    // 4.8 ms per update.  The final
     // basis keeps both projections and drops the third pass (QT_ORTH_FINAL=1,
     // the default; 0 restores it): a second CholeskyQR after the shifted one
     // already leaves the block orthonormal to a few u.
