@@ -1296,7 +1296,7 @@ template int qt_gaussian<float2>(qt_handle*, float2*, int64_t, int64_t, int64_t,
 template int qt_gaussian<double2>(qt_handle*, double2*, int64_t, int64_t, int64_t, uint64_t);
 
 template <typename C>
-int qt_orthonormalize(qt_handle* h, C* Y, int64_t m, int64_t l, bool range_only) {
+int qt_orthonormalize(qt_handle* h, C* Y, int64_t m, int64_t l, int use) {
   if (l > m) return qt_fail(h, QT_EINVAL, "orthonormalize: more columns than rows");
   if constexpr (std::is_same<C, float2>::value) {
     int ldy = 0;
@@ -1308,13 +1308,16 @@ int qt_orthonormalize(qt_handle* h, C* Y, int64_t m, int64_t l, bool range_only)
     // the default; 1 keeps both projections, 0 all three passes).  At the
     // chi = 1024 bench bond that leaves the truncation error unchanged
     // (1.00014 of the exact split with a three-pass final basis) and saves
-    // 4.8 ms per update.  The final
-    // basis keeps both projections and drops the third pass (QT_ORTH_FINAL=1,
-    // the default; 0 restores it): a second CholeskyQR after the shifted one
-    // already leaves the block orthonormal to a few u.
+    // 4.8 ms per update.  The final basis of a sketch keeps both
+    // projections and drops the third pass (QT_ORTH_FINAL=1, the default; 0
+    // restores it): a second CholeskyQR after the shifted one already leaves
+    // the block orthonormal to a few u, and the split that follows projects
+    // theta' exactly (B' = A'^H theta').  A basis kept as such (an MPS site)
+    // takes all passes.
     const char* env = std::getenv("QT_ORTH_RANGE");
     const char* fenv = std::getenv("QT_ORTH_FINAL");
-    const int light = range_only ? (env ? std::atoi(env) : 2) : (fenv ? std::atoi(fenv) : 1);
+    const int light = use == QT_ORTH_USE_RANGE ? (env ? std::atoi(env) : 2)
+                      : use == QT_ORTH_USE_SKETCH ? (fenv ? std::atoi(fenv) : 1) : 0;
     if (ncta > 0) return orth_one_launch(h, Y, m, l, ncta, ldy, smem, std::min(2, std::max(0, light)));
   }
   qt_scratch s(h);
@@ -1381,5 +1384,5 @@ int qt_orthonormalize(qt_handle* h, C* Y, int64_t m, int64_t l, bool range_only)
   }
   return QT_OK;
 }
-template int qt_orthonormalize<float2>(qt_handle*, float2*, int64_t, int64_t, bool);
-template int qt_orthonormalize<double2>(qt_handle*, double2*, int64_t, int64_t, bool);
+template int qt_orthonormalize<float2>(qt_handle*, float2*, int64_t, int64_t, int);
+template int qt_orthonormalize<double2>(qt_handle*, double2*, int64_t, int64_t, int);

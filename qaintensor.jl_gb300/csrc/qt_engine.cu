@@ -955,12 +955,12 @@ int svd_split_chosen(qt_handle* h, float2* theta, int64_t m, int64_t n, double c
   // range finder: Y = theta^H Omega, q rounds of subspace iteration
   QT_TRY(qt_gaussian<float2>(h, om, m, l, m, h->cfg.seed + 0x9E37ull * (++h->sketch_counter)));
   QT_TRY(qt_gemm_any(h, QT_OP_C, QT_OP_N, n, l, m, one, theta, m, om, m, zero, Y, n));
-  QT_TRY(qt_orthonormalize<float2>(h, Y, n, l, h->cfg.power_iters > 0));
+  QT_TRY(qt_orthonormalize<float2>(h, Y, n, l, h->cfg.power_iters > 0 ? QT_ORTH_USE_RANGE : QT_ORTH_USE_SKETCH));
   for (int q = 0; q < h->cfg.power_iters; q++) {
     QT_TRY(qt_gemm_any(h, QT_OP_N, QT_OP_N, m, l, n, one, theta, m, Y, n, zero, Z, m));
-    QT_TRY(qt_orthonormalize<float2>(h, Z, m, l, true));
+    QT_TRY(qt_orthonormalize<float2>(h, Z, m, l, QT_ORTH_USE_RANGE));
     QT_TRY(qt_gemm_any(h, QT_OP_C, QT_OP_N, n, l, m, one, theta, m, Z, m, zero, Y, n));
-    QT_TRY(qt_orthonormalize<float2>(h, Y, n, l));
+    QT_TRY(qt_orthonormalize<float2>(h, Y, n, l, q + 1 < h->cfg.power_iters ? QT_ORTH_USE_RANGE : QT_ORTH_USE_SKETCH));
   }
   {
     // a Cholesky pivot that vanished means the sketch held fewer than l

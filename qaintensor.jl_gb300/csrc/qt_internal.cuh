@@ -274,8 +274,14 @@ template <typename C>
 int qt_gaussian(qt_handle* h, C* out, int64_t rows, int64_t cols, int64_t ld, uint64_t seed);
 // Block classical Gram-Schmidt with re-orthogonalisation, intra-block shifted
 // CholeskyQR2 (FP64 Gram / Cholesky): Y (m x l, ld m) -> orthonormal columns.
+// What an orthonormalised FP32 basis is for (the one-launch kernel's passes
+// per 32-column block): an orthonormal basis kept as such (project, shifted
+// CholeskyQR, project, two CholeskyQR passes), the final basis of a sketch
+// (one CholeskyQR pass fewer) and a range carried to the next product of a
+// power iteration (one projection, two CholeskyQR passes).
+enum { QT_ORTH_USE_BASIS = 0, QT_ORTH_USE_SKETCH = 1, QT_ORTH_USE_RANGE = 2 };
 template <typename C>
-int qt_orthonormalize(qt_handle* h, C* Y, int64_t m, int64_t l, bool range_only = false);
+int qt_orthonormalize(qt_handle* h, C* Y, int64_t m, int64_t l, int use = QT_ORTH_USE_BASIS);
 
 // k_ncon.cu ------------------------------------------------------------------
 // device buffer of a qt_tensor (column-major, its dtype's element)
