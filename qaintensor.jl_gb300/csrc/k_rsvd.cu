@@ -795,15 +795,17 @@ int block_cholqr(qt_handle* h, C* Yb, int64_t m, int b, bool shifted, double2* d
 // CTA c keeps rows 16 c .. 16 c + 15 of Y (all l columns, zero-padded) in
 // shared memory from start to end, and the steps of the block Gram-Schmidt
 // above (project, shifted CholeskyQR, project, CholeskyQR, CholeskyQR per
-// 32-column block; three CholeskyQR passes for the first block) become
-// phases between grid barriers:
+// 32-column block; three CholeskyQR passes for the first block; fewer
+// passes for the lighter uses, OrthArgs::light) become phases between grid
+// barriers:
 //   projection of block j0 .. j0 + 31 against the j0 columns before it:
 //     (1) the CTA's partial coefficients Y[rows, :j0]^H Y[rows, block] in
 //         FP32 over its 16 rows, to part[c];                      barrier
-//     (2) CTA c adds the partials of its slice of the j0 x 32 coefficients,
-//         CTAs in order, to coef;                                 barrier
+//     (2) CTA c adds the partials of its slice of the j0 x 32 coefficients
+//         in a fixed order (warp w over CTAs w S .. w S + S - 1, then the
+//         eight warp sums), to coef;                              barrier
 //     (3) every CTA subtracts Y[rows, :j0] coef from its rows of the block,
-//         the coefficients staged through shared memory 64 rows at a time;
+//         the coefficients streamed through a six-chunk ring of 32 rows;
 //   CholeskyQR pass:
 //     (1) the CTA's partial Gram of the block (FP32 over its rows) to
 //         gpart[c];                                               barrier
@@ -813,10 +815,11 @@ int block_cholqr(qt_handle* h, C* Yb, int64_t m, int b, bool shifted, double2* d
 //         (cq_factor) and replaces its rows of the block by rows R^{-1}.
 // The rows go back to global memory once, at the end.  Sums run in a fixed
 // order, so the result is reproducible for a given m.  The barrier is a
-// monotone arrival counter; every wait is bounded, and a wait that gives up
-// sets an abort word (ending the other CTAs' waits) and the handle's sticky
-// device status (2).  Data written by other CTAs is read past L1
-// (ld.global.cg / cp.async.cg).
+// monotone arrival counter whose last arriving CTA publishes the barrier's
+// number; every wait is bounded, and a wait that gives up sets an abort
+// word (ending the other CTAs' waits) and the handle's sticky device status
+// (2).  Data written by other CTAs is read past L1 (ld.global.cg /
+// cp.async.cg).
 // ---------------------------------------------------------------------------
 constexpr int OP_NT = 256;     // threads per CTA
 constexpr int OP_R = 16;       // rows per CTA
