@@ -6,9 +6,13 @@
 // block orthonormalised by CholeskyQR passes -- the first one shifted
 // (Fukaya, Kannan, Nakatsukasa, Zhang, Yamamoto 2020) so that numerically
 // rank-deficient blocks still factor, and a third one for an FP32 basis.  The
-// basis is stored in the element type of Y.  Two CholeskyQR implementations:
-//   - FP32 blocks of up to 4096 rows: one thread-block cluster launch per run
-//     of passes (cholqr_cluster_kernel).  The block's rows stay in shared
+// basis is stored in the element type of Y.  Three implementations:
+//   - FP32 bases of up to 2368 rows (whose rows fit the shared memory of one
+//     CTA per 16 rows): the whole orthonormalisation in one cooperative
+//     launch (orth_one_launch_kernel), grid barriers between its phases.
+//   - Other FP32 bases, blocks of up to 4096 rows: per block the projection
+//     kernels and one thread-block cluster launch per run of CholeskyQR
+//     passes (cholqr_cluster_kernel).  The block's rows stay in shared
 //     memory; the Gram is summed in FP32 tiles and float-float across row
 //     groups and CTAs, and R and R^{-1} are formed in FP32.
 //   - FP64 blocks and taller FP32 blocks: four launches per pass (the Gram in
