@@ -1038,7 +1038,9 @@ pair_apply32_kernel(float2* __restrict__ X, int64_t ldx, int mm, float2* __restr
 // in place by pair_apply32_kernel after the last sweep.
 //
 // With halves = 2 each pair is served by two CTAs, CTA 2q + h holding rows
-// [row_lo(h), row_hi(h)) of the pair's columns (and the matching rows of V).
+// [row_lo(h), row_hi(h)) of the pair's columns (and the matching rows of V;
+// both splits at a multiple of 32 rows, clamped to the matrix, so a V of
+// fewer than 32 rows belongs to half 0 alone).
 // A row half reads and writes only its own rows, so each half runs the round
 // protocol above on its own copies of the round flags, unitaries and rotate
 // decisions (done, wbuf, rotbuf offset by h); the two halves of a pair meet
